@@ -1,0 +1,118 @@
+// gbpt_host.h -- host-side preparation of the per-frame / per-scene records
+// that the per-ray arithmetic of gbpt_math.h consumes.  Used by libgbpt and
+// by the CPU oracle so both see the same constants.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+
+#include "../../include/gbpt.h"
+#include "gbpt_math.h"
+
+namespace gb {
+
+// Per-material constants of principledMaterial.h:178-252 (mon2lin, Ctint,
+// Cspec0, Csheen, anisotropic alphas, the remapped roughness of :158 and the
+// GTR1 normalisation of :186-192), from a material_t-like description.
+static inline MaterialRec make_material(const gb_material& m, const gb_principled_params* params) {
+    MaterialRec r;
+    std::memset(&r, 0, sizeof(r));
+    if (m.principled < 0) {
+        r.kind = MAT_LAMBERT;
+        for (int k = 0; k < 3; ++k) r.diffuse[k] = m.diffuse[k];
+        r.opacity = 1.0f;
+        return r;
+    }
+    const gb_principled_params& p = params[m.principled];
+    r.kind = MAT_PRINCIPLED;
+    for (int k = 0; k < 3; ++k) r.diffuse[k] = p.color[k];
+    r.metallic = p.metallic; r.subsurface = p.subsurface; r.roughness = p.roughness;
+    r.sheen = p.sheen; r.clearcoat = p.clearcoat; r.opacity = p.opacity;
+    float aspect = (float)std::sqrt(1.0 - (double)p.anisotropic * .9);
+    float r2 = p.roughness * p.roughness;
+    r.ax = std::max(.001f, r2 / aspect);
+    r.ay = std::max(.001f, r2 * aspect);
+    float roughg = (float)((double)(r.ax * r.ay) * .5 + .5);
+    roughg = roughg * roughg;
+    r.roughg2 = roughg * roughg;
+    float cdlin[3];
+    for (int k = 0; k < 3; ++k) cdlin[k] = (float)std::pow((double)p.color[k], 2.2);
+    float cdlum = (float)(.3 * cdlin[0] + .6 * cdlin[1] + .1 * cdlin[2]);
+    float ctint[3];
+    for (int k = 0; k < 3; ++k) ctint[k] = cdlum > 0 ? cdlin[k] / cdlum : 1.0f;
+    float spec08 = (float)((double)p.specular * .08);
+    for (int k = 0; k < 3; ++k) {
+        r.cdlin[k] = cdlin[k];
+        r.csheen[k] = (1.0f - p.sheen_tint) * 1.0f + p.sheen_tint * ctint[k];
+        float st = (1.0f - p.specular_tint) * 1.0f + p.specular_tint * ctint[k];
+        float a = spec08 * st;
+        r.cspec0[k] = (1.0f - p.metallic) * a + p.metallic * cdlin[k];
+    }
+    float a = (1.0f - p.clearcoat_gloss) * 0.1f + p.clearcoat_gloss * 0.001f;
+    float a2 = a * a;
+    r.cc_a = a;
+    r.cc_a2m1 = a2 - 1.0f;
+    r.cc_pilog = kPi * (float)std::log((double)a2);
+    return r;
+}
+
+// Flattened device record (kMaterialFloats floats).
+static inline void pack_material(const MaterialRec& r, float* f) {
+    std::memset(f, 0, sizeof(float) * kMaterialFloats);
+    f[0] = (float)r.kind;
+    f[1] = r.diffuse[0]; f[2] = r.diffuse[1]; f[3] = r.diffuse[2];
+    f[4] = r.metallic; f[5] = r.subsurface; f[6] = r.roughness; f[7] = r.sheen;
+    f[8] = r.clearcoat; f[9] = r.opacity; f[10] = r.ax; f[11] = r.ay; f[12] = r.roughg2;
+    for (int k = 0; k < 3; ++k) { f[13 + k] = r.cdlin[k]; f[16 + k] = r.csheen[k]; f[19 + k] = r.cspec0[k]; }
+    f[22] = r.cc_a; f[23] = r.cc_a2m1; f[24] = r.cc_pilog;
+}
+
+// gi::light rect light with its fixed basis (arealight-sampler-cpu.cpp:70-73).
+static inline LightRec make_light(const gb_light& l) {
+    LightRec r;
+    r.center = mk(l.center[0], l.center[1], l.center[2]);
+    r.dir = mk(l.dir[0], l.dir[1], l.dir[2]);
+    r.col = mk(l.col[0], l.col[1], l.col[2]);
+    r.w = l.wh[0]; r.h = l.wh[1];
+    r.right = make_tangential(mk(1.0f, 0.0f, 0.0f), r.dir);
+    r.up = make_tangential(mk(0.0f, 1.0f, 0.0f), r.dir);
+    r.power = l.power >= 0.0f ? l.power : rect_light_power(r.w, r.h, r.col);
+    return r;
+}
+
+// hybrid-pt.cpp:74-78
+static inline float overall_power(const LightRec* L, int n) {
+    float p = 0.0f;
+    for (int i = 0; i < n; ++i) p += L[i].power;
+    return p;
+}
+
+// Per-frame camera constants (raygen.cu:71-90).  aspect = w/h; the half
+// field of view tangent is taken in double on the host.
+static inline CameraRec make_camera(const gb_camera& c, int w, int h) {
+    CameraRec r;
+    r.pos = mk(c.pos[0], c.pos[1], c.pos[2]);
+    r.view = mk(c.dir[0], c.dir[1], c.dir[2]);
+    v3 up = mk(c.up[0], c.up[1], c.up[2]);
+    camera_frame(r.view, up, &r.U, &r.V, &r.W);
+    double half = (double)c.fovy_deg / 2.0;
+    r.height = (float)std::tan(3.14159265358979323846 * half / 180.0);
+    float aspect = (float)w / (float)h;
+    r.width = aspect * r.height;
+    r.aperture = c.aperture;
+    r.focus = c.focus_distance;
+    r.w = w; r.h = h;
+    return r;
+}
+
+static inline ShadeParams make_shade_params(const gb_render_desc& d) {
+    ShadeParams s;
+    s.ray_offset = d.ray_offset;
+    s.shadow_offset = d.shadow_offset;
+    s.background = mk(d.background[0], d.background[1], d.background[2]);
+    s.rr_start = d.rr_start;
+    s.seed = d.seed;
+    return s;
+}
+
+}  // namespace gb

@@ -1,0 +1,563 @@
+// gbpt_math.h -- per-ray arithmetic of the globillum path-tracing hot path.
+//
+// One definition of every formula the path evaluates (camera ray, triangle
+// test, light sample, principled/Lambert BRDF sample + eval, throughput
+// update), compiled both into the sm_103a kernels (nvcc, -fmad=false) and
+// into the CPU oracle (g++, -ffp-contract=off).  Only IEEE-exact operations
+// are used (+ - * / sqrt and explicit fmaf); the two transcendentals the
+// per-ray path needs (sin/cos of 2*pi*u) are evaluated by a quadrant
+// reduction plus the Taylor series of sin/cos(pi/2 * r) in Horner form, so
+// host and device produce the same bits.  Per-material constants that need
+// pow/log (mon2lin, GTR1 normalisation) are precomputed on the host.
+//
+// Reference formulas followed (file:line in kiselgra/globillum src/):
+//   camera ray          raygen.cu:61-118 (setup_jittered_dof_shirley)
+//   area-light sample   arealight-sampler-cpu.cpp:25-143
+//   shade / bounce      hybrid-pt.cpp:330-371, 421-448, 450-584
+//   principled BRDF     principledMaterial.h:27-401
+//   Lambert BRDF        simpleMaterial.h:162-193, materialBase.h:16-24
+//   Halton              util.cpp:22-32
+//   moving average      util-kernels.cu:17-25
+// Helpers that live in the (absent) rta/libhyb libraries -- the triangle
+// test, make_tangent_frame, make_tangential, barycentric interpolation,
+// normalize_vec3f, cross -- are defined here once (see each function).
+#pragma once
+
+#include <stdint.h>
+#include <math.h>
+#include <float.h>
+
+#if defined(__CUDACC__)
+#define GB_HD __host__ __device__ __forceinline__
+#else
+#define GB_HD static inline
+#endif
+
+namespace gb {
+
+// ---------------------------------------------------------------- vectors --
+struct v3 { float x, y, z; };
+
+GB_HD v3 mk(float x, float y, float z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+GB_HD v3 operator+(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+GB_HD v3 operator-(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+GB_HD v3 operator-(v3 a) { return mk(-a.x, -a.y, -a.z); }
+GB_HD v3 operator*(v3 a, v3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+GB_HD v3 operator*(float s, v3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+GB_HD v3 operator*(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+GB_HD v3 operator/(v3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+GB_HD v3 operator/(v3 a, v3 b) { return mk(a.x / b.x, a.y / b.y, a.z / b.z); }
+
+// dot product in the reference's operator| order (left to right, no fma).
+GB_HD float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// cross product as rta's cross_vec3f (plain products, no fma).
+GB_HD v3 cross(v3 a, v3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+GB_HD float length(v3 a) { return sqrtf(dot(a, a)); }
+// libhyb normalize_vec3f: divide by the length.
+GB_HD v3 normalize_div(v3 a) { float l = length(a); return a / l; }
+// principledMaterial.h:34-37 normalize: multiply by 1/sqrt.
+GB_HD v3 normalize_rcp(v3 a) { float b = 1.0f / sqrtf(dot(a, a)); return a * b; }
+
+// fused forms used only by the ray/triangle and ray/box tests.
+GB_HD float fdot(v3 a, v3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+GB_HD v3 fcross(v3 a, v3 b) {
+    return mk(fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x)));
+}
+
+GB_HD float clampf(float a, float lo, float hi) { return fminf(fmaxf(a, lo), hi); }
+GB_HD float sqr(float a) { return a * a; }
+
+static const float kPi = 3.14159265358979f;
+static const float kInvPi = 0.318309873342514f;
+
+// --------------------------------------------------------- sin/cos(2*pi*u) --
+// Quadrant reduction: 4u = q + r with q integral and r in [-1/2, 1/2] (both
+// steps exact in binary floating point), then sin/cos(pi/2 * r) from the
+// Taylor series of sin and cos (coefficients (-1)^k (pi/2)^n / n!, rounded
+// to float) in Horner form with fmaf.  Error below 2 ulp for u in [0, 1].
+GB_HD void sincos_2pi(float u, float* s, float* c) {
+    float u4 = u * 4.0f;
+    float q = rintf(u4);
+    float r = u4 - q;
+    int qi = ((int)q) & 3;
+    float r2 = r * r;
+    float sp = fmaf(r2, -3.598843250074424e-06f, 0.00016044118092395365f);
+    sp = fmaf(r2, sp, -0.004681753925979137f);
+    sp = fmaf(r2, sp, 0.07969262450933456f);
+    sp = fmaf(r2, sp, -0.6459640860557556f);
+    sp = fmaf(r2, sp, 1.5707963705062866f);
+    float sn = r * sp;
+    float cp = fmaf(r2, 4.710874748070637e-07f, -2.520204179745633e-05f);
+    cp = fmaf(r2, cp, 0.0009192602592520416f);
+    cp = fmaf(r2, cp, -0.020863480865955353f);
+    cp = fmaf(r2, cp, 0.25366950035095215f);
+    cp = fmaf(r2, cp, -1.2337005138397217f);
+    float cs = fmaf(r2, cp, 1.0f);
+    float so, co;
+    if (qi == 0) { so = sn; co = cs; }
+    else if (qi == 1) { so = cs; co = -sn; }
+    else if (qi == 2) { so = -sn; co = -cs; }
+    else { so = -cs; co = sn; }
+    *s = so; *c = co;
+}
+
+// ------------------------------------------------------------ tangent frame --
+// make_tangent_frame (libhyb, absent): orthonormal basis around a unit N by
+// Duff et al., "Building an Orthonormal Basis, Revisited", JCGT 6(1) 2017.
+GB_HD void make_tangent_frame(v3 n, v3* T, v3* B) {
+    float sign = copysignf(1.0f, n.z);
+    float a = -1.0f / (sign + n.z);
+    float b = n.x * n.y * a;
+    *T = mk(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    *B = mk(b, sign + n.y * n.y * a, -n.y);
+}
+// make_tangential(v, N) (libhyb, absent): local z-up vector v to world space
+// around N (arealight-sampler-cpu.cpp:72-73, :93 use it this way).
+GB_HD v3 make_tangential(v3 v, v3 n) {
+    v3 T, B; make_tangent_frame(n, &T, &B);
+    return (v.x * T + v.y * B) + v.z * n;
+}
+GB_HD v3 to_tangent(v3 v, v3 T, v3 B, v3 N) { return mk(dot(v, T), dot(v, B), dot(v, N)); }
+GB_HD v3 from_tangent(v3 v, v3 T, v3 B, v3 N) { return (v.x * T + v.y * B) + v.z * N; }
+// materialBase.h:36-38 reflectR; libhyb reflect uses the same convention.
+GB_HD v3 reflect(v3 v, v3 n) { return v - (2.0f * dot(v, n)) * n; }
+
+// barycentric_coord / barycentric_interpolation (rta, absent):
+// bc = (1 - beta - gamma, beta, gamma); value = bc.x*a + bc.y*b + bc.z*c.
+GB_HD v3 bary(float beta, float gamma, v3 a, v3 b, v3 c) {
+    float w = (1.0f - beta) - gamma;
+    return (w * a + beta * b) + gamma * c;
+}
+
+// ------------------------------------------------------ ray/triangle test --
+// Moller-Trumbore (intersect_tri_opt in rta is not available; this is the
+// published test of Moller & Trumbore 1997, double sided, strict t > 0).
+// e1 = v1 - v0 and e2 = v2 - v0 are passed precomputed (same float bits as
+// computing them from the corners).
+GB_HD bool intersect_tri(v3 o, v3 d, v3 v0, v3 e1, v3 e2, float* t, float* beta, float* gamma) {
+    v3 p = fcross(d, e2);
+    float det = fdot(e1, p);
+    if (det == 0.0f) return false;
+    float inv = 1.0f / det;
+    v3 s = o - v0;
+    float u = fdot(s, p) * inv;
+    if (!(u >= 0.0f && u <= 1.0f)) return false;
+    v3 q = fcross(s, e1);
+    float v = fdot(d, q) * inv;
+    if (!(v >= 0.0f && u + v <= 1.0f)) return false;
+    float tt = fdot(e2, q) * inv;
+    if (!(tt > 0.0f)) return false;
+    *t = tt; *beta = u; *gamma = v;
+    return true;
+}
+
+// closest-hit acceptance: lexicographic minimum of (t, canonical id) over
+// all triangles with 0 < t <= t_max; the result is independent of the BVH
+// layout and traversal order (tracers.cu:113 keeps `is.t < closest.t &&
+// is.t <= t_max`, which is the same except at exact ties in t).
+GB_HD bool closer(float t, uint32_t id, float best_t, uint32_t best_id) {
+    return t < best_t || (t == best_t && id < best_id);
+}
+
+// ----------------------------------------------------------- sample streams --
+// util.cpp:22-32
+GB_HD float halton(int index, int base) {
+    float result = 0.0f;
+    float f = 1.0f / float(base);
+    int i = index;
+    while (i > 0) {
+        result += f * float(i % base);
+        i = i / base;
+        f = f / float(base);
+    }
+    return result;
+}
+
+// Integer hash for the Russian-roulette extension (not in the reference):
+// "lowbias32" integer finaliser (C. Wellons, hash-prospector, 2018).
+GB_HD uint32_t hash32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+GB_HD float rr_uniform(uint32_t seed, uint32_t pixel, uint32_t path, uint32_t bounce) {
+    uint32_t h = hash32(seed ^ hash32(pixel ^ hash32(path * 0x9e3779b9U ^ hash32(bounce + 0x632be5abU))));
+    return float(h >> 8) * (1.0f / 16777216.0f);
+}
+
+// ----------------------------------------------------------------- camera --
+// Per-frame constants of setup_jittered_dof_shirley (raygen.cu:61-118); the
+// host fills them once (W, U, V are the same for every ray).
+struct CameraRec {
+    v3 pos, view, U, V, W;
+    float width, height;      // aspect*tan(fovy/2), tan(fovy/2)
+    float aperture, focus;
+    int w, h;
+};
+
+GB_HD void camera_frame(v3 view, v3 up, v3* U, v3* V, v3* W) {
+    *W = view / length(view);
+    v3 TxW = cross(up, *W);
+    *U = TxW / length(TxW);
+    *V = cross(*W, *U);
+}
+
+// jitter = (rnd.x, rnd.y) of the jitter stream; lens = aperture sample
+// (zero when aperture == 0, where it is multiplied by zero in the reference).
+GB_HD void camera_ray(const CameraRec& c, int x, int y, float jx_r, float jy_r, float lens_x, float lens_y,
+                      v3* org, v3* dir) {
+    float jx = float(x) + jx_r;
+    float jy = float(y) + jy_r;
+    float u_s = ((jx) / (float)c.w) * 2.0f - 1.0f;
+    float v_s = ((jy) / (float)c.h) * 2.0f - 1.0f;
+    u_s = c.width * u_s;
+    v_s = c.height * v_s;
+    v3 d = c.U * u_s;
+    d = d + c.V * v_s;
+    d = d + c.W;
+    d = normalize_div(d);
+    v3 focal = c.pos + (d * (1.0f / dot(d, c.view))) * c.focus;
+    v3 jp = (c.pos + (c.U * lens_x) * c.aperture) + (c.V * lens_y) * c.aperture;
+    d = focal - jp;
+    *dir = normalize_div(d);
+    *org = jp;
+}
+
+// ----------------------------------------------------------------- lights --
+// gi::light (lights.h:94-154) restricted to rectangular lights; right/up are
+// make_tangential((1,0,0)|(0,1,0), dir) (arealight-sampler-cpu.cpp:72-73),
+// fixed per light and filled by the host.
+struct LightRec {
+    v3 center, dir, col, right, up;
+    float w, h, power;
+};
+
+// lights.cpp:92: power = w*h*(r+g+b)*.333
+GB_HD float rect_light_power(float w, float h, v3 col) {
+    return (float)((double)(w * h * (col.x + col.y + col.z)) * .333);
+}
+
+// Light pick (arealight-sampler-cpu.cpp:32-39).  The reference reads
+// lights[n] when the accumulated power falls short of choice by rounding;
+// here the index stops at n-1.
+GB_HD int pick_light(const LightRec* L, int n, float overall_power, float rnd_z) {
+    float choice = rnd_z * overall_power;
+    float acc = 0.0f;
+    int l = 0;
+    while (l < n - 1 && choice > acc + L[l].power) {
+        acc += L[l].power;
+        ++l;
+    }
+    return l;
+}
+
+// Rectangular-light sample at a hit (arealight-sampler-cpu.cpp:65-86, 114-119).
+// P, N: interpolated hit point and (unnormalised) normal.  Outputs the
+// shadow ray and potential_sample_contribution.
+GB_HD void rect_light_sample(const LightRec& l, float overall_power, v3 P, v3 N, float rx, float ry,
+                             float shadow_offset, v3* so, v3* sd, float* smax, v3* psc) {
+    float offx = (rx - 0.5f) * l.w;
+    float offy = (ry - 0.5f) * l.h;
+    v3 ls = (l.center + offx * l.right) + offy * l.up;
+    v3 dir = ls - P;
+    float len = length(dir);
+    dir = dir / len;
+    float ndotl = fmaxf(dot(N, dir), 0.0f);
+    float light_cos = fmaxf(dot(l.dir, -dir), 0.0f);
+    float factor = l.w * l.h * ndotl * light_cos / (len * len);
+    v3 contribution = l.col * factor;
+    dir = normalize_div(dir);
+    *so = P + shadow_offset * dir;
+    *sd = dir;
+    *smax = len;
+    *psc = contribution * (overall_power / l.power);
+}
+
+// -------------------------------------------------------------- materials --
+// material_t (material.h:142-184) + PrincipledBRDFParameters
+// (principledParameters.h:7-24), flattened with the per-material constants
+// of principledMaterial.h:178-252 precomputed on the host.
+enum { MAT_LAMBERT = 0, MAT_PRINCIPLED = 1 };
+struct MaterialRec {
+    int kind;
+    float diffuse[3];          // Lambert: diffuse_color; principled: parameters->color
+    float metallic, subsurface, roughness, sheen, clearcoat, opacity;
+    float ax, ay, roughg2;     // principledMaterial.h:179-181, :158, :166
+    float cdlin[3];            // mon2lin(color)           :226
+    float csheen[3];           // mix(1, Ctint, sheenTint) :276
+    float cspec0[3];           // :231
+    float cc_a, cc_a2m1, cc_pilog;  // GTR1 constants        :186-192, :241
+};
+static const int kMaterialFloats = 32;  // padded device record size
+
+// Inverse of pack_material (gbpt_host.h): record from its 32-float form.
+GB_HD MaterialRec unpack_material(const float* f) {
+    MaterialRec r;
+    r.kind = (int)f[0];
+    r.diffuse[0] = f[1]; r.diffuse[1] = f[2]; r.diffuse[2] = f[3];
+    r.metallic = f[4]; r.subsurface = f[5]; r.roughness = f[6]; r.sheen = f[7];
+    r.clearcoat = f[8]; r.opacity = f[9]; r.ax = f[10]; r.ay = f[11]; r.roughg2 = f[12];
+    for (int k = 0; k < 3; ++k) { r.cdlin[k] = f[13 + k]; r.csheen[k] = f[16 + k]; r.cspec0[k] = f[19 + k]; }
+    r.cc_a = f[22]; r.cc_a2m1 = f[23]; r.cc_pilog = f[24];
+    return r;
+}
+
+enum { LOBE_DIFFUSE = 0, LOBE_SPECULAR = 1, LOBE_DISNEY_REFLECTION = 2,
+       LOBE_SPECULAR_REFLECTION = 3, LOBE_SPECULAR_TRANSMISSION = 4 };
+
+GB_HD float schlick(float u) {
+    float m = clampf(1.0f - u, 0.0f, 1.0f);
+    float m2 = m * m;
+    return m2 * m2 * m;
+}
+GB_HD float mixf(float x, float y, float s) { return (1.0f - s) * x + s * y; }
+
+// materialBase.h:16-24
+GB_HD v3 cosine_sample_hemisphere(float u, float v) {
+    float r = sqrtf(u);
+    float sn, cs; sincos_2pi(v, &sn, &cs);
+    return mk(r * cs, r * sn, sqrtf(fmaxf(0.0f, 1.0f - u)));
+}
+
+// principledMaterial.h:64-69
+GB_HD float smithG_GGX(float ndv, float alphaG) {
+    float a = alphaG * alphaG;
+    float b = ndv * ndv;
+    return 1.0f / (ndv + sqrtf(a + b - a * b));
+}
+// principledMaterial.h:76-80 (Walter et al. G1 with the Xi indicator)
+GB_HD float G1(v3 v, v3 m, v3 n, float a2, float tanv) {
+    float fac = (dot(v, m) / dot(v, n)) > 0.0f ? 1.0f : 0.0f;
+    return fac * 2.0f / (1.0f + sqrtf(1.0f + a2 * tanv * tanv));
+}
+
+// principledMaterial.h:121-176 with T=(1,0,0), B=(0,1,0), n=(0,0,1) in
+// tangent space (:369-371).  Returns the Walter weight (>= 0.01 or NaN).
+GB_HD float sample_gtr2_aniso(float u, float v, float ax, float ay, float roughg2, v3 V, v3* Lout) {
+    float sn, cs; sincos_2pi(u, &sn, &cs);
+    float fac = sqrtf(v / (1.0f - v));
+    v3 t = mk(ax * cs, 0.0f, 0.0f);
+    t = t + mk(0.0f, ay * sn, 0.0f);
+    v3 h = normalize_rcp(fac * t + mk(0.0f, 0.0f, 1.0f));
+    v3 n = mk(0.0f, 0.0f, 1.0f);
+    v3 L = reflect(V, h);
+    if (dot(L, n) < 0.0f) L = -1.0f * L;
+    float dotLm = dot(L, h);
+    float dotVm = dot(V, h);
+    float tanL = sqrtf(1.0f - dotLm * dotLm) / dotLm;
+    float tanV = sqrtf(1.0f - dotVm * dotVm) / dotVm;
+    float Gs = G1(L, h, n, roughg2, tanL) * G1(V, h, n, roughg2, tanV);
+    float w = (fabsf(dot(L, h)) * Gs) / (fabsf(dot(L, n)) * fabsf(dot(n, h)));
+    if (w < 0.01f) w = 0.01f;
+    *Lout = L;
+    return w;
+}
+
+// principledMaterial.h:86-118
+GB_HD v3 sample_glass(float u, v3 V, float ior, int* lobe) {
+    v3 n = mk(0.0f, 0.0f, 1.0f);
+    float c = dot(n, V);
+    float fresnel = schlick(c);
+    if (u > fresnel) {
+        *lobe = LOBE_SPECULAR_REFLECTION;
+        return -V;
+    }
+    float ti = 1.0f + ior * (c * c - 1.0f);
+    if (ti <= 0.0f) {
+        *lobe = LOBE_SPECULAR_REFLECTION;
+        return reflect(V, n);
+    }
+    *lobe = LOBE_SPECULAR_TRANSMISSION;
+    float sg = dot(V, n) > 0.0f ? 1.0f : -1.0f;
+    return (ior * c - sg * sqrtf(ti)) * n - ior * V;
+}
+
+GB_HD bool is_glass(const MaterialRec& m) { return m.kind == MAT_PRINCIPLED && m.opacity < 1.0f; }
+
+// materialBRDF::sample (material-wrapper.h:224-227) -> LambertianMaterial::sample
+// (simpleMaterial.h:183-186) or PrincipledMaterial::sample
+// (principledMaterial.h:354-390).  wo, wi in tangent space.
+GB_HD void material_sample(const MaterialRec& m, v3 wo, v3 rnd, v3* wi, float* pdf, int* lobe) {
+    if (m.kind == MAT_LAMBERT) {
+        v3 w = cosine_sample_hemisphere(rnd.x, rnd.y);
+        *wi = w;
+        *pdf = fabsf(w.z) * kInvPi;
+        *lobe = LOBE_DIFFUSE;
+        return;
+    }
+    if (m.opacity < 1.0f) {
+        *wi = sample_glass(rnd.x, wo, 1.9f, lobe);
+        *pdf = 1.0f;
+        return;
+    }
+    if (rnd.z < m.metallic) {
+        v3 L;
+        float p = sample_gtr2_aniso(rnd.x, rnd.y, m.ax, m.ay, m.roughg2, wo, &L);
+        *lobe = LOBE_DISNEY_REFLECTION;
+        *wi = L;
+        *pdf = p;
+        if (p == 0.0f || p != p) {
+            v3 w = cosine_sample_hemisphere(rnd.x, rnd.y);
+            *wi = w;
+            *lobe = LOBE_DIFFUSE;
+            *pdf = clampf(w.z, 0.0f, FLT_MAX) * kInvPi;
+        }
+        return;
+    }
+    v3 w = cosine_sample_hemisphere(rnd.x, rnd.y);
+    *wi = w;
+    *lobe = LOBE_DIFFUSE;
+    *pdf = fmaxf(w.z, 0.0f) * kInvPi;
+}
+
+// principledMaterial.h:254-301
+GB_HD v3 principled_diffuse(const MaterialRec& m, v3 V, v3 N, v3 L) {
+    float NdotL = dot(N, L);
+    float NdotV = dot(N, V);
+    if (NdotL < 0.0f || NdotV < 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    v3 H = normalize_rcp(L + V);
+    float LdotH = dot(L, H);
+    float FL = schlick(NdotL), FV = schlick(NdotV);
+    float Fd90 = 0.5f + 2.0f * LdotH * LdotH * m.roughness;
+    float Fd = mixf(1.0f, Fd90, FL) * mixf(1.0f, Fd90, FV);
+    float FH = schlick(LdotH);
+    float fs = FH * m.sheen;
+    v3 Fsheen = fs * mk(m.csheen[0], m.csheen[1], m.csheen[2]);
+    float Fss90 = LdotH * LdotH * m.roughness;
+    float Fss = mixf(1.0f, Fss90, FL) * mixf(1.0f, Fss90, FV);
+    float ss = 1.25f * (Fss * (1.0f / (NdotL + NdotV) - 0.5f) + 0.5f);
+    float k = kInvPi * mixf(Fd, ss, m.subsurface);
+    v3 dcol = (k * mk(m.cdlin[0], m.cdlin[1], m.cdlin[2]) + Fsheen) * (1.0f - m.metallic);
+    return dcol * NdotL;
+}
+
+// principledMaterial.h:210-252
+GB_HD v3 principled_specular(const MaterialRec& m, v3 V, v3 N, v3 L) {
+    float NdotL = dot(N, L);
+    float NdotV = dot(N, V);
+    if (NdotL < 0.0f || NdotV < 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    v3 H = normalize_rcp(L + V);
+    float NdotH = dot(N, H);
+    float LdotH = dot(L, H);
+    float FH = schlick(LdotH);
+    v3 Fs = (1.0f - FH) * mk(m.cspec0[0], m.cspec0[1], m.cspec0[2]) + FH * mk(1.0f, 1.0f, 1.0f);
+    float cg = 0.0f;
+    if (m.clearcoat > 0.0f) {
+        float Dr;
+        if (m.cc_a >= 1.0f) Dr = kInvPi;
+        else {
+            float t = 1.0f + m.cc_a2m1 * NdotH * NdotH;
+            Dr = m.cc_a2m1 / (m.cc_pilog * t);
+        }
+        float Fr = mixf(0.04f, 1.0f, FH);
+        float Gr = smithG_GGX(NdotL, 0.25f) * smithG_GGX(NdotV, 0.25f);
+        cg = 0.25f * m.clearcoat * Gr * Fr * Dr;
+    }
+    v3 sum = Fs + mk(cg, cg, cg);
+    return (sum * NdotL) * m.metallic;
+}
+
+// materialBRDF::evaluate (material-wrapper.h:228-232) with the lobe chosen by
+// the preceding sample() (principledMaterial.h:336-352); world space.
+GB_HD v3 material_eval(const MaterialRec& m, int lobe, v3 wo, v3 wi, v3 N) {
+    if (m.kind == MAT_LAMBERT)
+        return (mk(m.diffuse[0], m.diffuse[1], m.diffuse[2]) * kInvPi) * fabsf(dot(wi, N));
+    if (lobe == LOBE_DISNEY_REFLECTION) return principled_specular(m, wo, N, wi);
+    if (lobe == LOBE_SPECULAR_REFLECTION) return mk(1.0f, 1.0f, 1.0f);
+    if (lobe == LOBE_SPECULAR_TRANSMISSION) return mk(1.0f, 1.0f, 1.0f) * (1.0f / fabsf(dot(wi, N)));
+    return principled_diffuse(m, wo, N, wi);
+}
+
+// ------------------------------------------------------------ shade/bounce --
+// Parameters of compute_path_contribution_and_bounce that the reference hard
+// codes (hybrid-pt.cpp:45, :52, :551; arealight-sampler-cpu.cpp:115).
+struct ShadeParams {
+    float ray_offset;       // 0.3 in the reference
+    float shadow_offset;    // 0.9 in the reference
+    v3 background;          // (1,1,1), added for primary misses (NO_BACKGROUND)
+    int rr_start;           // Russian roulette from this bounce (extension); <0 = off
+    uint32_t seed;
+};
+
+struct ShadeOut {
+    v3 org, dir;     // next ray
+    v3 tp;           // new throughput
+    v3 accum_add;    // added to col_accum this bounce
+    bool alive;
+};
+
+// One pixel of compute_path_contribution_and_bounce (hybrid-pt.cpp:465-564)
+// for a valid hit.  P, Nraw: interpolated hit point / normal; ray_dir: the
+// ray direction; rnd: the path-stream draw; unoccluded: shadow result;
+// to_light, psc: the NEE outputs of this bounce.
+GB_HD ShadeOut shade_hit(const MaterialRec& m, v3 P, v3 Nraw, v3 ray_dir, v3 tp, v3 rnd,
+                         bool unoccluded, v3 to_light, v3 psc, const ShadeParams& sp,
+                         uint32_t pixel, uint32_t path, int bounce) {
+    ShadeOut o;
+    v3 org_dir = normalize_div(ray_dir);
+    v3 N = normalize_div(Nraw);
+    v3 T, B;
+    make_tangent_frame(N, &T, &B);
+    T = normalize_div(T);
+    B = normalize_div(B);
+    // sample_material (hybrid-pt.cpp:330-349)
+    v3 inv_org_dir = -1.0f * org_dir;
+    bool glass = is_glass(m);
+    if (dot(org_dir, N) > 0.0f) N = N * -1.0f;
+    v3 wo_ts = to_tangent(inv_org_dir, T, B, N);
+    v3 wi; float pdf; int lobe;
+    material_sample(m, wo_ts, rnd, &wi, &pdf, &lobe);
+    wi = from_tangent(wi, T, B, N);
+    wi = normalize_div(wi);
+    // evaluate_material (hybrid-pt.cpp:351-371)
+    o.accum_add = mk(0.0f, 0.0f, 0.0f);
+    if (!glass && unoccluded) {
+        v3 currTP = tp * psc;
+        v3 ld = normalize_div(to_light);
+        v3 bl = material_eval(m, lobe, inv_org_dir, ld, N);
+        v3 add = bl * currTP;
+        if (add.x == add.x && add.y == add.y && add.z == add.z) o.accum_add = add;
+    }
+    v3 brdf = material_eval(m, lobe, inv_org_dir, wi, N);
+    // next ray (hybrid-pt.cpp:550-562)
+    v3 Pn = glass ? P + sp.ray_offset * org_dir : P + sp.ray_offset * N;
+    o.org = Pn;
+    o.dir = wi;
+    v3 ntp = (tp * brdf) / pdf;
+    if (ntp.x > 1.0f) ntp.x = 1.0f;
+    if (ntp.y > 1.0f) ntp.y = 1.0f;
+    if (ntp.z > 1.0f) ntp.z = 1.0f;
+    o.alive = true;
+    // pdf == 0 or a NaN throughput would poison the pixel forever in the
+    // reference; such paths end here.
+    if (!(pdf > 0.0f) || ntp.x != ntp.x || ntp.y != ntp.y || ntp.z != ntp.z) {
+        o.alive = false;
+        ntp = mk(0.0f, 0.0f, 0.0f);
+    }
+    // Russian roulette (extension, off when rr_start < 0)
+    if (o.alive && sp.rr_start >= 0 && bounce >= sp.rr_start) {
+        float q = fmaxf(fmaxf(ntp.x, ntp.y), ntp.z);
+        q = clampf(q, 0.05f, 1.0f);
+        float u = rr_uniform(sp.seed, pixel, path, (uint32_t)bounce);
+        if (u >= q) { o.alive = false; ntp = mk(0.0f, 0.0f, 0.0f); }
+        else ntp = ntp / q;
+    }
+    o.tp = ntp;
+    return o;
+}
+
+// handle_no_hit (hybrid-pt.cpp:196-206, :567-575): primary misses are
+// recognised by throughput == (1,1,1); no sky light is modelled, so other
+// misses add throughput * 0.
+GB_HD v3 miss_contribution(v3 tp, const ShadeParams& sp) {
+    if (tp.x == 1.0f && tp.y == 1.0f && tp.z == 1.0f) return tp * sp.background;
+    return tp * mk(0.0f, 0.0f, 0.0f);
+}
+
+// util-kernels.cu:17-25
+GB_HD v3 combine_sample(v3 sofar, v3 sample, int k) {
+    return (float(k) * sofar + sample) / float(k + 1);
+}
+
+}  // namespace gb

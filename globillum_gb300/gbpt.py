@@ -1,0 +1,278 @@
+"""ctypes binding of libgbpt.so (include/gbpt.h).
+
+This is the Python form of the binding a reference-side maintainer would add
+(the C++ form is include/gb_hybrid_pt.h).  It loads the in-tree library and
+raises if it is missing: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libgbpt.so"
+
+GB_OK, GB_ERR_INVALID, GB_ERR_CUDA, GB_ERR_OOM, GB_ERR_TIMEOUT, GB_ERR_TRAVERSAL, GB_ERR_UNSUPPORTED = range(7)
+GB_LIGHT_RECT, GB_LIGHT_SKY = 0, 1
+GB_RNG_MRG32K3A_POOL, GB_RNG_HALTON_LIGHT = 0, 1
+
+F3 = C.c_float * 3
+
+
+class CtxDesc(C.Structure):
+    _fields_ = [("device", C.c_int), ("stream", C.c_void_p)]
+
+
+class PrincipledParams(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("metallic", "subsurface", "specular", "roughness", "specular_tint",
+                                          "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss",
+                                          "opacity", "transmiss")] + [("color", F3), ("tangent", F3)]
+
+
+class Material(C.Structure):
+    _fields_ = [("diffuse", F3), ("principled", C.c_int)]
+
+
+class Light(C.Structure):
+    _fields_ = [("type", C.c_int), ("power", C.c_float), ("center", F3), ("dir", F3), ("up", F3), ("col", F3),
+                ("wh", C.c_float * 2)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_triangles", C.c_int), ("positions", C.c_void_p), ("normals", C.c_void_p),
+                ("material_index", C.c_void_p), ("num_materials", C.c_int), ("materials", C.POINTER(Material)),
+                ("num_params", C.c_int), ("params", C.POINTER(PrincipledParams)), ("num_lights", C.c_int),
+                ("lights", C.POINTER(Light))]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_int), ("num_nodes", C.c_int), ("depth", C.c_int), ("binary_nodes", C.c_int),
+                ("build_ms", C.c_double), ("device_bytes", C.c_size_t), ("overall_light_power", C.c_float)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", F3), ("dir", F3), ("up", F3), ("fovy_deg", C.c_float), ("aperture", C.c_float),
+                ("focus_distance", C.c_float), ("eye_to_lens", C.c_float)]
+
+
+class RenderDesc(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("spp", C.c_int), ("max_bounces", C.c_int),
+                ("rng_mode", C.c_int), ("seed", C.c_uint32), ("ray_offset", C.c_float),
+                ("shadow_offset", C.c_float), ("background", F3), ("rr_start", C.c_int)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("t", C.c_float), ("beta", C.c_float), ("gamma", C.c_float), ("ref", C.c_uint32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("camera_rays", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("closest_node_visits", C.c_uint64), ("closest_tri_tests", C.c_uint64),
+                ("shadow_node_visits", C.c_uint64), ("shadow_tri_tests", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("render_ms", C.c_double), ("stage_ms", C.c_double * 4),
+                ("stage_launches", C.c_uint64 * 4), ("paths_done", C.c_int)]
+
+
+HIT_DTYPE = np.dtype([("t", "<f4"), ("beta", "<f4"), ("gamma", "<f4"), ("ref", "<u4")])
+
+# exported symbols of include/gbpt.h (checked by the CPU tests)
+EXPORTS = [
+    "gb_ctx_create", "gb_ctx_destroy", "gb_last_error", "gb_ctx_set_stream", "gb_scene_create", "gb_scene_destroy",
+    "gb_scene_get_info", "gb_render", "gb_render_begin", "gb_render_step", "gb_render_paths_done", "gb_render_read",
+    "gb_trace_closest", "gb_trace_any", "gb_generate_arealight_sample", "gb_compute_path_contribution_and_bounce",
+    "gb_mrg_pool", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
+]
+
+_lib = None
+
+
+def load_library(path: Path | str | None = None) -> C.CDLL:
+    """Loads libgbpt.so; raises FileNotFoundError when it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: run globillum_gb300.build.build_lib() first")
+    lib = C.CDLL(str(p))
+    vp, ip, fp = C.c_void_p, C.c_int, C.POINTER(C.c_float)
+    lib.gb_ctx_create.argtypes = [C.POINTER(CtxDesc), C.POINTER(vp)]
+    lib.gb_ctx_destroy.argtypes = [vp]
+    lib.gb_ctx_destroy.restype = None
+    lib.gb_last_error.argtypes = [vp]
+    lib.gb_last_error.restype = C.c_char_p
+    lib.gb_ctx_set_stream.argtypes = [vp, vp]
+    lib.gb_scene_create.argtypes = [vp, C.POINTER(SceneDesc), C.POINTER(vp)]
+    lib.gb_scene_destroy.argtypes = [vp]
+    lib.gb_scene_destroy.restype = None
+    lib.gb_scene_get_info.argtypes = [vp, C.POINTER(SceneInfo)]
+    lib.gb_render.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, ip]
+    lib.gb_render_instrumented.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, ip]
+    lib.gb_render_begin.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc)]
+    lib.gb_render_step.argtypes = [vp, ip]
+    lib.gb_render_paths_done.argtypes = [vp, C.POINTER(C.c_int)]
+    lib.gb_render_read.argtypes = [vp, vp, ip]
+    lib.gb_trace_closest.argtypes = [vp, vp, ip, vp, vp, vp, vp, ip]
+    lib.gb_trace_any.argtypes = [vp, vp, ip, vp, vp, vp, vp, ip]
+    lib.gb_generate_arealight_sample.argtypes = [vp, vp, ip, ip, C.c_float, vp, vp, vp, vp, vp, vp]
+    lib.gb_compute_path_contribution_and_bounce.argtypes = [vp, vp, ip, ip, C.POINTER(RenderDesc), vp, vp, vp, vp,
+                                                            vp, vp, vp, vp, vp, vp, ip, ip]
+    lib.gb_mrg_pool.argtypes = [vp, ip, C.c_uint32, ip, ip, vp]
+    lib.gb_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    lib.gb_layout_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.gb_ctx_set_stage_timing.argtypes = [vp, ip]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class GBError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gbpt error {code}: {msg}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f3(v) -> F3:
+    return F3(*[float(x) for x in v])
+
+
+def make_camera(cam: dict) -> Camera:
+    return Camera(_f3(cam["pos"]), _f3(cam["dir"]), _f3(cam["up"]), float(cam["fovy_deg"]),
+                  float(cam.get("aperture", 0.0)), float(cam.get("focus_distance", 970.0)),
+                  float(cam.get("eye_to_lens", 5.0)))
+
+
+def make_render_desc(r: dict) -> RenderDesc:
+    return RenderDesc(int(r["width"]), int(r["height"]), int(r["spp"]), int(r["max_bounces"]),
+                      int(r.get("rng_mode", GB_RNG_MRG32K3A_POOL)), int(r.get("seed", 0)),
+                      float(r.get("ray_offset", 0.3)), float(r.get("shadow_offset", 0.9)),
+                      _f3(r.get("background", (1.0, 1.0, 1.0))), int(r.get("rr_start", -1)))
+
+
+def make_scene_desc(scene) -> tuple[SceneDesc, list]:
+    """SceneDesc for a globillum_gb300.scenes.SceneData; returns (desc, keepalive)."""
+    pos = np.ascontiguousarray(scene.positions, dtype=np.float32)
+    nrm = None if scene.normals is None else np.ascontiguousarray(scene.normals, dtype=np.float32)
+    mid = np.ascontiguousarray(scene.material_index, dtype=np.int32)
+    mats = (Material * len(scene.materials))()
+    for i, m in enumerate(scene.materials):
+        mats[i] = Material(_f3(m["diffuse"]), int(m.get("principled", -1)))
+    params = (PrincipledParams * max(1, len(scene.params)))()
+    for i, p in enumerate(scene.params):
+        params[i] = PrincipledParams(*[float(p.get(k, d)) for k, d in (
+            ("metallic", 0), ("subsurface", 0), ("specular", 0), ("roughness", 0), ("specular_tint", 0),
+            ("anisotropic", 0), ("sheen", 0), ("sheen_tint", 0), ("clearcoat", 0), ("clearcoat_gloss", 0),
+            ("opacity", 1), ("transmiss", 1))], _f3(p.get("color", (0, 0, 0))), _f3(p.get("tangent", (0, 0, 0))))
+    lights = (Light * max(1, len(scene.lights)))()
+    for i, l in enumerate(scene.lights):
+        lights[i] = Light(int(l.get("type", GB_LIGHT_RECT)), float(l.get("power", -1.0)), _f3(l["center"]),
+                          _f3(l["dir"]), _f3(l.get("up", (0, 0, 1))), _f3(l["col"]),
+                          (C.c_float * 2)(*[float(x) for x in l["wh"]]))
+    d = SceneDesc(int(pos.shape[0]), _ptr(pos), _ptr(nrm), _ptr(mid), len(scene.materials), mats,
+                  len(scene.params), params, len(scene.lights), lights)
+    return d, [pos, nrm, mid, mats, params, lights]
+
+
+class Context:
+    """One gb_ctx (one device, one stream)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        rc = self.lib.gb_ctx_create(C.byref(CtxDesc(device, stream)), C.byref(self.h))
+        if rc != GB_OK:
+            raise GBError(rc, "gb_ctx_create failed")
+
+    def check(self, rc: int):
+        if rc != GB_OK:
+            raise GBError(rc, self.lib.gb_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.gb_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream: int | None):
+        self.check(self.lib.gb_ctx_set_stream(self.h, stream))
+
+    def scene(self, scene_data) -> "Scene":
+        return Scene(self, scene_data)
+
+    def stats(self) -> dict:
+        s = Stats()
+        self.check(self.lib.gb_get_stats(self.h, C.byref(s)))
+        d = {k: getattr(s, k) for k, _ in Stats._fields_}
+        d["stage_ms"] = list(s.stage_ms)
+        d["stage_launches"] = list(s.stage_launches)
+        return d
+
+    def set_stage_timing(self, on: bool):
+        self.check(self.lib.gb_ctx_set_stage_timing(self.h, 1 if on else 0))
+
+    def mrg_pool(self, npix: int, num_updates: int, first_update: int = 0, seed: int = 0) -> np.ndarray:
+        out = np.empty((num_updates, npix, 3), dtype=np.float32)
+        self.check(self.lib.gb_mrg_pool(self.h, npix, seed, first_update, num_updates, _ptr(out)))
+        return out
+
+
+class Scene:
+    """A resident gb_scene."""
+
+    def __init__(self, ctx: Context, scene_data):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        desc, self._keep = make_scene_desc(scene_data)
+        ctx.check(ctx.lib.gb_scene_create(ctx.h, C.byref(desc), C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.gb_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def info(self) -> dict:
+        i = SceneInfo()
+        self.ctx.check(self.ctx.lib.gb_scene_get_info(self.h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in SceneInfo._fields_}
+
+    def render(self, cam: dict, rdesc: dict, instrumented: bool = False, out: np.ndarray | None = None) -> np.ndarray:
+        rd = make_render_desc(rdesc)
+        if out is None:
+            out = np.empty((rd.height, rd.width, 3), dtype=np.float32)
+        fn = self.ctx.lib.gb_render_instrumented if instrumented else self.ctx.lib.gb_render
+        self.ctx.check(fn(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd), _ptr(out), 0))
+        return out
+
+    def render_device(self, cam: dict, rdesc: dict, out_ptr: int) -> None:
+        rd = make_render_desc(rdesc)
+        self.ctx.check(self.ctx.lib.gb_render(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd),
+                                              C.c_void_p(out_ptr), 1))
+
+    def trace_closest(self, orig: np.ndarray, dirs: np.ndarray, max_t: np.ndarray) -> np.ndarray:
+        o = np.ascontiguousarray(orig, dtype=np.float32)
+        d = np.ascontiguousarray(dirs, dtype=np.float32)
+        t = np.ascontiguousarray(max_t, dtype=np.float32)
+        n = t.shape[0]
+        hits = np.empty(n, dtype=HIT_DTYPE)
+        self.ctx.check(self.ctx.lib.gb_trace_closest(self.ctx.h, self.h, n, _ptr(o), _ptr(d), _ptr(t), _ptr(hits), 0))
+        return hits
+
+    def trace_any(self, orig: np.ndarray, dirs: np.ndarray, max_t: np.ndarray) -> np.ndarray:
+        o = np.ascontiguousarray(orig, dtype=np.float32)
+        d = np.ascontiguousarray(dirs, dtype=np.float32)
+        t = np.ascontiguousarray(max_t, dtype=np.float32)
+        n = t.shape[0]
+        occ = np.empty(n, dtype=np.uint8)
+        self.ctx.check(self.ctx.lib.gb_trace_any(self.ctx.h, self.h, n, _ptr(o), _ptr(d), _ptr(t), _ptr(occ), 0))
+        return occ

@@ -1,0 +1,244 @@
+/* gbpt.h -- C ABI of the GB300 path-tracing hot path (libgbpt.so).
+ *
+ * Drop-in boundary for globillum's `hybrid_pt` integrator: the library owns
+ * the device memory of a scene and of a frame, runs the whole progressive
+ * frame (camera rays, closest-hit, area-light sample, any-hit shadow ray,
+ * BRDF sample/eval, moving-average accumulation) as a wavefront of
+ * hand-written sm_103a kernels, and exposes the per-stage entry points the
+ * reference's hybrid bouncer calls on the CPU.  Plain C types only; every
+ * call returns a status code, no exception crosses the ABI, and
+ * gb_last_error() gives the message of the last failing call of a context.
+ * One context per host thread.
+ *
+ * Reference interfaces replaced (kiselgra/globillum, src/):
+ *   gi_algorithm / hybrid_pt          gi_algorithm.h:12-68, hybrid-pt.h:256-288
+ *   hybrid_pt::activate/compute/update hybrid-pt.cpp:65-174
+ *   hybrid_pt_bouncer (bounce loop)   hybrid-pt.h:16-253
+ *   rta::generate_arealight_sample    arealight-sampler-cpu.cpp:144-156
+ *   compute_path_contribution_and_bounce hybrid-pt.cpp:450-584
+ *   closest / any-hit tracers (rta bbvh-cuda) hl-main.cpp:375-385, tracers.cu:38-140
+ *   gi::cuda::generate_mt_pool_on_gpu / update_mt_pool util-kernels.cu:277-333
+ *   gi::cuda::generate_halton_pool_on_gpu util.cpp:38-51
+ */
+#ifndef GBPT_H
+#define GBPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+enum {
+    GB_OK = 0,
+    GB_ERR_INVALID = 1,     /* bad argument / handle / size                       */
+    GB_ERR_CUDA = 2,        /* a CUDA runtime call failed                         */
+    GB_ERR_OOM = 3,         /* device or host allocation failed                   */
+    GB_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up                 */
+    GB_ERR_TRAVERSAL = 5,   /* traversal stack or iteration bound exceeded         */
+    GB_ERR_UNSUPPORTED = 6  /* feature not available (e.g. no CUDA device)         */
+};
+
+typedef struct gb_ctx gb_ctx;
+typedef struct gb_scene gb_scene;
+
+/* --------------------------------------------------------------- context */
+typedef struct {
+    int device;             /* CUDA device ordinal                                */
+    void* stream;           /* cudaStream_t to launch on; NULL = library-owned    */
+} gb_ctx_desc;
+
+/* Creates a context on `device`.  Replaces the implicit global CUDA state of
+ * the reference (checked_cuda + cudaDeviceSynchronize after every launch). */
+int gb_ctx_create(const gb_ctx_desc* desc, gb_ctx** out);
+void gb_ctx_destroy(gb_ctx* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* gb_last_error(const gb_ctx* ctx);
+/* Switches the stream later launches of this context use. */
+int gb_ctx_set_stream(gb_ctx* ctx, void* stream);
+
+/* ------------------------------------------------------------------ scene */
+/* PrincipledBRDFParameters (principledParameters.h:7-22), same field order. */
+typedef struct {
+    float metallic, subsurface, specular, roughness, specular_tint, anisotropic;
+    float sheen, sheen_tint, clearcoat, clearcoat_gloss, opacity, transmiss;
+    float color[3];
+    float tangent[3];
+} gb_principled_params;
+
+/* rta::cuda::material_t (material.h:142-184) without textures: a material is
+ * principled when `principled` >= 0 (index into gb_scene_desc.params), else
+ * Lambert with `diffuse` (ALL_MATERIAL_LAMBERT, material-wrapper.h:11). */
+typedef struct {
+    float diffuse[3];
+    int principled;
+} gb_material;
+
+enum { GB_LIGHT_RECT = 0, GB_LIGHT_SKY = 1 };
+/* gi::light / rect_light (lights.h:94-154).  power < 0 means "compute it
+ * with the add-rectlight rule" w*h*(r+g+b)*.333 (lights.cpp:92). */
+typedef struct {
+    int type;
+    float power;
+    float center[3], dir[3], up[3], col[3];
+    float wh[2];
+} gb_light;
+
+typedef struct {
+    int num_triangles;
+    const float* positions;       /* 9 floats per triangle: a, b, c           */
+    const float* normals;         /* 9 floats per triangle: na, nb, nc        */
+    const int* material_index;    /* per triangle, into `materials`           */
+    int num_materials;
+    const gb_material* materials;
+    int num_params;
+    const gb_principled_params* params;
+    int num_lights;
+    const gb_light* lights;
+} gb_scene_desc;
+
+typedef struct {
+    int num_triangles, num_nodes, depth, binary_nodes;
+    double build_ms;              /* host BVH build (binned SAH + collapse)   */
+    size_t device_bytes;          /* resident scene bytes                     */
+    float overall_light_power;    /* sum of light powers (hybrid-pt.cpp:74-78) */
+} gb_scene_info;
+
+/* Uploads triangles, materials and lights and builds the BVH (replaces
+ * setup_rta's plugin_create_rt_set + convert_and_upload_materials,
+ * hl-main.cpp:357-464, and hybrid_pt::activate's light copy). */
+int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* desc, gb_scene** out);
+void gb_scene_destroy(gb_scene* scene);
+int gb_scene_get_info(const gb_scene* scene, gb_scene_info* info);
+
+/* ----------------------------------------------------------------- camera */
+/* crgs->setup(pos, dir, up, fovy) + jittered_lens_ray_generator
+ * (hybrid-pt.cpp:86, :169; raygen.cu:61-118).  fovy_deg is the full
+ * vertical field of view; aperture 0 gives the jittered pinhole. */
+typedef struct {
+    float pos[3], dir[3], up[3];
+    float fovy_deg;
+    float aperture, focus_distance, eye_to_lens;
+} gb_camera;
+
+/* ----------------------------------------------------------------- render */
+enum {
+    GB_RNG_MRG32K3A_POOL = 0,  /* light and path draws from the per-pixel MRG32k3a
+                                  streams (curand_init(seed, pixel, 0)), 3 per bounce */
+    GB_RNG_HALTON_LIGHT = 1    /* light draws (h2(i+1), h3(i+1), h3(i+1)) per pixel,
+                                  path draws from MRG32k3a (util.cpp:38-51)        */
+};
+
+typedef struct {
+    int width, height;
+    int spp;                 /* path samples (init_path_samples)                   */
+    int max_bounces;         /* path length (init_path_length)                     */
+    int rng_mode;            /* GB_RNG_*                                            */
+    uint32_t seed;           /* curand seed (0 in the reference)                    */
+    float ray_offset;        /* 0.3 in the reference (hybrid-pt.cpp:551)            */
+    float shadow_offset;     /* 0.9 in the reference (arealight-sampler-cpu.cpp:115) */
+    float background[3];     /* (1,1,1) in the reference (hybrid-pt.cpp:52)          */
+    int rr_start;            /* Russian roulette from this bounce; -1 = off (parity) */
+} gb_render_desc;
+
+/* Renders a full progressive frame (spp paths of max_bounces bounces per
+ * pixel) and writes the moving-average image (float RGB, w*h*3, pixel
+ * (x,y) at index y*w+x as output_color in hybrid-pt.h:35).  `out_rgb` may be
+ * host memory (copied back inside the call) or device memory
+ * (out_is_device = 1). */
+int gb_render(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+              float* out_rgb, int out_is_device);
+
+/* Progressive form mirroring gi_algorithm::compute/update: begin sets up a
+ * pass (new_pass, hybrid-pt.h:115-122), each step renders `paths` further
+ * path samples (one update() of the reference advances half a bounce; here
+ * a step is whole paths), read copies the current image. */
+int gb_render_begin(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc);
+int gb_render_step(gb_ctx* ctx, int paths);
+int gb_render_paths_done(const gb_ctx* ctx, int* done);
+int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device);
+
+/* -------------------------------------------------------------- tracing */
+/* triangle_intersection (t, beta, gamma, ref): ref = canonical triangle id,
+ * 0xffffffff and t = FLT_MAX for a miss. */
+typedef struct {
+    float t, beta, gamma;
+    uint32_t ref;
+} gb_hit;
+
+/* Closest hit for n rays (origin/direction 3 floats each, AoS; max_t per
+ * ray).  Pointers are host memory unless `device_ptrs` is 1. */
+int gb_trace_closest(gb_ctx* ctx, gb_scene* scene, int n, const float* orig, const float* dir,
+                     const float* max_t, gb_hit* hits, int device_ptrs);
+/* Any hit with 0 < t <= max_t: occluded[i] = 1 / 0.  max_t < 0 = no ray. */
+int gb_trace_any(gb_ctx* ctx, gb_scene* scene, int n, const float* orig, const float* dir,
+                 const float* max_t, uint8_t* occluded, int device_ptrs);
+
+/* --------------------------------------------------------- hybrid stages */
+/* GPU form of rta::generate_arealight_sample (arealight-sampler-cpu.cpp:144-156)
+ * for a w x h pixel grid, device pointers, float3 = 3 packed floats:
+ *   rnd[3*i]        light-stream draw of pixel i
+ *   hits[i]         closest hits of this bounce
+ *   ray_dir[3*i]    in: path ray direction (used for misses); out: shadow dir
+ *   ray_orig, max_t out: shadow ray (max_t = -1 for misses)
+ *   psc[3*i]        out: potential_sample_contribution */
+int gb_generate_arealight_sample(gb_ctx* ctx, gb_scene* scene, int w, int h, float shadow_offset,
+                                 const float* rnd, const gb_hit* hits, float* ray_orig,
+                                 float* ray_dir, float* max_t, float* psc);
+
+/* GPU form of compute_path_contribution_and_bounce (hybrid-pt.cpp:450-584),
+ * device pointers, same buffers as the reference:
+ *   ray_orig/ray_dir/max_t  path rays (in: this bounce, out: next bounce)
+ *   hits, shadow_occluded   closest hits and any-hit results (1 = blocked)
+ *   rnd                     path-stream draw; throughput, col_accum in/out
+ *   to_light, psc           outputs of gb_generate_arealight_sample
+ * `path` and `bounce` only feed the Russian-roulette extension. */
+int gb_compute_path_contribution_and_bounce(gb_ctx* ctx, gb_scene* scene, int w, int h,
+                                            const gb_render_desc* desc, float* ray_orig,
+                                            float* ray_dir, float* max_t, const gb_hit* hits,
+                                            const uint8_t* shadow_occluded, const float* rnd,
+                                            float* throughput, float* col_accum,
+                                            const float* to_light, const float* psc,
+                                            int path, int bounce);
+
+/* ----------------------------------------------------------- sample pools */
+/* Draws of the per-pixel MRG32k3a streams: out[(u*npix + i)*3 + k] is draw
+ * 3*(first_update+u)+k of pixel i's stream, i.e. what update_mt_pool
+ * (util-kernels.cu:287-302) leaves in the pool at update first_update+u
+ * (curand_init(seed, i, 0), 3 curand_uniform per update).  Host `out`. */
+int gb_mrg_pool(gb_ctx* ctx, int npix, uint32_t seed, int first_update, int num_updates, float* out);
+
+/* ------------------------------------------------------------- statistics */
+typedef struct {
+    uint64_t camera_rays, extension_rays, shadow_rays;  /* traced in the last render  */
+    /* traversal work, only counted by gb_render_instrumented                        */
+    uint64_t closest_node_visits, closest_tri_tests;    /* camera + extension rays    */
+    uint64_t shadow_node_visits, shadow_tri_tests;      /* shadow (any-hit) rays      */
+    uint64_t kernel_launches;                           /* launches of the last render */
+    double render_ms;                                   /* device time, begin -> last step */
+    /* per-stage device time when stage timing is on (gb_ctx_set_stage_timing):
+     * 0 raygen, 1 closest-hit + light sample, 2 any-hit + shade, 3 accumulate  */
+    double stage_ms[4];
+    uint64_t stage_launches[4];
+    int paths_done;
+} gb_stats;
+
+/* Records CUDA events around every stage launch of later renders on the
+ * context's stream (for per-kernel timing); off by default. */
+int gb_ctx_set_stage_timing(gb_ctx* ctx, int on);
+int gb_get_stats(const gb_ctx* ctx, gb_stats* stats);
+/* Same as gb_render but counts 8-wide node visits and triangle tests of
+ * every traced ray (slower; used for the roofline's algorithmic bytes). */
+int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
+                           const gb_render_desc* desc, float* out_rgb, int out_is_device);
+
+/* Bytes of one stored 8-wide node / triangle (for roofline arithmetic). */
+int gb_layout_sizes(int* node_bytes, int* tri_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPT_H */

@@ -1,0 +1,533 @@
+// gbpt_oracle.cpp -- CPU oracle of the globillum path-tracing hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This library is loaded by tests/, by
+// __graft_entry__.smoke() and by bench.py's CPU-baseline / reference arm as
+// the checker and the timed CPU path; the product (libgbpt.so) never links,
+// loads or calls it.
+//
+// It restates the reference's CPU hot path frame-synchronously, exactly as
+// the hybrid bouncer sequences it (hybrid-pt.h:115-249): for every path
+// sample, camera rays for all pixels (raygen.h:122-181 / raygen.cu:61-118),
+// then per bounce a closest-hit trace of all pixels, the area-light sample
+// of all pixels (rta::generate_arealight_sample,
+// arealight-sampler-cpu.cpp:144-156), an any-hit trace of all shadow rays
+// and compute_path_contribution_and_bounce over all pixels
+// (hybrid-pt.cpp:450-584, OpenMP over rows as at :462), followed by the
+// moving average of new_path (hybrid-pt.h:123-131, util-kernels.cu:17-25).
+// Random numbers come in as pools, as the reference downloads them from
+// the device (hybrid-pt.h:112-113, :232-233): pool update u of pixel i holds
+// three uniforms; path p uses update p for the camera jitter and update
+// p*L+b for both the light and the path draws of bounce b (the three
+// reference pools are seeded identically, util-kernels.cu:284).
+//
+// Traversal: its own binary binned-SAH BVH (or brute force), with the
+// closest-hit rule "minimum (t, canonical id) over all triangles with
+// 0 < t <= t_max" (tracers.cu:113 up to exact ties), so results do not
+// depend on the tree.  The per-ray arithmetic (triangle test, light sample,
+// BRDFs, camera) is the shared gbpt_math.h, compiled with
+// -ffp-contract=off so that every value equals the device's bit for bit.
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../globillum_gb300/csrc/gbpt_host.h"
+#include "../globillum_gb300/csrc/gbpt_math.h"
+#include "../include/gbpt.h"
+
+using namespace gb;
+
+namespace {
+
+struct OBox {
+    float lo[3], hi[3];
+};
+
+struct ONode {
+    OBox b;
+    int left, right;   // inner: children
+    int first, count;  // leaf: range in idx
+};
+
+struct OScene {
+    int n = 0;
+    std::vector<float> pos, nrm;  // 9 per triangle
+    std::vector<int> mat;
+    std::vector<MaterialRec> mats;
+    std::vector<LightRec> lights;
+    float overall = 0.0f;
+    bool use_bvh = true;
+    std::vector<ONode> nodes;
+    std::vector<int> idx;
+};
+
+void box_grow(OBox& b, const float* p) {
+    for (int a = 0; a < 3; ++a) { b.lo[a] = std::min(b.lo[a], p[a]); b.hi[a] = std::max(b.hi[a], p[a]); }
+}
+void box_grow(OBox& b, const OBox& c) {
+    for (int a = 0; a < 3; ++a) { b.lo[a] = std::min(b.lo[a], c.lo[a]); b.hi[a] = std::max(b.hi[a], c.hi[a]); }
+}
+OBox box_empty() {
+    OBox b;
+    for (int a = 0; a < 3; ++a) { b.lo[a] = 3e38f; b.hi[a] = -3e38f; }
+    return b;
+}
+float box_area(const OBox& b) {
+    float d0 = std::max(0.0f, b.hi[0] - b.lo[0]), d1 = std::max(0.0f, b.hi[1] - b.lo[1]),
+          d2 = std::max(0.0f, b.hi[2] - b.lo[2]);
+    return d0 * d1 + d1 * d2 + d2 * d0;
+}
+
+// Binned SAH (12 bins), leaves of at most 4 triangles.
+int build_node(OScene& s, std::vector<OBox>& tb, std::vector<float>& cen, int b, int e) {
+    OBox nb = box_empty(), cb = box_empty();
+    for (int i = b; i < e; ++i) { box_grow(nb, tb[s.idx[i]]); box_grow(cb, &cen[3 * s.idx[i]]); }
+    int me = (int)s.nodes.size();
+    s.nodes.push_back(ONode{nb, -1, -1, b, 0});
+    int cnt = e - b;
+    if (cnt <= 4) { s.nodes[me].count = cnt; return me; }
+    const int K = 12;
+    float best = 3e38f; int ba = -1, bk = -1;
+    for (int a = 0; a < 3; ++a) {
+        float ext = cb.hi[a] - cb.lo[a];
+        if (!(ext > 0.0f)) continue;
+        OBox bins[K]; int bc[K];
+        for (int k = 0; k < K; ++k) { bins[k] = box_empty(); bc[k] = 0; }
+        for (int i = b; i < e; ++i) {
+            int t = s.idx[i];
+            int k = std::min(K - 1, (int)((cen[3 * t + a] - cb.lo[a]) / ext * K));
+            box_grow(bins[k], tb[t]); bc[k]++;
+        }
+        for (int k = 0; k < K - 1; ++k) {
+            OBox l = box_empty(), r = box_empty(); int nl = 0, nr = 0;
+            for (int j = 0; j <= k; ++j) { box_grow(l, bins[j]); nl += bc[j]; }
+            for (int j = k + 1; j < K; ++j) { box_grow(r, bins[j]); nr += bc[j]; }
+            if (!nl || !nr) continue;
+            float c = box_area(l) * nl + box_area(r) * nr;
+            if (c < best) { best = c; ba = a; bk = k; }
+        }
+    }
+    int mid = b + cnt / 2;
+    if (ba >= 0) {
+        float ext = cb.hi[ba] - cb.lo[ba];
+        int* p = std::partition(&s.idx[b], &s.idx[b] + cnt, [&](int t) {
+            return std::min(K - 1, (int)((cen[3 * t + ba] - cb.lo[ba]) / ext * K)) <= bk;
+        });
+        mid = (int)(p - &s.idx[0]);
+        if (mid == b || mid == e) mid = b + cnt / 2;
+    }
+    int l = build_node(s, tb, cen, b, mid);
+    int r = build_node(s, tb, cen, mid, e);
+    s.nodes[me].left = l; s.nodes[me].right = r;
+    return me;
+}
+
+void build_bvh(OScene& s) {
+    std::vector<OBox> tb(s.n);
+    std::vector<float> cen(3 * (size_t)s.n);
+    for (int t = 0; t < s.n; ++t) {
+        OBox b = box_empty();
+        for (int v = 0; v < 3; ++v) box_grow(b, &s.pos[9 * (size_t)t + 3 * v]);
+        // pad outward by 2^-18 of the magnitude so that slab tests stay
+        // conservative under rounding
+        float m = 0.0f;
+        for (int a = 0; a < 3; ++a) m = std::max(m, std::max(std::fabs(b.lo[a]), std::fabs(b.hi[a])));
+        float d = m * (1.0f / 262144.0f) + 1e-30f;
+        for (int a = 0; a < 3; ++a) { b.lo[a] -= d; b.hi[a] += d; cen[3 * (size_t)t + a] = 0.5f * (b.lo[a] + b.hi[a]); }
+        tb[t] = b;
+    }
+    s.idx.resize(s.n);
+    for (int i = 0; i < s.n; ++i) s.idx[i] = i;
+    s.nodes.clear();
+    s.nodes.reserve(2 * (size_t)s.n);
+    build_node(s, tb, cen, 0, s.n);
+}
+
+// Slab test with a relative slack of 1e-5 on the interval (conservative).
+inline bool slab(const OBox& b, const v3& o, const v3& inv, float bound, float* tentry) {
+    float t0x = (b.lo[0] - o.x) * inv.x, t1x = (b.hi[0] - o.x) * inv.x;
+    float t0y = (b.lo[1] - o.y) * inv.y, t1y = (b.hi[1] - o.y) * inv.y;
+    float t0z = (b.lo[2] - o.z) * inv.z, t1z = (b.hi[2] - o.z) * inv.z;
+    float tmin = std::max(std::max(std::min(t0x, t1x), std::min(t0y, t1y)), std::min(t0z, t1z));
+    float tmax = std::min(std::min(std::max(t0x, t1x), std::max(t0y, t1y)), std::max(t0z, t1z));
+    float lo = std::max(tmin * 0.99999f, 0.0f);
+    float hi = std::min(tmax * 1.00001f, bound);
+    *tentry = lo;
+    return lo <= hi;
+}
+
+inline bool tri_test(const OScene& s, int t, const v3& o, const v3& d, float* tt, float* u, float* v) {
+    const float* p = &s.pos[9 * (size_t)t];
+    v3 a = mk(p[0], p[1], p[2]);
+    v3 e1 = mk(p[3] - p[0], p[4] - p[1], p[5] - p[2]);
+    v3 e2 = mk(p[6] - p[0], p[7] - p[1], p[8] - p[2]);
+    return intersect_tri(o, d, a, e1, e2, tt, u, v);
+}
+
+// Closest hit: minimum (t, id) over 0 < t <= tmax.
+gb_hit trace_closest(const OScene& s, v3 o, v3 d, float tmax, uint64_t* visits, uint64_t* tests) {
+    gb_hit h{FLT_MAX, 0.0f, 0.0f, 0xffffffffu};
+    if (!(tmax >= 0.0f)) return h;
+    if (!s.use_bvh) {
+        for (int t = 0; t < s.n; ++t) {
+            float tt, u, v;
+            if (tests) ++*tests;
+            if (tri_test(s, t, o, d, &tt, &u, &v) && tt <= tmax && closer(tt, (uint32_t)t, h.t, h.ref))
+                h = gb_hit{tt, u, v, (uint32_t)t};
+        }
+        return h;
+    }
+    const float ooeps = 8.271806125530277e-25f;
+    v3 inv = mk(1.0f / (std::fabs(d.x) > ooeps ? d.x : std::copysign(ooeps, d.x)),
+                1.0f / (std::fabs(d.y) > ooeps ? d.y : std::copysign(ooeps, d.y)),
+                1.0f / (std::fabs(d.z) > ooeps ? d.z : std::copysign(ooeps, d.z)));
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const ONode& nd = s.nodes[stack[--sp]];
+        float te;
+        if (visits) ++*visits;
+        if (!slab(nd.b, o, inv, std::min(h.t, tmax), &te)) continue;
+        if (nd.count > 0) {
+            for (int i = 0; i < nd.count; ++i) {
+                int t = s.idx[nd.first + i];
+                float tt, u, v;
+                if (tests) ++*tests;
+                if (tri_test(s, t, o, d, &tt, &u, &v) && tt <= tmax && closer(tt, (uint32_t)t, h.t, h.ref))
+                    h = gb_hit{tt, u, v, (uint32_t)t};
+            }
+            continue;
+        }
+        float tl, tr;
+        bool hl = slab(s.nodes[nd.left].b, o, inv, std::min(h.t, tmax), &tl);
+        bool hr = slab(s.nodes[nd.right].b, o, inv, std::min(h.t, tmax), &tr);
+        if (hl && hr) {
+            if (sp + 2 > 128) break;
+            if (tl <= tr) { stack[sp++] = nd.right; stack[sp++] = nd.left; }
+            else { stack[sp++] = nd.left; stack[sp++] = nd.right; }
+        } else if (hl) { stack[sp++] = nd.left; }
+        else if (hr) { stack[sp++] = nd.right; }
+    }
+    return h;
+}
+
+bool trace_any(const OScene& s, v3 o, v3 d, float tmax) {
+    if (!(tmax >= 0.0f)) return false;
+    if (!s.use_bvh) {
+        for (int t = 0; t < s.n; ++t) {
+            float tt, u, v;
+            if (tri_test(s, t, o, d, &tt, &u, &v) && tt <= tmax) return true;
+        }
+        return false;
+    }
+    const float ooeps = 8.271806125530277e-25f;
+    v3 inv = mk(1.0f / (std::fabs(d.x) > ooeps ? d.x : std::copysign(ooeps, d.x)),
+                1.0f / (std::fabs(d.y) > ooeps ? d.y : std::copysign(ooeps, d.y)),
+                1.0f / (std::fabs(d.z) > ooeps ? d.z : std::copysign(ooeps, d.z)));
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const ONode& nd = s.nodes[stack[--sp]];
+        float te;
+        if (!slab(nd.b, o, inv, tmax, &te)) continue;
+        if (nd.count > 0) {
+            for (int i = 0; i < nd.count; ++i) {
+                float tt, u, v;
+                if (tri_test(s, s.idx[nd.first + i], o, d, &tt, &u, &v) && tt <= tmax) return true;
+            }
+            continue;
+        }
+        if (sp + 2 > 128) break;
+        stack[sp++] = nd.left;
+        stack[sp++] = nd.right;
+    }
+    return false;
+}
+
+inline v3 tri_interp(const std::vector<float>& a, int t, float beta, float gamma) {
+    const float* p = &a[9 * (size_t)t];
+    return bary(beta, gamma, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]));
+}
+
+// pixel_generate_arealight_sample_cpu (arealight-sampler-cpu.cpp:25-143)
+// without a sky light.
+void nee_pixel(const OScene& s, int id, const gb_hit& h, v3 rnd, float shadow_offset, v3* so, v3* sd, float* smax,
+               v3* psc) {
+    if (h.ref != 0xffffffffu && !s.lights.empty()) {
+        int l = pick_light(s.lights.data(), (int)s.lights.size(), s.overall, rnd.z);
+        v3 P = tri_interp(s.pos, (int)h.ref, h.beta, h.gamma);
+        v3 N = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
+        rect_light_sample(s.lights[l], s.overall, P, N, rnd.x, rnd.y, shadow_offset, so, sd, smax, psc);
+    } else {
+        *so = mk(FLT_MAX, FLT_MAX, FLT_MAX);
+        *sd = mk(0.0f, 0.0f, 0.0f);
+        *smax = -1.0f;
+        *psc = mk(0.0f, 0.0f, 0.0f);
+    }
+    (void)id;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_scene_create(int n, const float* pos, const float* nrm, const int* mat, int nmat, const gb_material* mats,
+                       int nparams, const gb_principled_params* params, int nl, const gb_light* lights, int use_bvh) {
+    if (n <= 0 || !pos || !mat || nmat <= 0 || !mats) return nullptr;
+    OScene* s = new OScene();
+    s->n = n;
+    s->pos.assign(pos, pos + 9 * (size_t)n);
+    if (nrm) s->nrm.assign(nrm, nrm + 9 * (size_t)n);
+    else {
+        s->nrm.resize(9 * (size_t)n);
+        for (int t = 0; t < n; ++t) {
+            const float* p = pos + 9 * (size_t)t;
+            v3 fn = normalize_div(cross(mk(p[3] - p[0], p[4] - p[1], p[5] - p[2]), mk(p[6] - p[0], p[7] - p[1], p[8] - p[2])));
+            for (int k = 0; k < 3; ++k) { s->nrm[9 * t + 3 * k] = fn.x; s->nrm[9 * t + 3 * k + 1] = fn.y; s->nrm[9 * t + 3 * k + 2] = fn.z; }
+        }
+    }
+    s->mat.assign(mat, mat + n);
+    (void)nparams;
+    for (int m = 0; m < nmat; ++m) {
+        // the round trip through the 32-float record is what the device sees
+        float f[kMaterialFloats];
+        pack_material(make_material(mats[m], params), f);
+        s->mats.push_back(unpack_material(f));
+    }
+    for (int l = 0; l < nl; ++l) s->lights.push_back(make_light(lights[l]));
+    s->overall = overall_power(s->lights.data(), (int)s->lights.size());
+    s->use_bvh = use_bvh != 0;
+    if (s->use_bvh) build_bvh(*s);
+    return s;
+}
+
+void orc_scene_destroy(void* s) { delete (OScene*)s; }
+
+int orc_trace_closest(void* sp, int n, const float* o, const float* d, const float* tmax, gb_hit* hits,
+                      uint64_t* counts) {
+    const OScene& s = *(const OScene*)sp;
+    uint64_t vis = 0, tst = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : vis, tst)
+    for (int i = 0; i < n; ++i) {
+        uint64_t v = 0, t = 0;
+        hits[i] = trace_closest(s, mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]), mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]),
+                                tmax[i], &v, &t);
+        vis += v; tst += t;
+    }
+    if (counts) { counts[0] = vis; counts[1] = tst; }
+    return 0;
+}
+
+int orc_trace_any(void* sp, int n, const float* o, const float* d, const float* tmax, uint8_t* occl) {
+    const OScene& s = *(const OScene*)sp;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < n; ++i)
+        occl[i] = trace_any(s, mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]), mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]),
+                            tmax[i]) ? 1 : 0;
+    return 0;
+}
+
+// rta::generate_arealight_sample on a w x h grid (host buffers, reference
+// layout).  Serial when `serial` (the reference's `omp prallel` typo at
+// arealight-sampler-cpu.cpp:148), else OpenMP over rows.
+int orc_generate_arealight_sample(void* sp, int w, int h, float shadow_offset, const float* rnd, const gb_hit* hits,
+                                  float* ray_orig, float* ray_dir, float* max_t, float* psc, int serial) {
+    const OScene& s = *(const OScene*)sp;
+#pragma omp parallel for schedule(dynamic, 1) if (!serial)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            int id = y * w + x;
+            v3 so, sd, ps; float sm;
+            nee_pixel(s, id, hits[id], mk(rnd[3 * id], rnd[3 * id + 1], rnd[3 * id + 2]), shadow_offset, &so, &sd, &sm, &ps);
+            ray_orig[3 * id] = so.x; ray_orig[3 * id + 1] = so.y; ray_orig[3 * id + 2] = so.z;
+            ray_dir[3 * id] = sd.x; ray_dir[3 * id + 1] = sd.y; ray_dir[3 * id + 2] = sd.z;
+            max_t[id] = sm;
+            psc[3 * id] = ps.x; psc[3 * id + 1] = ps.y; psc[3 * id + 2] = ps.z;
+        }
+    return 0;
+}
+
+// compute_path_contribution_and_bounce (hybrid-pt.cpp:450-584), host buffers.
+int orc_compute_path_contribution_and_bounce(void* sp, int w, int h, const gb_render_desc* desc, float* ray_orig,
+                                             float* ray_dir, float* max_t, const gb_hit* hits,
+                                             const uint8_t* occl, const float* rnd, float* tp, float* accum,
+                                             const float* to_light, const float* psc, int path, int bounce,
+                                             int pixel_base) {
+    const OScene& s = *(const OScene*)sp;
+    ShadeParams par = make_shade_params(*desc);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            int id = y * w + x;
+            const gb_hit& hh = hits[id];
+            v3 t = mk(tp[3 * id], tp[3 * id + 1], tp[3 * id + 2]);
+            v3 ac = mk(accum[3 * id], accum[3 * id + 1], accum[3 * id + 2]);
+            bool alive = false;
+            if (hh.ref != 0xffffffffu) {
+                v3 P = tri_interp(s.pos, (int)hh.ref, hh.beta, hh.gamma);
+                v3 N = tri_interp(s.nrm, (int)hh.ref, hh.beta, hh.gamma);
+                const MaterialRec& m = s.mats[s.mat[hh.ref]];
+                ShadeOut o = shade_hit(m, P, N, mk(ray_dir[3 * id], ray_dir[3 * id + 1], ray_dir[3 * id + 2]), t,
+                                       mk(rnd[3 * id], rnd[3 * id + 1], rnd[3 * id + 2]), occl[id] == 0,
+                                       mk(to_light[3 * id], to_light[3 * id + 1], to_light[3 * id + 2]),
+                                       mk(psc[3 * id], psc[3 * id + 1], psc[3 * id + 2]), par,
+                                       (uint32_t)(pixel_base + id), (uint32_t)path, bounce);
+                ac = ac + o.accum_add;
+                t = o.tp;
+                alive = o.alive;
+                if (alive) {
+                    ray_orig[3 * id] = o.org.x; ray_orig[3 * id + 1] = o.org.y; ray_orig[3 * id + 2] = o.org.z;
+                    ray_dir[3 * id] = o.dir.x; ray_dir[3 * id + 1] = o.dir.y; ray_dir[3 * id + 2] = o.dir.z;
+                    max_t[id] = FLT_MAX;
+                }
+            } else {
+                if (max_t[id] != -1.0f) ac = ac + miss_contribution(t, par);
+                t = mk(0.0f, 0.0f, 0.0f);
+            }
+            if (!alive) {
+                ray_orig[3 * id] = FLT_MAX; ray_orig[3 * id + 1] = FLT_MAX; ray_orig[3 * id + 2] = FLT_MAX;
+                ray_dir[3 * id] = 0.0f; ray_dir[3 * id + 1] = 0.0f; ray_dir[3 * id + 2] = 0.0f;
+                max_t[id] = -1.0f;
+            }
+            tp[3 * id] = t.x; tp[3 * id + 1] = t.y; tp[3 * id + 2] = t.z;
+            accum[3 * id] = ac.x; accum[3 * id + 1] = ac.y; accum[3 * id + 2] = ac.z;
+        }
+    return 0;
+}
+
+// Full progressive frame over rows [row0, row1) of a w x h image.
+// pool: `pool_updates` updates of the rows' pixels, layout
+// [update][pixel - row0*w][3]; needs spp*L updates.  out_rgb: (row1-row0)*w*3.
+// stats (optional): camera, extension, shadow rays, node visits, tri tests.
+int orc_render(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0, int row1, const float* pool,
+               int pool_updates, float* out_rgb, int serial_nee, uint64_t* stats) {
+    const OScene& s = *(const OScene*)sp;
+    const int W = d->width, H = d->height, L = d->max_bounces;
+    if (row0 < 0 || row1 > H || row0 >= row1) return 1;
+    if (pool_updates < d->spp * L) return 2;
+    if (cam->aperture != 0.0f && (row0 != 0 || row1 != H)) return 3;
+    const int h = row1 - row0, n = W * h, base = row0 * W;
+    CameraRec C = make_camera(*cam, W, H);
+    ShadeParams par = make_shade_params(*d);
+    std::vector<float> ro(3 * (size_t)n), rd(3 * (size_t)n), mt(n), so(3 * (size_t)n), sd(3 * (size_t)n), sm(n),
+        ps(3 * (size_t)n), tp(3 * (size_t)n), ac(3 * (size_t)n), lr(3 * (size_t)n), rnd(3 * (size_t)n);
+    std::vector<gb_hit> hits(n);
+    std::vector<uint8_t> occl(n);
+    std::fill(out_rgb, out_rgb + 3 * (size_t)n, 0.0f);
+    uint64_t n_cam = 0, n_ext = 0, n_sh = 0, n_vis = 0, n_tst = 0;
+    for (int p = 0; p < d->spp; ++p) {
+        // new_path: throughput 1, accumulation 0, camera rays with jitter update p
+        const float* jp = pool + (size_t)p * n * 3;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            int id = base + i;
+            int x = id % W, y = id / W;
+            float lx = 0.0f, ly = 0.0f;
+            if (C.aperture != 0.0f) {
+                int o = (id + 17) % (W * H);
+                lx = jp[3 * o + 2] - 0.5f;
+                ly = jp[3 * o + 1] - 0.5f;
+            }
+            v3 o, dd;
+            camera_ray(C, x, y, jp[3 * i], jp[3 * i + 1], lx, ly, &o, &dd);
+            ro[3 * i] = o.x; ro[3 * i + 1] = o.y; ro[3 * i + 2] = o.z;
+            rd[3 * i] = dd.x; rd[3 * i + 1] = dd.y; rd[3 * i + 2] = dd.z;
+            mt[i] = FLT_MAX;
+            tp[3 * i] = tp[3 * i + 1] = tp[3 * i + 2] = 1.0f;
+            ac[3 * i] = ac[3 * i + 1] = ac[3 * i + 2] = 0.0f;
+        }
+        n_cam += n;
+        for (int b = 0; b < L; ++b) {
+            const float* up = pool + ((size_t)p * L + b) * n * 3;
+            // closest hit of every live ray (dead rays: max_t == -1)
+            uint64_t ce = 0, cv = 0, ct = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : ce, cv, ct)
+            for (int i = 0; i < n; ++i) {
+                if (mt[i] < 0.0f) { hits[i] = gb_hit{FLT_MAX, 0.0f, 0.0f, 0xffffffffu}; continue; }
+                uint64_t v = 0, t = 0;
+                hits[i] = trace_closest(s, mk(ro[3 * i], ro[3 * i + 1], ro[3 * i + 2]),
+                                        mk(rd[3 * i], rd[3 * i + 1], rd[3 * i + 2]), mt[i], &v, &t);
+                ce += 1; cv += v; ct += t;
+            }
+            if (b > 0) n_ext += ce;
+            n_vis += cv; n_tst += ct;
+            // light draws: the light pool, or Halton (h2(i+1), h3(i+1), h3(i+1))
+            for (int i = 0; i < n; ++i) {
+                if (d->rng_mode == GB_RNG_HALTON_LIGHT) {
+                    float hy = halton(base + i + 1, 3);
+                    lr[3 * i] = halton(base + i + 1, 2); lr[3 * i + 1] = hy; lr[3 * i + 2] = hy;
+                } else {
+                    lr[3 * i] = up[3 * i]; lr[3 * i + 1] = up[3 * i + 1]; lr[3 * i + 2] = up[3 * i + 2];
+                }
+                rnd[3 * i] = up[3 * i]; rnd[3 * i + 1] = up[3 * i + 1]; rnd[3 * i + 2] = up[3 * i + 2];
+            }
+            orc_generate_arealight_sample(sp, W, h, d->shadow_offset, lr.data(), hits.data(), so.data(), sd.data(),
+                                          sm.data(), ps.data(), serial_nee);
+            uint64_t cs = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : cs)
+            for (int i = 0; i < n; ++i) {
+                if (hits[i].ref == 0xffffffffu) { occl[i] = 1; continue; }
+                occl[i] = (sm[i] >= 0.0f) ? (trace_any(s, mk(so[3 * i], so[3 * i + 1], so[3 * i + 2]),
+                                                       mk(sd[3 * i], sd[3 * i + 1], sd[3 * i + 2]), sm[i]) ? 1 : 0)
+                                          : 1;
+                cs += 1;
+            }
+            n_sh += cs;
+            orc_compute_path_contribution_and_bounce(sp, W, h, d, ro.data(), rd.data(), mt.data(), hits.data(),
+                                                     occl.data(), rnd.data(), tp.data(), ac.data(), sd.data(),
+                                                     ps.data(), p, b, base);
+        }
+        // new_path: moving average
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            v3 c = combine_sample(mk(out_rgb[3 * i], out_rgb[3 * i + 1], out_rgb[3 * i + 2]),
+                                  mk(ac[3 * i], ac[3 * i + 1], ac[3 * i + 2]), p);
+            out_rgb[3 * i] = c.x; out_rgb[3 * i + 1] = c.y; out_rgb[3 * i + 2] = c.z;
+        }
+    }
+    (void)par;
+    if (stats) { stats[0] = n_cam; stats[1] = n_ext; stats[2] = n_sh; stats[3] = n_vis; stats[4] = n_tst; }
+    return 0;
+}
+
+// Halton pool of util.cpp:38-51 for pixels [0, n): (h2(i+1), h3(i+1)).
+int orc_halton_pool(int n, float* out) {
+    for (int i = 0; i < n; ++i) { out[2 * i] = halton(i + 1, 2); out[2 * i + 1] = halton(i + 1, 3); }
+    return 0;
+}
+
+// Exposed per-ray functions for the pinning tests against the reference's
+// own BRDF / light code.
+int orc_material_sample_eval(const gb_material* mat, const gb_principled_params* params, const float* wo_ts,
+                             const float* rnd, const float* N, const float* wo_world, const float* wi_eval,
+                             float* wi_out, float* pdf_out, int* lobe_out, float* f_sampled, float* f_eval) {
+    float f[kMaterialFloats];
+    pack_material(make_material(*mat, params), f);
+    MaterialRec m = unpack_material(f);
+    v3 wi; float pdf; int lobe;
+    material_sample(m, mk(wo_ts[0], wo_ts[1], wo_ts[2]), mk(rnd[0], rnd[1], rnd[2]), &wi, &pdf, &lobe);
+    wi_out[0] = wi.x; wi_out[1] = wi.y; wi_out[2] = wi.z;
+    *pdf_out = pdf; *lobe_out = lobe;
+    v3 n = mk(N[0], N[1], N[2]), wo = mk(wo_world[0], wo_world[1], wo_world[2]);
+    v3 fs = material_eval(m, lobe, wo, wi, n);
+    v3 fe = material_eval(m, lobe, wo, mk(wi_eval[0], wi_eval[1], wi_eval[2]), n);
+    f_sampled[0] = fs.x; f_sampled[1] = fs.y; f_sampled[2] = fs.z;
+    f_eval[0] = fe.x; f_eval[1] = fe.y; f_eval[2] = fe.z;
+    return 0;
+}
+
+int orc_sincos_2pi(int n, const float* u, float* s, float* c) {
+    for (int i = 0; i < n; ++i) sincos_2pi(u[i], &s[i], &c[i]);
+    return 0;
+}
+
+int orc_threads(void) { return omp_get_max_threads(); }
+void orc_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+"""ctypes wrapper of the CPU oracle (oracle/gbpt_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference arm, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from globillum_gb300 import build as _build  # noqa: E402
+from globillum_gb300 import gbpt as _gbpt  # noqa: E402
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        lib = C.CDLL(str(path))
+        vp, ip, fp = C.c_void_p, C.c_int, C.c_float
+        lib.orc_scene_create.restype = vp
+        lib.orc_scene_create.argtypes = [ip, vp, vp, vp, ip, vp, ip, vp, ip, vp, ip]
+        lib.orc_scene_destroy.argtypes = [vp]
+        lib.orc_scene_destroy.restype = None
+        lib.orc_trace_closest.argtypes = [vp, ip, vp, vp, vp, vp, vp]
+        lib.orc_trace_any.argtypes = [vp, ip, vp, vp, vp, vp]
+        lib.orc_generate_arealight_sample.argtypes = [vp, ip, ip, fp, vp, vp, vp, vp, vp, vp, ip]
+        lib.orc_compute_path_contribution_and_bounce.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                                                 vp, vp, ip, ip, ip]
+        lib.orc_render.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp]
+        lib.orc_halton_pool.argtypes = [ip, vp]
+        lib.orc_material_sample_eval.argtypes = [vp] * 12
+        lib.orc_sincos_2pi.argtypes = [ip, vp, vp, vp]
+        lib.orc_threads.restype = ip
+        lib.orc_set_threads.argtypes = [ip]
+        lib.orc_set_threads.restype = None
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class OracleScene:
+    def __init__(self, scene, use_bvh: bool = True):
+        self.lib = load()
+        desc, self._keep = _gbpt.make_scene_desc(scene)
+        self.h = self.lib.orc_scene_create(desc.num_triangles, desc.positions, desc.normals, desc.material_index,
+                                           desc.num_materials, C.cast(desc.materials, C.c_void_p),
+                                           desc.num_params, C.cast(desc.params, C.c_void_p), desc.num_lights,
+                                           C.cast(desc.lights, C.c_void_p), 1 if use_bvh else 0)
+        if not self.h:
+            raise ValueError("oracle scene creation failed")
+
+    def close(self):
+        if self.h:
+            self.lib.orc_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace_closest(self, o, d, tmax, counts: bool = False):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        tmax = np.ascontiguousarray(tmax, np.float32)
+        hits = np.empty(tmax.shape[0], _gbpt.HIT_DTYPE)
+        c = np.zeros(2, np.uint64)
+        self.lib.orc_trace_closest(self.h, tmax.shape[0], _p(o), _p(d), _p(tmax), _p(hits), _p(c))
+        return (hits, c) if counts else hits
+
+    def trace_any(self, o, d, tmax):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        tmax = np.ascontiguousarray(tmax, np.float32)
+        occ = np.empty(tmax.shape[0], np.uint8)
+        self.lib.orc_trace_any(self.h, tmax.shape[0], _p(o), _p(d), _p(tmax), _p(occ))
+        return occ
+
+    def render(self, cam: dict, rdesc: dict, pool: np.ndarray, row0: int = 0, row1: int | None = None,
+               serial_nee: bool = False, with_stats: bool = False):
+        """Progressive frame over rows [row0, row1); pool: (updates, pixels of the rows, 3)."""
+        rd = _gbpt.make_render_desc(rdesc)
+        cm = _gbpt.make_camera(cam)
+        row1 = rd.height if row1 is None else row1
+        pool = np.ascontiguousarray(pool, np.float32)
+        n = (row1 - row0) * rd.width
+        assert pool.shape[1] == n and pool.shape[2] == 3
+        out = np.empty((row1 - row0, rd.width, 3), np.float32)
+        st = np.zeros(5, np.uint64)
+        rc = self.lib.orc_render(self.h, C.byref(cm), C.byref(rd), row0, row1, _p(pool), pool.shape[0], _p(out),
+                                 1 if serial_nee else 0, _p(st))
+        if rc != 0:
+            raise ValueError(f"orc_render failed ({rc})")
+        return (out, st) if with_stats else out
+
+    def generate_arealight_sample(self, w, h, shadow_offset, rnd, hits, ray_dir, serial=False):
+        n = w * h
+        ro = np.empty((n, 3), np.float32)
+        rd = np.ascontiguousarray(ray_dir, np.float32).copy()
+        mt = np.empty(n, np.float32)
+        psc = np.empty((n, 3), np.float32)
+        self.lib.orc_generate_arealight_sample(self.h, w, h, float(shadow_offset), _p(np.ascontiguousarray(rnd, np.float32)),
+                                               _p(hits), _p(ro), _p(rd), _p(mt), _p(psc), 1 if serial else 0)
+        return ro, rd, mt, psc
+
+    def compute_path_contribution_and_bounce(self, w, h, rdesc, ray_orig, ray_dir, max_t, hits, occl, rnd, tp,
+                                             accum, to_light, psc, path, bounce):
+        ro = np.ascontiguousarray(ray_orig, np.float32).copy()
+        rd = np.ascontiguousarray(ray_dir, np.float32).copy()
+        mt = np.ascontiguousarray(max_t, np.float32).copy()
+        t = np.ascontiguousarray(tp, np.float32).copy()
+        a = np.ascontiguousarray(accum, np.float32).copy()
+        desc = _gbpt.make_render_desc(rdesc)
+        self.lib.orc_compute_path_contribution_and_bounce(
+            self.h, w, h, C.byref(desc), _p(ro), _p(rd), _p(mt), _p(hits), _p(np.ascontiguousarray(occl, np.uint8)),
+            _p(np.ascontiguousarray(rnd, np.float32)), _p(t), _p(a), _p(np.ascontiguousarray(to_light, np.float32)),
+            _p(np.ascontiguousarray(psc, np.float32)), path, bounce, 0)
+        return ro, rd, mt, t, a
+
+
+def halton_pool(n: int) -> np.ndarray:
+    out = np.empty((n, 2), np.float32)
+    load().orc_halton_pool(n, _p(out))
+    return out
+
+
+def sincos_2pi(u: np.ndarray):
+    u = np.ascontiguousarray(u, np.float32)
+    s = np.empty_like(u)
+    c = np.empty_like(u)
+    load().orc_sincos_2pi(u.shape[0], _p(u), _p(s), _p(c))
+    return s, c
+
+
+def material_sample_eval(material: dict, params: dict | None, wo_ts, rnd, N, wo_world, wi_eval):
+    lib = load()
+    m = _gbpt.Material(_gbpt._f3(material["diffuse"]), 0 if params is not None else -1)
+    pp = (_gbpt.PrincipledParams * 1)()
+    if params is not None:
+        sd, _ = _gbpt.make_scene_desc(type("S", (), {
+            "positions": np.zeros((1, 9), np.float32), "normals": None, "material_index": np.zeros(1, np.int32),
+            "materials": [material], "params": [params], "lights": []})())
+        pp[0] = sd.params[0]
+    f = lambda v: np.ascontiguousarray(v, np.float32)
+    wi = np.empty(3, np.float32)
+    pdf = np.empty(1, np.float32)
+    lobe = np.empty(1, np.int32)
+    fs = np.empty(3, np.float32)
+    fe = np.empty(3, np.float32)
+    args = [f(wo_ts), f(rnd), f(N), f(wo_world), f(wi_eval)]
+    lib.orc_material_sample_eval(C.byref(m), C.cast(pp, C.c_void_p), *[_p(a) for a in args], _p(wi), _p(pdf),
+                                 _p(lobe), _p(fs), _p(fe))
+    return wi, float(pdf[0]), int(lobe[0]), fs, fe
+
+
+def threads() -> int:
+    return load().orc_threads()
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_threads(n)

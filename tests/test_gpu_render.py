@@ -1,0 +1,115 @@
+"""Frame parity: the GPU wavefront frame vs the CPU oracle's restatement of
+the hybrid bouncer, fed with the same MRG32k3a pools (gb_mrg_pool: curand
+MRG32k3a, seed 0, subsequence = pixel).  Per-pixel radiance must agree
+within 1e-4 relative (absolute floor 1e-6); the arithmetic is shared and
+IEEE-exact, so in practice the frames are bit-identical."""
+import numpy as np
+import pytest
+
+from globillum_gb300 import gbpt, scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+ATOL = 1e-6
+
+
+def _compare(img, ref):
+    assert img.shape == ref.shape
+    assert np.isfinite(img).all()
+    diff = np.abs(img.astype(np.float64) - ref)
+    bad = diff > RTOL * np.abs(ref) + ATOL
+    assert not bad.any(), f"{bad.any(axis=2).sum()} pixels differ, max abs diff {diff.max():.3g}"
+
+
+def _render_pair(ctx, sc, rd, use_bvh=True):
+    from oracle import oracle
+    scene = ctx.scene(sc)
+    img = scene.render(sc.camera, rd)
+    npx = rd["width"] * rd["height"]
+    pool = ctx.mrg_pool(npx, rd["spp"] * rd["max_bounces"], seed=rd.get("seed", 0))
+    ref = oracle.OracleScene(sc, use_bvh=use_bvh).render(sc.camera, rd, pool)
+    scene.close()
+    return img, ref
+
+
+@pytest.mark.parametrize("rng_mode", [gbpt.GB_RNG_HALTON_LIGHT, gbpt.GB_RNG_MRG32K3A_POOL])
+def test_cornell_frame(gpu_ctx, rng_mode):
+    sc = scenes.cornell(width=64, height=48, spp=4, max_bounces=5)
+    rd = dict(sc.render, rng_mode=rng_mode)
+    img, ref = _render_pair(gpu_ctx, sc, rd, use_bvh=False)
+    _compare(img, ref)
+    assert img.mean() > 0.01
+
+
+def test_icospheres_frame_principled(gpu_ctx):
+    sc = scenes.icospheres(n_spheres=60, level=3, box=20.0, width=80, height=45, spp=3, max_bounces=6,
+                           rr_start=-1)
+    rd = dict(sc.render)
+    img, ref = _render_pair(gpu_ctx, sc, rd)
+    _compare(img, ref)
+
+
+def test_icospheres_frame_russian_roulette(gpu_ctx):
+    sc = scenes.icospheres(n_spheres=60, level=3, box=20.0, width=64, height=40, spp=2, max_bounces=8, rr_start=2)
+    rd = dict(sc.render)
+    img, ref = _render_pair(gpu_ctx, sc, rd)
+    _compare(img, ref)
+
+
+def test_thin_lens_frame(gpu_ctx):
+    sc = scenes.cornell(width=40, height=40, spp=3, max_bounces=3)
+    cam = dict(sc.camera, aperture=0.05, focus_distance=1.9)
+    rd = dict(sc.render, rng_mode=gbpt.GB_RNG_MRG32K3A_POOL)
+    from oracle import oracle
+    scene = gpu_ctx.scene(sc)
+    img = scene.render(cam, rd)
+    pool = gpu_ctx.mrg_pool(40 * 40, rd["spp"] * rd["max_bounces"])
+    ref = oracle.OracleScene(sc, use_bvh=False).render(cam, rd, pool)
+    scene.close()
+    _compare(img, ref)
+
+
+def test_progressive_steps_match_full_frame(gpu_ctx):
+    """gb_render_begin/step/read (gi_algorithm::update form) == gb_render."""
+    import ctypes as C
+    sc = scenes.cornell(width=32, height=32, spp=4, max_bounces=4)
+    rd = dict(sc.render)
+    scene = gpu_ctx.scene(sc)
+    full = scene.render(sc.camera, rd)
+    lib = gpu_ctx.lib
+    cam, desc = gbpt.make_camera(sc.camera), gbpt.make_render_desc(rd)
+    gpu_ctx.check(lib.gb_render_begin(gpu_ctx.h, scene.h, C.byref(cam), C.byref(desc)))
+    done = C.c_int()
+    for _ in range(4):
+        gpu_ctx.check(lib.gb_render_step(gpu_ctx.h, 1))
+    gpu_ctx.check(lib.gb_render_paths_done(gpu_ctx.h, C.byref(done)))
+    assert done.value == 4
+    out = np.empty_like(full)
+    gpu_ctx.check(lib.gb_render_read(gpu_ctx.h, out.ctypes.data_as(C.c_void_p), 0))
+    assert np.array_equal(out, full)
+    scene.close()
+
+
+def test_determinism_and_stats(gpu_ctx):
+    sc = scenes.cornell(width=48, height=48, spp=2, max_bounces=3)
+    scene = gpu_ctx.scene(sc)
+    a = scene.render(sc.camera, sc.render)
+    s1 = gpu_ctx.stats()
+    b = scene.render(sc.camera, sc.render, instrumented=True)
+    s2 = gpu_ctx.stats()
+    scene.close()
+    assert np.array_equal(a, b)
+    assert s1["camera_rays"] == 48 * 48 * 2
+    assert s1["extension_rays"] == s2["extension_rays"] and s1["shadow_rays"] == s2["shadow_rays"]
+    assert s2["closest_node_visits"] > 0 and s2["closest_tri_tests"] > 0 and s2["shadow_node_visits"] > 0
+
+
+def test_mrg_pool_streams(gpu_ctx):
+    """Update u of pixel i = draws 3u..3u+2 of curand MRG32k3a(seed, i): a later
+    window equals the tail of a longer one, values lie in (0, 1]."""
+    a = gpu_ctx.mrg_pool(100, 6)
+    b = gpu_ctx.mrg_pool(100, 2, first_update=4)
+    assert np.array_equal(a[4:], b)
+    assert (a > 0).all() and (a <= 1).all()
+    assert not np.array_equal(a[0, 0], a[0, 1])
