@@ -39,16 +39,21 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
     ap.add_argument("--workload", default="icospheres-1m", choices=["icospheres-1m", "small"])
-    ap.add_argument("--cpu-rows", type=int, default=0, help="rows of the CPU sample (0 = auto)")
+    ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling runs)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="minimum CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
 
-def workload(name: str):
+def workload(name: str, spp: int = 0):
     from globillum_gb300 import scenes
     if name == "small":
-        return scenes.icospheres(n_spheres=50, level=3, box=20.0, width=320, height=180, spp=4, max_bounces=8)
-    return scenes.icospheres()
+        sc = scenes.icospheres(n_spheres=50, level=3, box=20.0, width=320, height=180, spp=4, max_bounces=8)
+    else:
+        sc = scenes.icospheres()
+    if spp:
+        sc.render["spp"] = spp
+    return sc
 
 
 def config_of(sc, extra=None):
@@ -122,40 +127,46 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_sample(sc, rows: int, threads: int | None = None):
-    """Times the oracle (CPU restatement of the hybrid path) on `rows` rows
-    of the frame at 1 spp; returns (Mpaths/s, seconds, pixels, cores)."""
+def cpu_sample(sc, min_seconds: float, max_frames: int = 64, orc=None):
+    """Times the oracle (CPU restatement of the hybrid path, all host threads)
+    on whole frames of the workload at 1 spp until `min_seconds` have passed;
+    returns (Mpaths/s, seconds, frames, cores).  The BVH build is excluded."""
     from oracle import oracle
     rd = dict(sc.render, spp=1)
-    W, H = rd["width"], rd["height"]
-    row0 = max(0, H // 2 - rows // 2)
-    row1 = min(H, row0 + rows)
-    n = (row1 - row0) * W
-    # the pools' values do not change the amount of work; a seeded uniform
-    # pool keeps this leg off the GPU
-    pool = np.random.default_rng(11).uniform(1e-7, 1.0, size=(rd["max_bounces"], n, 3)).astype(np.float32)
-    if threads:
-        oracle.set_threads(threads)
-    orc = oracle.OracleScene(sc, use_bvh=True)
-    t0 = time.perf_counter()
-    orc.render(sc.camera, rd, pool, row0=row0, row1=row1)
-    dt = time.perf_counter() - t0
-    return n / dt / 1e6, dt, n, oracle.threads()
+    n = rd["width"] * rd["height"]
+    own = orc is None
+    if own:
+        orc = oracle.OracleScene(sc, use_bvh=True)
+    total, frames = 0.0, 0
+    while frames < max_frames and (total < min_seconds or frames == 0):
+        # the pool values do not change the amount of work on average; seeded
+        # uniform pools keep this leg off the GPU
+        pool = np.random.default_rng(11 + frames).uniform(1e-7, 1.0, size=(rd["max_bounces"], n, 3)).astype(
+            np.float32)
+        t0 = time.perf_counter()
+        orc.render(sc.camera, rd, pool)
+        total += time.perf_counter() - t0
+        frames += 1
+    if own:
+        orc.close()
+    return n * frames / total / 1e6, total, frames, oracle.threads()
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    sc = workload(args.workload)
-    rows = args.cpu_rows or (8 if args.workload == "icospheres-1m" else 32)
+    from oracle import oracle
+    sc = workload(args.workload, args.spp)
+    orc = oracle.OracleScene(sc, use_bvh=True)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, n, cores = cpu_sample(sc, rows)
+        v, dt, frames, cores = cpu_sample(sc, 0.0, max_frames=1, orc=orc)
         if i >= args.warmup:
             vals.append((v, dt))
-    v = float(np.mean([x[0] for x in vals]))
-    ms = float(np.mean([x[1] for x in vals])) * 1e3
-    sample = f"{rows} rows x {sc.render['width']} px at 1 spp of the frame (bounded sample), pools seeded uniform"
+    ms = float(np.sum([x[1] for x in vals])) * 1e3 / len(vals)
+    v = sc.render["width"] * sc.render["height"] * len(vals) / (ms * len(vals) / 1e3) / 1e6
+    sample = f"one whole {sc.render['width']}x{sc.render['height']} frame at 1 spp per step (bounded sample of " \
+             f"the {sc.render['spp']}-spp frame), seeded uniform pools"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(sc, {"sample": sample}),
@@ -174,7 +185,7 @@ def run_gbpt(args, rank, world):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    sc = workload(args.workload)
+    sc = workload(args.workload, args.spp)
     r = sc.render
     W, H, spp = r["width"], r["height"], r["spp"]
     stream = torch.cuda.current_stream()
@@ -276,10 +287,10 @@ def run_gbpt(args, rank, world):
                     "d2h_bytes_per_step": W * H * 3 * 4},
             "gpu_launches": int(launches)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rows = args.cpu_rows or (8 if args.workload == "icospheres-1m" else 32)
-        v, dt, n, cores = cpu_sample(sc, rows)
+        v, dt, frames, cores = cpu_sample(sc, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
-                                "sample": f"{rows} rows x {W} px at 1 spp of the same frame ({dt:.1f} s)"}
+                                "sample": f"{frames} whole {W}x{H} frames at 1 spp ({dt:.1f} s of CPU time, "
+                                          f"BVH build excluded)"}
     scene.close()
     ctx.close()
     if rank == 0:
