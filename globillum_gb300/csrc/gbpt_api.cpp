@@ -587,3 +587,12 @@ int gb_mrg_pool(gb_ctx* ctx, int npix, uint32_t seed, int first_update, int num_
 }
 
 }  // extern "C"
+
+namespace gb {
+// Internal views used by gb_render_noalloc (gbpt_noalloc.cu).
+const DevScene* scene_device_view(const gb_scene* s) { return s ? &s->S : nullptr; }
+int scene_device(const gb_scene* s) { return s && s->ctx ? s->ctx->device : -1; }
+void scene_set_error(const gb_scene* s, const char* msg) {
+    if (s && s->ctx) s->ctx->err = msg;
+}
+}  // namespace gb

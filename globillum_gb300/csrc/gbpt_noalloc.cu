@@ -1,0 +1,151 @@
+// gbpt_noalloc.cu -- gb_render_noalloc: the progressive frame of gb_render
+// without any device allocation.
+//
+// gb_render keeps its per-pixel wavefront state (rays, throughput,
+// accumulators, RNG streams, queues) in buffers a context allocates with
+// cudaMalloc on first use.  Some callers cannot allow that: a render loop
+// that runs while other work owns the device's memory through its own pool
+// (cudaMalloc and cudaFree synchronise the whole device and fragment such a
+// pool), or code on a path where the host must not block in the driver's
+// allocator.  For them this entry point keeps that state in one
+// file-scope __device__ array of fixed size instead.  Every GPU that loads
+// the library holds the array until the process exits.
+//
+// Limits: at most kNoAllocMaxPixels pixels (a 256 x 256 frame) and at most
+// kNoAllocMaxBounces bounces per call; larger requests return
+// GB_ERR_INVALID.  All calls share the one array, so calls whose work
+// overlaps on the GPU (two streams, or two host threads) race and corrupt
+// each other's frames: serialise them.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address (cudaGetSymbolAddress) and caches it; make that
+// first call before any stream capture on the device.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "../../include/gbpt.h"
+#include "gbpt_host.h"
+#include "gbpt_kernels.h"
+
+namespace gb {
+const DevScene* scene_device_view(const gb_scene* s);
+int scene_device(const gb_scene* s);
+void scene_set_error(const gb_scene* s, const char* msg);
+}  // namespace gb
+
+using namespace gb;
+
+namespace {
+
+constexpr int kNoAllocMaxPixels = 65536;
+constexpr int kNoAllocMaxBounces = 64;
+constexpr int kMaxDevices = 64;
+constexpr size_t kAlign = 256;
+
+constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+constexpr size_t kV4 = align_up(sizeof(float4) * (size_t)kNoAllocMaxPixels);  // one float4 per pixel
+constexpr size_t kRng = align_up(48 * (size_t)kNoAllocMaxPixels);             // curandStateMRG32k3a per pixel
+constexpr size_t kU32 = align_up(4 * (size_t)kNoAllocMaxPixels);              // one 32-bit word per pixel
+constexpr size_t kCtr = align_up(4 * 4 * (size_t)(kNoAllocMaxBounces + 1));
+constexpr size_t kStats = align_up(8 * 8);
+constexpr size_t kStatus = align_up(4);
+// 12 float4 planes, 2 RNG planes, draws + 3 queues, counters, stats, status
+constexpr size_t kScratchBytes = 12 * kV4 + 2 * kRng + 4 * kU32 + kCtr + kStats + kStatus;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_mutex;
+unsigned char* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the array on `dev` (current device), looked up once.
+cudaError_t scratch_on_device(int dev, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = (unsigned char*)p;
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+Frame carve(unsigned char* base, int w, int h) {
+    Frame F{};
+    F.w = w; F.h = h; F.n = w * h;
+    size_t off = 0;
+    float4** planes[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.out, &F.sh_o, &F.sh_d,
+                         &F.psc, &F.rnd, &F.hit_p, &F.hit_n, &F.jpool};
+    for (float4** p : planes) { *p = (float4*)(base + off); off += kV4; }
+    F.rng = base + off; off += kRng;
+    F.rngj = base + off; off += kRng;
+    F.draws = (int*)(base + off); off += kU32;
+    for (int k = 0; k < 3; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
+    F.ctr = (uint32_t*)(base + off); off += kCtr;
+    F.stats = (unsigned long long*)(base + off); off += kStats;
+    F.status = (uint32_t*)(base + off); off += kStatus;
+    return F;
+}
+
+int fail(const gb_scene* s, int code, const char* msg) {
+    scene_set_error(s, msg);
+    return code;
+}
+
+}  // namespace
+
+extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* d,
+                                 float* out_rgb, void* stream) {
+    if (!scene || !cam || !d || !out_rgb) return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: null argument");
+    if (d->width <= 0 || d->height <= 0 || d->spp <= 0 || d->max_bounces <= 0)
+        return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad resolution / spp / bounces");
+    if ((long long)d->width * d->height > kNoAllocMaxPixels)
+        return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: more than 65536 pixels (256 x 256) per call");
+    if (d->max_bounces > kNoAllocMaxBounces)
+        return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: more than 64 bounces");
+    if (d->rng_mode != GB_RNG_MRG32K3A_POOL && d->rng_mode != GB_RNG_HALTON_LIGHT)
+        return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad rng_mode");
+    if (!(cam->fovy_deg > 0.0f && cam->fovy_deg < 180.0f))
+        return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad fovy");
+    int dev = scene_device(scene);
+    if (dev < 0 || dev >= kMaxDevices) return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad scene device");
+    if (cudaSetDevice(dev) != cudaSuccess) { cudaGetLastError(); return fail(scene, GB_ERR_CUDA, "cudaSetDevice failed"); }
+    unsigned char* base = nullptr;
+    if (scratch_on_device(dev, &base) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(scene, GB_ERR_CUDA, "gb_render_noalloc: cudaGetSymbolAddress of the scratch array failed");
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const DevScene& S = *scene_device_view(scene);
+    Frame F = carve(base, d->width, d->height);
+    RenderParams P{};
+    P.cam = make_camera(*cam, d->width, d->height);
+    P.sp = make_shade_params(*d);
+    P.spp = d->spp;
+    P.L = d->max_bounces;
+    P.rng_mode = d->rng_mode;
+    P.seed = d->seed;
+    cudaError_t e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(F.status, 0, 4, st);
+    if (e == cudaSuccess) e = k_launch_rng_init(F, d->seed, st);
+    for (int p = 0; p < P.spp && e == cudaSuccess; ++p) {
+        e = cudaMemsetAsync(F.ctr, 0, 4 * 4 * (size_t)(P.L + 1), st);
+        if (e == cudaSuccess) e = k_launch_raygen(F, P, p, st);
+        for (int b = 0; b < P.L && e == cudaSuccess; ++b) {
+            e = k_launch_extend(S, F, P, p, b, false, st);
+            if (e == cudaSuccess) e = k_launch_shade(S, F, P, p, b, false, st);
+        }
+        if (e == cudaSuccess) e = k_launch_finalize(F, p, st);
+    }
+    if (e == cudaSuccess) e = k_launch_pack_rgb(F.out, F.n, out_rgb, st);
+    uint32_t status = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&status, F.status, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(scene, GB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (status) return fail(scene, GB_ERR_TRAVERSAL, "gb_render_noalloc: traversal bound exceeded");
+    return GB_OK;
+}

@@ -234,6 +234,24 @@ int gb_get_stats(const gb_ctx* ctx, gb_stats* stats);
 int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
                            const gb_render_desc* desc, float* out_rgb, int out_is_device);
 
+/* Allocation-free gb_render (no counterpart in the reference).  For callers
+ * that must not allocate device memory while rendering -- e.g. a loop that
+ * shares the GPU with work whose memory lives in its own pool, where
+ * cudaMalloc/cudaFree would synchronise the device and fragment that pool.
+ * The scene is created beforehand (gb_scene_create allocates); this call
+ * renders the same frame as gb_render into the caller's device buffer
+ * `out_rgb` (w*h*3 floats) on `stream` (NULL = legacy default stream), with
+ * its wavefront state in one fixed file-scope device array (about 19 MB,
+ * held by every GPU that loads the library until exit) instead of cudaMalloc.
+ * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) with
+ * that device current; make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race; serialise them.  Returns
+ * after the frame is finished; errors are reported through the scene's
+ * context (gb_last_error). */
+int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+                      float* out_rgb, void* stream);
+
 /* Bytes of one stored 8-wide node / triangle (for roofline arithmetic). */
 int gb_layout_sizes(int* node_bytes, int* tri_bytes);
 
