@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="minimum CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--refill", type=int, default=0, help="traversal refill threshold (0 = library default)")
+    ap.add_argument("--slots", type=int, default=0, help="paths in flight (0 = library default)")
     return ap.parse_args()
 
 
@@ -190,6 +192,8 @@ def run_gbpt(args, rank, world):
     W, H, spp = r["width"], r["height"], r["spp"]
     stream = torch.cuda.current_stream()
     ctx = gbpt.Context(local, stream.cuda_stream)
+    if args.refill or args.slots:
+        ctx.set_tuning(refill=args.refill, slots=args.slots)
     t0 = time.perf_counter()
     scene = ctx.scene(sc)
     upload_s = time.perf_counter() - t0
@@ -208,7 +212,7 @@ def run_gbpt(args, rank, world):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    times, stage_ms, stage_n, launches = [], np.zeros(4), np.zeros(4), 0
+    times, stage_ms, stage_n, launches = [], np.zeros(6), np.zeros(6), 0
     st_last = None
     for _ in range(args.steps):
         flush.zero_()
@@ -270,12 +274,15 @@ def run_gbpt(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config_of(sc, {"parallelism": f"replicas x{world}", "bvh_build_ms": info["build_ms"],
                                      "scene_upload_s": upload_s, "bvh_nodes": info["num_nodes"],
-                                     "bvh_depth": info["depth"]}),
+                                     "bvh_depth": info["depth"], "tuning": ctx.get_tuning()}),
             "mrays_per_s": mrays,
             "rays_per_frame": {"camera": ist["camera_rays"], "extension": ist["extension_rays"],
                                "shadow": ist["shadow_rays"]},
-            "stage_ms_per_frame": {"raygen": stage_ms[0] / args.steps, "closest_hit+light_sample": ext_ms,
-                                   "any_hit+shade": stage_ms[2] / args.steps, "accumulate": stage_ms[3] / args.steps},
+            "stage_ms_per_frame": {"path_start": stage_ms[0] / args.steps, "closest_hit+light_sample": ext_ms,
+                                   "any_hit": stage_ms[2] / args.steps, "shade": stage_ms[3] / args.steps,
+                                   "path_end+restart": stage_ms[4] / args.steps,
+                                   "moving_average": stage_ms[5] / args.steps},
+            "stage_launches_per_frame": [int(x / args.steps) for x in stage_n],
             "roofline": {"bound": "hbm", "kernel": "k_extend (closest-hit traversal + light sample)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": None,

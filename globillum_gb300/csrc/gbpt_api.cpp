@@ -21,16 +21,18 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+static const int kSnaps = 16;
+
 struct gb_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::string err;
-    // frame
+    // frame: per-slot, per-pixel and sample-buffer capacities
     Frame F{};
-    size_t frame_cap = 0;
-    int ctr_cap = 0;
-    std::vector<void*> frame_allocs;
+    size_t slot_cap = 0, pixel_cap = 0, sample_cap = 0;
+    std::vector<void*> slot_allocs, pixel_allocs, sample_allocs;
+    int chunk = 1;                      // path samples per chunk of the current render
     // progressive render
     gb_scene* scene = nullptr;
     RenderParams P{};
@@ -43,9 +45,19 @@ struct gb_ctx {
     gb_stats stats{};
     uint64_t launches = 0;
     bool stage_timing = false;
+    int refill = 16;                    // idle lanes that trigger a warp refill
+    int slots = 1 << 20;                // path slots in flight (upper bound; at most one per pixel)
+    int sample_mb = 1024;               // sample buffer budget (chunk size)
+    // queue-count snapshots: pinned ring + events (host stays a few iterations ahead)
+    uint32_t* snap_host = nullptr;
+    cudaEvent_t snap_ev[kSnaps] = {};
     std::vector<cudaEvent_t> ev_pool;   // stage timing events (pairs)
     std::vector<int> ev_stage;          // stage of each recorded pair
     size_t ev_used = 0;
+    // curand states right after curand_init(seed, pixel, 0) are kept in
+    // F.pristine while the seed and pixel buffer stay the same
+    size_t pristine_n = 0;
+    uint32_t pristine_seed = 0;
     // scratch for API calls with host pointers
     DevBuf scratch[4];
     float* d_rgb = nullptr;
@@ -100,28 +112,47 @@ cudaError_t ensure_scratch(gb_ctx* ctx, int k, size_t bytes) {
     return e;
 }
 
-cudaError_t ensure_frame(gb_ctx* ctx, int n, int L) {
-    if ((size_t)n <= ctx->frame_cap && L + 1 <= ctx->ctr_cap) return cudaSuccess;
-    cudaStreamSynchronize(ctx->stream);
-    free_all(ctx->frame_allocs);
-    ctx->frame_cap = 0;
-    ctx->ctr_cap = 0;
+// Per-slot buffers for `nslots` slots, per-pixel buffers for `n` pixels and a
+// sample buffer of `samples` float4 entries; grown on demand.
+cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples) {
     Frame& F = ctx->F;
-    size_t v4 = sizeof(float4) * (size_t)n;
-    float4** bufs[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.out, &F.sh_o, &F.sh_d,
-                       &F.psc, &F.rnd, &F.hit_p, &F.hit_n, &F.jpool};
     cudaError_t e;
-    for (float4** b : bufs)
-        if ((e = dalloc(ctx->frame_allocs, (void**)b, v4)) != cudaSuccess) return e;
-    if ((e = dalloc(ctx->frame_allocs, &F.rng, 48 * (size_t)n)) != cudaSuccess) return e;
-    if ((e = dalloc(ctx->frame_allocs, &F.rngj, 48 * (size_t)n)) != cudaSuccess) return e;
-    if ((e = dalloc(ctx->frame_allocs, (void**)&F.draws, sizeof(int) * (size_t)n)) != cudaSuccess) return e;
-    for (int k = 0; k < 3; ++k)
-        if ((e = dalloc(ctx->frame_allocs, (void**)&F.q[k], sizeof(uint32_t) * (size_t)n)) != cudaSuccess) return e;
-    int ctr_n = std::max(L + 1, 64);
-    if ((e = dalloc(ctx->frame_allocs, (void**)&F.ctr, sizeof(uint32_t) * 4 * (size_t)ctr_n)) != cudaSuccess) return e;
-    ctx->frame_cap = (size_t)n;
-    ctx->ctr_cap = ctr_n;
+    if ((size_t)nslots > ctx->slot_cap) {
+        cudaStreamSynchronize(ctx->stream);
+        free_all(ctx->slot_allocs);
+        ctx->slot_cap = 0;
+        size_t v4 = sizeof(float4) * (size_t)nslots;
+        float4** bufs[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
+        for (float4** b : bufs)
+            if ((e = dalloc(ctx->slot_allocs, (void**)b, v4)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, &F.rng, 48 * (size_t)nslots)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.pix, 4 * (size_t)nslots)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.pb, 4 * (size_t)nslots)) != cudaSuccess) return e;
+        for (int k = 0; k < 4; ++k)
+            if ((e = dalloc(ctx->slot_allocs, (void**)&F.q[k], 4 * (size_t)nslots)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.ctr, 4 * 32)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.path_ctr, 4 * 8)) != cudaSuccess) return e;
+        ctx->slot_cap = (size_t)nslots;
+    }
+    if ((size_t)n > ctx->pixel_cap) {
+        cudaStreamSynchronize(ctx->stream);
+        free_all(ctx->pixel_allocs);
+        ctx->pixel_cap = 0;
+        ctx->pristine_n = 0;
+        if ((e = dalloc(ctx->pixel_allocs, (void**)&F.out, sizeof(float4) * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, &F.pristine, 48 * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, &F.cursor, 48 * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, &F.jcursor, 48 * (size_t)n)) != cudaSuccess) return e;
+        ctx->pixel_cap = (size_t)n;
+    }
+    if (samples > ctx->sample_cap) {
+        cudaStreamSynchronize(ctx->stream);
+        free_all(ctx->sample_allocs);
+        ctx->sample_cap = 0;
+        if ((e = dalloc(ctx->sample_allocs, (void**)&F.samples, sizeof(float4) * samples)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->sample_allocs, (void**)&F.jpool, sizeof(float4) * samples)) != cudaSuccess) return e;
+        ctx->sample_cap = samples;
+    }
     return cudaSuccess;
 }
 
@@ -196,6 +227,8 @@ int gb_ctx_create(const gb_ctx_desc* desc, gb_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(unsigned long long) * 8);
     if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_stats, 0, sizeof(unsigned long long) * 8);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&ctx->snap_host, sizeof(uint32_t) * kSnaps, cudaHostAllocDefault);
+    for (int k = 0; k < kSnaps && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->snap_ev[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         gb_ctx_destroy(ctx);
@@ -209,8 +242,12 @@ void gb_ctx_destroy(gb_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    free_all(ctx->frame_allocs);
+    free_all(ctx->slot_allocs);
+    free_all(ctx->pixel_allocs);
+    free_all(ctx->sample_allocs);
     for (auto& s : ctx->scratch) if (s.p) cudaFree(s.p);
+    if (ctx->snap_host) cudaFreeHost(ctx->snap_host);
+    for (int k = 0; k < kSnaps; ++k) if (ctx->snap_ev[k]) cudaEventDestroy(ctx->snap_ev[k]);
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_stats) cudaFree(ctx->d_stats);
@@ -353,12 +390,23 @@ int gb_render_begin(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb
     int rc = check_render_desc(ctx, cam, d);
     if (rc != GB_OK) return rc;
     CK(cudaSetDevice(ctx->device));
-    int n = d->width * d->height;
-    CK(ensure_frame(ctx, n, d->max_bounces));
+    const int n = d->width * d->height;
+    // chunk: path samples per pass of the slot pool (bounded by the sample
+    // buffer budget and by 2^31 paths); slots: paths in flight
+    long long budget = (long long)ctx->sample_mb << 20;
+    int chunk = (int)std::max(1ll, std::min<long long>(d->spp, budget / (16ll * n)));
+    chunk = (int)std::min<long long>(chunk, std::max(1ll, (1ll << 31) / n - 1));
+    long long chunk_paths = (long long)chunk * n;
+    // at most one slot per pixel: a launch then starts at most one path per
+    // pixel, which keeps the per-pixel stream cursors unshared
+    int nslots = (int)std::max(1ll, std::min<long long>(std::min<long long>(chunk_paths, n), ctx->slots));
+    CK(ensure_frame(ctx, n, nslots, (size_t)chunk_paths));
     Frame& F = ctx->F;
     F.w = d->width; F.h = d->height; F.n = n;
+    F.nslots = nslots;
     F.stats = ctx->d_stats;
     F.status = ctx->d_status;
+    ctx->chunk = chunk;
     RenderParams& P = ctx->P;
     P.cam = make_camera(*cam, d->width, d->height);
     P.sp = make_shade_params(*d);
@@ -366,47 +414,108 @@ int gb_render_begin(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb
     P.L = d->max_bounces;
     P.rng_mode = d->rng_mode;
     P.seed = d->seed;
+    P.refill = ctx->refill;
     ctx->scene = scene;
     ctx->paths_done = 0;
     ctx->active = true;
+    ctx->launches = 0;
+    ctx->ev_used = 0;
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * 8, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
-    ctx->launches = 1;
-    ctx->ev_used = 0;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    CK(k_launch_rng_init(F, d->seed, ctx->stream));
+    if (!(ctx->pristine_seed == d->seed && ctx->pristine_n >= (size_t)n)) {
+        CK(k_launch_rng_init(n, d->seed, F.pristine, ctx->stream));
+        ctx->launches += 1;
+        ctx->pristine_n = (size_t)n;
+        ctx->pristine_seed = d->seed;
+    }
+    // both streams of pixel i restart at curand_init(seed, i, 0)
+    CK(cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
     return GB_OK;
 }
+
+namespace {
+
+// Path samples [p0, p1) of every pixel through the slot pool.
+int run_chunk(gb_ctx* ctx, int p0, int p1) {
+    RenderParams& P = ctx->P;
+    const Frame& F = ctx->F;
+    const DevScene& S = ctx->scene->S;
+    P.p0 = p0;
+    P.chunk_paths = (p1 - p0) * F.n;
+    const int nstart = std::min(F.nslots, P.chunk_paths);
+    CK(cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, ctx->stream));
+    CK(stage_mark(ctx, 0, true));
+    CK(k_launch_jitter_pool(F, p0, p1, ctx->stream));
+    CK(k_launch_start(F, P, nstart, ctx->stream));
+    CK(stage_mark(ctx, 0, false));
+    ctx->launches += 2;
+    // iterations until the next extension queue is empty; the host checks
+    // that count through snapshots and stays at most kLead iterations ahead
+    const long long max_iters = (long long)P.chunk_paths * P.L + 8;
+    const int kEvery = 2, kLead = 12;
+    int snap_it[kSnaps];
+    int head = 0, tail = 0;  // pending snapshots [tail, head)
+    bool done = false;
+    for (long long it = 0; !done; ++it) {
+        if (it >= max_iters) return fail(ctx, GB_ERR_TRAVERSAL, "path iteration bound exceeded");
+        const int ii = (int)(it % 3000000);
+        CK(cudaMemsetAsync(F.ctr + 8 * ((ii + 1) % 3), 0, sizeof(uint32_t) * 8, ctx->stream));
+        CK(stage_mark(ctx, 1, true));
+        CK(k_launch_extend(S, F, P, ii, ctx->instrument, ctx->stream));
+        CK(stage_mark(ctx, 1, false));
+        CK(stage_mark(ctx, 2, true));
+        CK(k_launch_shadow(S, F, P, ii, ctx->instrument, ctx->stream));
+        CK(stage_mark(ctx, 2, false));
+        CK(stage_mark(ctx, 3, true));
+        CK(k_launch_shade(S, F, P, ii, ctx->stream));
+        CK(stage_mark(ctx, 3, false));
+        CK(stage_mark(ctx, 4, true));
+        CK(k_launch_regen(F, P, ii, ctx->stream));
+        CK(stage_mark(ctx, 4, false));
+        ctx->launches += 4;
+        if (it % kEvery == kEvery - 1) {
+            int k = head % kSnaps;
+            CK(cudaMemcpyAsync(ctx->snap_host + k, F.ctr + 8 * ((ii + 1) % 3), sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaEventRecord(ctx->snap_ev[k], ctx->stream));
+            snap_it[k] = (int)it;
+            ++head;
+        }
+        while (tail < head) {
+            int k = tail % kSnaps;
+            bool must_wait = (it - snap_it[k] >= kLead) || head - tail >= kSnaps;
+            if (must_wait) CK(cudaEventSynchronize(ctx->snap_ev[k]));
+            else {
+                cudaError_t q = cudaEventQuery(ctx->snap_ev[k]);
+                if (q == cudaErrorNotReady) break;
+                if (q != cudaSuccess) return cuda_fail(ctx, q, "snapshot event");
+            }
+            if (ctx->snap_host[k] == 0u) done = true;
+            ++tail;
+        }
+    }
+    CK(stage_mark(ctx, 5, true));
+    CK(k_launch_combine(F, p0, p1, ctx->stream));
+    CK(stage_mark(ctx, 5, false));
+    ctx->launches += 1;
+    return GB_OK;
+}
+
+}  // namespace
 
 int gb_render_step(gb_ctx* ctx, int paths) {
     if (!ctx || !ctx->active || !ctx->scene) return fail(ctx, GB_ERR_INVALID, "no render in progress");
     if (paths < 0) return fail(ctx, GB_ERR_INVALID, "negative path count");
     CK(cudaSetDevice(ctx->device));
-    const RenderParams& P = ctx->P;
-    const Frame& F = ctx->F;
-    const DevScene& S = ctx->scene->S;
-    int end = std::min(P.spp, ctx->paths_done + paths);
-    for (int p = ctx->paths_done; p < end; ++p) {
-        CK(cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 4 * (size_t)(P.L + 1), ctx->stream));
-        CK(stage_mark(ctx, 0, true));
-        CK(k_launch_raygen(F, P, p, ctx->stream));
-        CK(stage_mark(ctx, 0, false));
-        ctx->launches += P.cam.aperture != 0.0f ? 2 : 1;
-        for (int b = 0; b < P.L; ++b) {
-            CK(stage_mark(ctx, 1, true));
-            CK(k_launch_extend(S, F, P, p, b, ctx->instrument, ctx->stream));
-            CK(stage_mark(ctx, 1, false));
-            CK(stage_mark(ctx, 2, true));
-            CK(k_launch_shade(S, F, P, p, b, ctx->instrument, ctx->stream));
-            CK(stage_mark(ctx, 2, false));
-            ctx->launches += 2;
-        }
-        CK(stage_mark(ctx, 3, true));
-        CK(k_launch_finalize(F, p, ctx->stream));
-        CK(stage_mark(ctx, 3, false));
-        ctx->launches += 1;
+    int end = std::min(ctx->P.spp, ctx->paths_done + paths);
+    while (ctx->paths_done < end) {
+        int p1 = std::min(end, ctx->paths_done + ctx->chunk);
+        int rc = run_chunk(ctx, ctx->paths_done, p1);
+        if (rc != GB_OK) return rc;
+        ctx->paths_done = p1;
     }
-    ctx->paths_done = end;
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     return GB_OK;
 }
@@ -423,6 +532,7 @@ int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device) {
     CK(cudaSetDevice(ctx->device));
     int n = ctx->F.n;
     size_t bytes = sizeof(float) * 3 * (size_t)n;
+    if (ctx->paths_done == 0) CK(cudaMemsetAsync(ctx->F.out, 0, sizeof(float4) * (size_t)n, ctx->stream));
     if (out_is_device) {
         CK(k_launch_pack_rgb(ctx->F.out, n, out_rgb, ctx->stream));
         ctx->launches += 1;
@@ -450,7 +560,7 @@ int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device) {
     ctx->stats.shadow_tri_tests = st[6];
     ctx->stats.kernel_launches = ctx->launches;
     ctx->stats.paths_done = ctx->paths_done;
-    for (int k = 0; k < 4; ++k) { ctx->stats.stage_ms[k] = 0.0; ctx->stats.stage_launches[k] = 0; }
+    for (int k = 0; k < 6; ++k) { ctx->stats.stage_ms[k] = 0.0; ctx->stats.stage_launches[k] = 0; }
     for (size_t i = 0; i < ctx->ev_used; ++i) {
         float ems = 0.0f;
         if (cudaEventElapsedTime(&ems, ctx->ev_pool[2 * i], ctx->ev_pool[2 * i + 1]) == cudaSuccess) {
@@ -485,6 +595,24 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, c
 int gb_get_stats(const gb_ctx* ctx, gb_stats* stats) {
     if (!ctx || !stats) return GB_ERR_INVALID;
     *stats = ctx->stats;
+    return GB_OK;
+}
+
+int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* t) {
+    if (!ctx || !t) return fail(ctx, GB_ERR_INVALID, "null argument");
+    if (t->refill < 0 || t->refill > 32) return fail(ctx, GB_ERR_INVALID, "refill must be in 1..32");
+    if (t->slots < 0 || t->sample_mb < 0) return fail(ctx, GB_ERR_INVALID, "negative tuning value");
+    if (t->refill) ctx->refill = t->refill;
+    if (t->slots) ctx->slots = t->slots;
+    if (t->sample_mb) ctx->sample_mb = t->sample_mb;
+    return GB_OK;
+}
+
+int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* t) {
+    if (!ctx || !t) return GB_ERR_INVALID;
+    t->refill = ctx->refill;
+    t->slots = ctx->slots;
+    t->sample_mb = ctx->sample_mb;
     return GB_OK;
 }
 

@@ -1,20 +1,22 @@
 // gbpt_kernels.cu -- sm_103a kernels of the GB300 path-tracing hot path.
 //
-// Wavefront per path sample (one "generation" = path p of every pixel):
-//   k_raygen   camera rays (raygen.cu:61-118), jitter stream, stream skip
-//   per bounce b:
-//     k_extend  closest-hit traversal of the extension queue; misses add
-//               handle_no_hit's contribution (hybrid-pt.cpp:196-206); hits
-//               draw the bounce's 3 uniforms and emit the area-light shadow
-//               ray (arealight-sampler-cpu.cpp:25-143) into the shadow queue
-//     k_shade   any-hit traversal of the shadow queue fused with the
-//               BRDF sample/eval and throughput update of
-//               compute_path_contribution_and_bounce (hybrid-pt.cpp:450-584);
-//               surviving paths go to the next extension queue
-//   k_finalize moving average of the finished path into the image
-//              (new_path -> combine_color_samples, util-kernels.cu:17-25)
-// Queues are compacted with one warp ballot + one atomic per warp; queue
-// kernels run a persistent grid that fetches 32 rays per warp at a time.
+// The progressive frame runs as a wavefront over a pool of path slots.  The
+// paths of a chunk (samples p0..p1-1 of every pixel) are handed out to the
+// slots in path order; a slot whose path ends stores the path's sample and
+// takes the next path, so every iteration works on a full queue until the
+// chunk runs dry.  One iteration:
+//   k_extend  closest-hit traversal of the extension queue; misses add
+//             handle_no_hit's contribution (hybrid-pt.cpp:196-206) and end
+//             the path; hits draw the bounce's uniforms and emit the
+//             area-light shadow ray (arealight-sampler-cpu.cpp:25-143)
+//   k_shadow  any-hit traversal of the shadow queue
+//   k_shade   BRDF sample/eval, NEE accumulation, throughput and next ray of
+//             compute_path_contribution_and_bounce (hybrid-pt.cpp:450-584)
+// then k_combine folds the chunk's samples into the image with new_path's
+// moving average (util-kernels.cu:17-25), in path order per pixel, so the
+// image equals the reference's pixel-sequential one bit for bit.
+// Queues are compacted with one warp ballot + one atomic per warp; traversal
+// kernels run persistent warps that refill idle lanes from the queue.
 //
 // Traversal: compressed 8-wide BVH (80 B nodes, 8-bit quantised child
 // boxes), node-group stack of 32 entries, octant-ordered child visits,
@@ -23,6 +25,8 @@
 #include "gbpt_kernels.h"
 
 #include <curand_kernel.h>
+
+#include <algorithm>
 
 namespace gb {
 
@@ -34,7 +38,11 @@ constexpr int kIterLimit = 1 << 22;
 
 __device__ __forceinline__ v3 ld3(const float4 a) { return mk(a.x, a.y, a.z); }
 
-__device__ __forceinline__ float byte_f(uint32_t w, int sh) { return (float)((w >> sh) & 0xffu); }
+// Byte j of w as a float, exactly: the byte is placed in the mantissa of
+// 2^23 (one PRMT) and 2^23 is subtracted (one FADD).
+__device__ __forceinline__ float byte_f(uint32_t w, uint32_t j) {
+    return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | j)) - 8388608.0f;
+}
 
 struct RayInv {
     v3 o, d, idir;
@@ -55,6 +63,9 @@ __device__ __forceinline__ RayInv make_ray(v3 o, v3 d) {
 
 // Intersects the 8 children of node `ni`; returns the node group (child
 // base, hit bits 24-31 in visit order | imask) and the triangle group.
+// Per axis the near and far planes are chosen once per node from the sign
+// of the inverse direction (fma is monotonic in the plane index, so this
+// equals taking min/max of the two plane distances per child).
 __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes, uint32_t ni, const RayInv& r,
                                                float bound, uint2* ng, uint2* tg) {
     const float4* n = nodes + 5 * (size_t)ni;
@@ -66,6 +77,7 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
     uint32_t imask = ew >> 24;
     float aix = sx * r.idir.x, aiy = sy * r.idir.y, aiz = sz * r.idir.z;
     float aox = (n0.x - r.o.x) * r.idir.x, aoy = (n0.y - r.o.y) * r.idir.y, aoz = (n0.z - r.o.z) * r.idir.z;
+    const bool fx = r.idir.x < 0.0f, fy = r.idir.y < 0.0f, fz = r.idir.z < 0.0f;
     uint32_t hits_n = 0, hits_t = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -73,19 +85,19 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
         uint32_t qlx = __float_as_uint(half ? n2.y : n2.x), qly = __float_as_uint(half ? n2.w : n2.z);
         uint32_t qlz = __float_as_uint(half ? n3.y : n3.x), qhx = __float_as_uint(half ? n3.w : n3.z);
         uint32_t qhy = __float_as_uint(half ? n4.y : n4.x), qhz = __float_as_uint(half ? n4.w : n4.z);
+        uint32_t nx = fx ? qhx : qlx, fxw = fx ? qlx : qhx;
+        uint32_t ny = fy ? qhy : qly, fyw = fy ? qly : qhy;
+        uint32_t nz = fz ? qhz : qlz, fzw = fz ? qlz : qhz;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int sh = 8 * j;
-            const int slot = 4 * half + j;
-            uint32_t meta = (meta_w >> sh) & 0xffu;
-            float x0 = fmaf(byte_f(qlx, sh), aix, aox), x1 = fmaf(byte_f(qhx, sh), aix, aox);
-            float y0 = fmaf(byte_f(qly, sh), aiy, aoy), y1 = fmaf(byte_f(qhy, sh), aiy, aoy);
-            float z0 = fmaf(byte_f(qlz, sh), aiz, aoz), z1 = fmaf(byte_f(qhz, sh), aiz, aoz);
-            float tmin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
-            float tmax = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
-            float lo = fmaxf(tmin * 0.99999f, 0.0f);
-            float hi = fminf(tmax * 1.00001f, bound);
-            if (meta != 0u && lo <= hi) {
+        for (uint32_t j = 0; j < 4; ++j) {
+            const int slot = 4 * half + (int)j;
+            uint32_t meta = (meta_w >> (8 * j)) & 0xffu;
+            float tnx = fmaf(byte_f(nx, j), aix, aox), tfx = fmaf(byte_f(fxw, j), aix, aox);
+            float tny = fmaf(byte_f(ny, j), aiy, aoy), tfy = fmaf(byte_f(fyw, j), aiy, aoy);
+            float tnz = fmaf(byte_f(nz, j), aiz, aoz), tfz = fmaf(byte_f(fzw, j), aiz, aoz);
+            float lo = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f)) * 0.99999f;
+            float hi = fminf(fminf(tfx, tfy), tfz) * 1.00001f;
+            if (meta != 0u && lo <= fminf(hi, bound)) {
                 if ((imask >> slot) & 1u) hits_n |= 1u << (24 + (slot ^ r.oxor));
                 else hits_t |= (meta >> 5) << (meta & 31u);
             }
@@ -95,62 +107,80 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
     *tg = make_uint2(__float_as_uint(n1.y), hits_t);
 }
 
+// Resumable traversal state of one ray (the node-group stack lives beside it).
+struct Trav {
+    uint2 ng, tg;
+    int sp;
+    float best_t, bb, bg;
+    uint32_t best_id;
+};
+
+__device__ __forceinline__ void trav_init(Trav& s, const RayInv& r) {
+    s.ng = make_uint2(0u, 0x80000000u | (1u << (r.oxor ^ 7u)));
+    s.tg = make_uint2(0u, 0u);
+    s.sp = 0;
+    s.best_t = FLT_MAX;
+    s.best_id = 0xffffffffu;
+    s.bb = 0.0f;
+    s.bg = 0.0f;
+}
+
+// One traversal step: every pending triangle of the current group, then one
+// node (or a stack pop).  Returns true when the ray is finished; the result
+// is the (t, id)-minimum in s (any-hit: best_id != none when found).
+template <bool ANY, bool INSTR>
+__device__ __forceinline__ bool trav_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint2* stack,
+                                          uint32_t* status, uint32_t* nvis, uint32_t* ntri) {
+    while (s.tg.y != 0u) {
+        int b = __ffs(s.tg.y) - 1;
+        s.tg.y &= s.tg.y - 1u;
+        const float4* tp = S.tris + 3 * (size_t)(s.tg.x + (uint32_t)b);
+        float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
+        if (INSTR) ++*ntri;
+        float t, u, v;
+        if (intersect_tri(r.o, r.d, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= tmax) {
+            uint32_t id = __float_as_uint(a0.w);
+            if (ANY) { s.best_t = t; s.best_id = id; return true; }
+            if (closer(t, id, s.best_t, s.best_id)) { s.best_t = t; s.best_id = id; s.bb = u; s.bg = v; }
+        }
+    }
+    if (s.ng.y > 0x00ffffffu) {
+        uint32_t k = 31u - (uint32_t)__clz(s.ng.y);
+        s.ng.y &= ~(1u << k);
+        uint32_t slot = (k - 24u) ^ r.oxor;
+        uint32_t imask = s.ng.y & 0xffu;
+        uint32_t child = s.ng.x + (uint32_t)__popc(imask & ((1u << slot) - 1u));
+        if (s.ng.y > 0x00ffffffu) {
+            if (s.sp >= kStack) { atomicOr(status, ST_STACK_OVERFLOW); return true; }
+            stack[s.sp++] = s.ng;
+        }
+        if (INSTR) ++*nvis;
+        intersect_node(S.nodes, child, r, fminf(s.best_t, tmax), &s.ng, &s.tg);
+        return false;
+    }
+    if (s.sp > 0) { s.ng = stack[--s.sp]; return false; }
+    return true;
+}
+
 struct TraceOut {
     float t, beta, gamma;
     uint32_t id;
 };
 
-// Closest (ANY=false) or any (ANY=true) hit with 0 < t <= tmax.
-template <bool ANY, bool INSTR>
+// Whole traversal of one ray (API tracing kernel).
+template <bool ANY>
 __device__ __forceinline__ bool traverse(const DevScene& S, const RayInv& r, float tmax, TraceOut* out,
-                                         uint32_t* status, uint32_t* nvis, uint32_t* ntri) {
-    float best_t = FLT_MAX;
-    uint32_t best_id = 0xffffffffu;
-    float bb = 0.0f, bg = 0.0f;
+                                         uint32_t* status) {
+    Trav s;
+    trav_init(s, r);
     uint2 stack[kStack];
-    int sp = 0;
-    uint32_t oct = r.oxor ^ 7u;
-    uint2 ng = make_uint2(0u, 0x80000000u | (1u << oct));
-    uint2 tg = make_uint2(0u, 0u);
+    uint32_t nv = 0, nt = 0;
     int iters = 0;
-    bool found = false;
-    while (true) {
-        while (tg.y != 0u) {
-            int b = __ffs(tg.y) - 1;
-            tg.y &= tg.y - 1u;
-            const float4* tp = S.tris + 3 * (size_t)(tg.x + (uint32_t)b);
-            float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
-            if (INSTR) ++*ntri;
-            float t, u, v;
-            if (intersect_tri(r.o, r.d, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= tmax) {
-                uint32_t id = __float_as_uint(a0.w);
-                if (ANY) { found = true; tg.y = 0u; ng.y = 0u; sp = 0; break; }
-                if (closer(t, id, best_t, best_id)) { best_t = t; best_id = id; bb = u; bg = v; }
-            }
-        }
-        if (ANY && found) break;
-        if (ng.y > 0x00ffffffu) {
-            uint32_t k = 31u - (uint32_t)__clz(ng.y);
-            ng.y &= ~(1u << k);
-            uint32_t slot = (k - 24u) ^ r.oxor;
-            uint32_t imask = ng.y & 0xffu;
-            uint32_t child = ng.x + (uint32_t)__popc(imask & ((1u << slot) - 1u));
-            if (ng.y > 0x00ffffffu) {
-                if (sp >= kStack) { atomicOr(status, ST_STACK_OVERFLOW); break; }
-                stack[sp++] = ng;
-            }
-            if (INSTR) ++*nvis;
-            intersect_node(S.nodes, child, r, fminf(best_t, tmax), &ng, &tg);
-        } else if (sp > 0) {
-            ng = stack[--sp];
-        } else {
-            break;
-        }
+    while (!trav_step<ANY, false>(S, r, tmax, s, stack, status, &nv, &nt)) {
         if (++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); break; }
     }
-    if (ANY) return found;
-    out->t = best_t; out->beta = bb; out->gamma = bg; out->id = best_id;
-    return best_id != 0xffffffffu;
+    if (out) { out->t = s.best_t; out->beta = s.bb; out->gamma = s.bg; out->id = s.best_id; }
+    return s.best_id != 0xffffffffu;
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -171,6 +201,12 @@ __device__ __forceinline__ void add_stats(unsigned long long* s, uint32_t v) {
     if (lane_id() == 0u && w) atomicAdd(s, (unsigned long long)w);
 }
 
+// One count from a (possibly divergent) lane.
+__device__ __forceinline__ void add_stats_lane(unsigned long long* s) {
+    uint32_t m = __activemask();
+    if (lane_id() == (uint32_t)__ffs(m) - 1u) atomicAdd(s, (unsigned long long)__popc(m));
+}
+
 // ----------------------------------------------------------------- kernels
 
 __global__ void __launch_bounds__(kBlock) k_trace(DevScene S, int n, const float* __restrict__ orig,
@@ -182,26 +218,15 @@ __global__ void __launch_bounds__(kBlock) k_trace(DevScene S, int n, const float
     v3 d = mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
     float tmax = tmaxv[i];
     RayInv r = make_ray(o, d);
-    uint32_t nv = 0, nt = 0;
     if (any) {
-        bool f = (tmax >= 0.0f) && traverse<true, false>(S, r, tmax, nullptr, status, &nv, &nt);
+        bool f = (tmax >= 0.0f) && traverse<true>(S, r, tmax, nullptr, status);
         occluded[i] = f ? 1 : 0;
     } else {
         TraceOut h;
-        if (tmax >= 0.0f) traverse<false, false>(S, r, tmax, &h, status, &nv, &nt);
+        if (tmax >= 0.0f) traverse<false>(S, r, tmax, &h, status);
         else { h.t = FLT_MAX; h.beta = 0.0f; h.gamma = 0.0f; h.id = 0xffffffffu; }
         hits[i] = make_float4(h.t, h.beta, h.gamma, __uint_as_float(h.id));
     }
-}
-
-__global__ void k_rng_init(int n, uint32_t seed, curandStateMRG32k3a* rng, curandStateMRG32k3a* rngj, int* draws) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    curandStateMRG32k3a s;
-    curand_init((unsigned long long)seed, (unsigned long long)i, 0ull, &s);
-    rng[i] = s;
-    rngj[i] = s;
-    draws[i] = 0;
 }
 
 __device__ __forceinline__ v3 draw3(curandStateMRG32k3a* s) {
@@ -211,101 +236,238 @@ __device__ __forceinline__ v3 draw3(curandStateMRG32k3a* s) {
     return mk(x, y, z);
 }
 
-// Jitter pool for the thin-lens camera (the lens sample reads another pixel).
-__global__ void k_jitter_pool(Frame F) {
+// curand states right after curand_init(seed, pixel, 0) (util-kernels.cu:277-285).
+__global__ void k_rng_init(int n, uint32_t seed, curandStateMRG32k3a* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= F.n) return;
-    curandStateMRG32k3a* js = (curandStateMRG32k3a*)F.rngj;
-    curandStateMRG32k3a s = js[i];
-    v3 j = draw3(&s);
-    js[i] = s;
-    F.jpool[i] = make_float4(j.x, j.y, j.z, 0.0f);
+    if (i >= n) return;
+    curandStateMRG32k3a s;
+    curand_init((unsigned long long)seed, (unsigned long long)i, 0ull, &s);
+    out[i] = s;
 }
 
-__global__ void __launch_bounds__(kBlock) k_raygen(Frame F, RenderParams P, int path, int use_pool) {
+// ------------------------------------------------------------ path slots --
+// A slot carries one path (pixel, sample p) at a time; path l of a chunk is
+// (p, pixel) = (p0 + l / n, l % n).  The reference's three identically
+// seeded per-pixel pools (hybrid-pt.cpp:83-95, util-kernels.cu:284) become:
+//   camera jitter  = update p of the pixel's stream, read from the chunk's
+//                    jitter pool (k_jitter_pool walks each pixel's stream)
+//   lens sample    = update p of pixel (pixel+17)%n (raygen.cu:100-106)
+//   light/path     = updates pL, pL+1, ... one per bounce (hybrid-pt.h:229-233),
+//                    handed out by a per-pixel stream cursor that is advanced
+//                    by L updates whenever a path of the pixel starts.
+// A launch starts at most one path per pixel (the slot pool never holds more
+// paths than pixels and paths are started in path order), so the cursor is
+// never shared within a launch.
+__global__ void k_jitter_pool(Frame F, int p0, int p1) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) atomicAdd(&F.stats[0], (unsigned long long)F.n);
     if (i >= F.n) return;
-    if (path == 0) F.out[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    F.tp[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    F.accum[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    v3 j;
+    curandStateMRG32k3a* jc = (curandStateMRG32k3a*)F.jcursor;
+    curandStateMRG32k3a s = jc[i];
+    for (int p = p0; p < p1; ++p) {
+        v3 j = draw3(&s);
+        F.jpool[(size_t)(p - p0) * (size_t)F.n + (size_t)i] = make_float4(j.x, j.y, j.z, 0.0f);
+    }
+    jc[i] = s;
+}
+
+__device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t l) {
+    const uint32_t pixel = l % (uint32_t)F.n;
+    const uint32_t pc = l / (uint32_t)F.n;  // path within the chunk
+    const float4* jp = F.jpool + (size_t)pc * (size_t)F.n;
+    float4 j = jp[pixel];
     float lx = 0.0f, ly = 0.0f;
-    if (use_pool) {
-        float4 jp = F.jpool[i];
-        j = mk(jp.x, jp.y, jp.z);
-        // raygen.cu:100-106: one lens sample from pixel (id+17)%n (the loop
-        // condition never holds since |(z-.5, y-.5)| < 1)
-        float4 lp = F.jpool[(i + 17) % F.n];
-        lx = lp.z - 0.5f;
-        ly = lp.y - 0.5f;
-    } else {
-        curandStateMRG32k3a* js = (curandStateMRG32k3a*)F.rngj;
-        curandStateMRG32k3a s = js[i];
-        j = draw3(&s);
-        js[i] = s;
+    if (P.cam.aperture != 0.0f) {
+        float4 lj = jp[(pixel + 17u) % (uint32_t)F.n];
+        lx = lj.z - 0.5f;
+        ly = lj.y - 0.5f;
     }
-    // position the light/path stream at update path*L (paths that ended
-    // early still consume their remaining updates, as the pools do)
-    int target = path * P.L;
-    int d = F.draws[i];
-    if (d < target) {
-        curandStateMRG32k3a* rs = (curandStateMRG32k3a*)F.rng;
-        curandStateMRG32k3a s = rs[i];
-        for (; d < target; ++d) (void)draw3(&s);
-        rs[i] = s;
-        F.draws[i] = d;
-    }
-    int x = i % F.w, y = i / F.w;
-    v3 o, dir;
-    camera_ray(P.cam, x, y, j.x, j.y, lx, ly, &o, &dir);
-    F.ray_o[i] = make_float4(o.x, o.y, o.z, FLT_MAX);
-    F.ray_d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+    curandStateMRG32k3a* cur = (curandStateMRG32k3a*)F.cursor;
+    curandStateMRG32k3a bs = cur[pixel];
+    ((curandStateMRG32k3a*)F.rng)[slot] = bs;
+    for (int u = 0; u < P.L; ++u) (void)draw3(&bs);
+    cur[pixel] = bs;
+    v3 o, d;
+    camera_ray(P.cam, (int)(pixel % (uint32_t)F.w), (int)(pixel / (uint32_t)F.w), j.x, j.y, lx, ly, &o, &d);
+    F.ray_o[slot] = make_float4(o.x, o.y, o.z, FLT_MAX);
+    F.ray_d[slot] = make_float4(d.x, d.y, d.z, 0.0f);
+    F.tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    F.accum[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    F.pix[slot] = pixel;
+    F.pb[slot] = ((uint32_t)P.p0 + pc) << 10;
 }
 
+// Slots whose path ended go to the free queue; k_regen stores their
+// samples and starts the next paths.
+__device__ __forceinline__ void end_paths(const Frame& F, bool ended, uint32_t slot, uint32_t* cn) {
+    push(ended, slot, F.q[3], cn + 4);
+}
+
+// Stores the sample of every ended path (new_path's input to the moving
+// average) and starts the next paths of the chunk on the freed slots,
+// appending them to the next extension queue.
+__global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P, int it) {
+    uint32_t* cn = F.ctr + 8 * ((it + 1) % 3);
+    const uint32_t count = cn[4];
+    uint32_t* qout = F.q[(it + 1) & 1];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < count; i0 += stride) {
+        uint32_t qi = i0 + lane_id();
+        bool ended = qi < count;
+        uint32_t slot = 0;
+        if (ended) {
+            slot = F.q[3][qi];
+            uint32_t pixel = F.pix[slot];
+            uint32_t p = F.pb[slot] >> 10;
+            F.samples[(size_t)(p - (uint32_t)P.p0) * (size_t)F.n + pixel] = F.accum[slot];
+        }
+        uint32_t m = __ballot_sync(0xffffffffu, ended);
+        uint32_t leader = (uint32_t)__ffs(m) - 1u;
+        uint32_t base = 0;
+        if (lane_id() == leader) base = atomicAdd(F.path_ctr, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, (int)leader);
+        bool started = false;
+        if (ended) {
+            uint32_t l = base + (uint32_t)__popc(m & ((1u << lane_id()) - 1u));
+            if (l < (uint32_t)P.chunk_paths) {
+                start_path(F, P, slot, l);
+                started = true;
+            }
+        }
+        add_stats(&F.stats[0], started ? 1u : 0u);
+        push(started, slot, qout, cn);
+    }
+}
+
+// First paths of a chunk: slot s takes path s.
+__global__ void __launch_bounds__(kBlock) k_start(Frame F, RenderParams P, int nstart) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) *F.path_ctr = (uint32_t)nstart;
+    bool go = s < (uint32_t)nstart;
+    if (go) start_path(F, P, s, s);
+    add_stats(&F.stats[0], go ? 1u : 0u);
+    push(go, s, F.q[0], F.ctr + 0);  // queue of iteration 0
+}
+
+// Persistent-warp ray loop shared by the traversal kernels: lanes whose ray
+// has finished run `finish` together, idle lanes are refilled from the queue
+// as soon as `refill` lanes are idle (all lanes once the queue is
+// exhausted), and traversal resumes where each lane stopped.  The first
+// wave is assigned by warp index (warp w takes entries [32w, 32w+32)); later
+// fetches take one atomic per warp on `head`.
+template <bool ANY, bool INSTR, typename Fetch, typename Finish>
+__device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint32_t* head, int refill,
+                                         uint32_t* status, Fetch fetch, Finish finish, uint32_t* nvis,
+                                         uint32_t* ntri) {
+    const uint32_t lane = lane_id();
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t dyn0 = nwarps * 32u;
+    const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    bool act = false, fin = false, exhausted = false, first = true;
+    uint32_t qi = 0;
+    int iters = 0;
+    RayInv r;
+    float tmax = 0.0f;
+    Trav s;
+    uint2 stack[kStack];
+    while (true) {
+        finish(fin, qi, s);
+        fin = false;
+        uint32_t idle = __ballot_sync(0xffffffffu, !act);
+        if (!exhausted && idle) {
+            uint32_t n = (uint32_t)__popc(idle);
+            uint32_t base;
+            if (first) {
+                base = gwarp * 32u;
+                first = false;
+                if (dyn0 >= count) exhausted = true;
+            } else {
+                uint32_t leader = (uint32_t)__ffs(idle) - 1u;
+                base = 0;
+                if (lane == leader) base = atomicAdd(head, n);
+                base = dyn0 + __shfl_sync(0xffffffffu, base, (int)leader);
+                if (base + n >= count) exhausted = true;
+            }
+            if (!act) {
+                uint32_t q = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (q < count) {
+                    qi = q;
+                    v3 o, d;
+                    if (fetch(q, &o, &d, &tmax)) {
+                        r = make_ray(o, d);
+                        trav_init(s, r);
+                        iters = 0;
+                        act = true;
+                    } else {
+                        trav_init(s, make_ray(o, d));
+                        fin = true;  // nothing to trace (e.g. no light): finish directly
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, act || fin)) break;
+        while (true) {
+            if (act) {
+                bool done = trav_step<ANY, INSTR>(S, r, tmax, s, stack, status, nvis, ntri);
+                if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
+                if (done) { act = false; fin = true; }
+            }
+            uint32_t nidle = (uint32_t)__popc(__ballot_sync(0xffffffffu, !act));
+            if (nidle == 32u || (!exhausted && nidle >= (uint32_t)refill)) break;
+        }
+    }
+}
+
+// Counter set of iteration `it`: [0] queue count, [1] extension head,
+// [2] shadow count, [3] shadow head, [4] ended paths (free queue count).
+__device__ __forceinline__ uint32_t* ctr_set(const Frame& F, int it) { return F.ctr + 8 * (it % 3); }
+
+// Closest hit of the extension queue.  Misses add handle_no_hit's
+// contribution and end their path; hits draw the bounce's uniforms and emit
+// the area-light shadow ray (arealight-sampler-cpu.cpp:25-143).
 template <bool INSTR>
-__global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderParams P, int path, int bounce) {
-    uint32_t* ctr = F.ctr + 4 * bounce;
-    const uint32_t count = bounce == 0 ? (uint32_t)F.n : ctr[0];
-    const uint32_t* qin = F.q[bounce & 1];
+__global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderParams P, int it) {
+    uint32_t* cs = ctr_set(F, it);
+    uint32_t* cn = ctr_set(F, it + 1);
+    const uint32_t count = cs[0];
+    const uint32_t* qin = F.q[it & 1];
     uint32_t* qsh = F.q[2];
-    uint32_t* csh = ctr + 2;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && bounce > 0) atomicAdd(&F.stats[1], (unsigned long long)count);
     uint32_t nvis = 0, ntri = 0;
     curandStateMRG32k3a* rs = (curandStateMRG32k3a*)F.rng;
-    while (true) {
-        uint32_t base = 0;
-        if (lane_id() == 0) base = atomicAdd(ctr + 1, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        uint32_t qi = base + lane_id();
-        bool valid = qi < count;
-        uint32_t id = 0;
-        bool hit = false;
-        if (valid) {
-            id = bounce == 0 ? qi : qin[qi];
-            float4 ro = F.ray_o[id], rd = F.ray_d[id];
-            RayInv r = make_ray(ld3(ro), ld3(rd));
-            TraceOut h;
-            hit = traverse<false, INSTR>(S, r, ro.w, &h, F.status, &nvis, &ntri);
+    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax) {
+        uint32_t slot = qin[q];
+        float4 ro = F.ray_o[slot], rd = F.ray_d[slot];
+        *o = ld3(ro); *d = ld3(rd); *tmax = ro.w;
+        return true;
+    };
+    auto finish = [&](bool fin, uint32_t q, const Trav& h) {
+        bool hit = false, ended = false;
+        uint32_t slot = 0;
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (fin) {
+            slot = qin[q];
+            hit = h.best_id != 0xffffffffu;
+            uint32_t pbv = F.pb[slot];
+            if ((pbv & 1023u) > 0u) add_stats_lane(&F.stats[1]);
             if (!hit) {
-                float4 tp4 = F.tp[id], ac = F.accum[id];
+                float4 tp4 = F.tp[slot];
+                acc = F.accum[slot];
                 v3 add = miss_contribution(ld3(tp4), P.sp);
-                F.accum[id] = make_float4(ac.x + add.x, ac.y + add.y, ac.z + add.z, 0.0f);
+                acc = make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f);
+                ended = true;
             } else {
-                const float4* sh = S.shade + 6 * (size_t)h.id;
+                const float4* sh = S.shade + 6 * (size_t)h.best_id;
                 float4 a = __ldg(sh + 0), b = __ldg(sh + 1), c = __ldg(sh + 2);
                 float4 na = __ldg(sh + 3), nb = __ldg(sh + 4), nc = __ldg(sh + 5);
-                v3 Pp = bary(h.beta, h.gamma, ld3(a), ld3(b), ld3(c));
-                v3 Nr = bary(h.beta, h.gamma, ld3(na), ld3(nb), ld3(nc));
-                curandStateMRG32k3a s = rs[id];
-                v3 rnd = draw3(&s);
-                rs[id] = s;
-                F.draws[id] += 1;
+                v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
+                v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
+                curandStateMRG32k3a st = rs[slot];
+                v3 rnd = draw3(&st);
+                rs[slot] = st;
                 v3 lr = rnd;
                 if (P.rng_mode == 1) {
-                    float hy = halton((int)id + 1, 3);
-                    lr = mk(halton((int)id + 1, 2), hy, hy);
+                    int pid = (int)F.pix[slot] + 1;
+                    float hy = halton(pid, 3);
+                    lr = mk(halton(pid, 2), hy, hy);
                 }
                 v3 so = mk(0.0f, 0.0f, 0.0f), sd = mk(0.0f, 0.0f, 0.0f), psc = mk(0.0f, 0.0f, 0.0f);
                 float smax = -1.0f;
@@ -315,47 +477,68 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderPa
                     rect_light_sample(L, S.overall_power, Pp, Nr, lr.x, lr.y, P.sp.shadow_offset, &so, &sd, &smax,
                                       &psc);
                 }
-                F.sh_o[id] = make_float4(so.x, so.y, so.z, smax);
-                F.sh_d[id] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-                F.psc[id] = make_float4(psc.x, psc.y, psc.z, 0.0f);
-                F.rnd[id] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
-                F.hit_p[id] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
-                F.hit_n[id] = make_float4(Nr.x, Nr.y, Nr.z, 0.0f);
+                F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
+                F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+                F.psc[slot] = make_float4(psc.x, psc.y, psc.z, 0.0f);
+                F.rnd[slot] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
+                F.hit_p[slot] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
+                F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, 0.0f);
             }
         }
-        push(valid && hit, id, qsh, csh);
-    }
+        if (ended) F.accum[slot] = acc;
+        push(fin && hit, slot, qsh, cs + 2);
+        end_paths(F, ended, slot, cn);
+    };
+    ray_loop<false, INSTR>(S, count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[3], nvis); add_stats(&F.stats[4], ntri); }
 }
 
+// Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
 template <bool INSTR>
-__global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderParams P, int path, int bounce) {
-    uint32_t* ctr = F.ctr + 4 * bounce;
-    const uint32_t count = ctr[2];
+__global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, Frame F, RenderParams P, int it) {
+    uint32_t* cs = ctr_set(F, it);
+    const uint32_t count = cs[2];
     const uint32_t* qsh = F.q[2];
-    uint32_t* qout = F.q[(bounce + 1) & 1];
-    uint32_t* cout_ = F.ctr + 4 * (bounce + 1);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&F.stats[2], (unsigned long long)count);
     uint32_t nvis = 0, ntri = 0;
-    const bool last = bounce + 1 >= P.L;
-    while (true) {
-        uint32_t base = 0;
-        if (lane_id() == 0) base = atomicAdd(ctr + 3, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        uint32_t qi = base + lane_id();
+    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax) {
+        uint32_t slot = qsh[q];
+        float4 so = F.sh_o[slot], sd = F.sh_d[slot];
+        *o = ld3(so); *d = ld3(sd); *tmax = so.w;
+        return so.w >= 0.0f;
+    };
+    auto finish = [&](bool fin, uint32_t q, const Trav& h) {
+        if (fin) {
+            uint32_t slot = qsh[q];
+            float smax = F.sh_o[slot].w;
+            bool occl = smax < 0.0f || h.best_id != 0xffffffffu;
+            reinterpret_cast<float*>(F.sh_d + slot)[3] = occl ? 1.0f : 0.0f;
+        }
+    };
+    ray_loop<true, INSTR>(S, count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
+}
+
+// BRDF sample/eval, NEE accumulation and next ray for every shadow-queue
+// entry (compute_path_contribution_and_bounce for the hits); paths that end
+// store their sample and their slots start new paths.
+__global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderParams P, int it) {
+    uint32_t* cs = ctr_set(F, it);
+    uint32_t* cn = ctr_set(F, it + 1);
+    const uint32_t count = cs[2];
+    const uint32_t* qsh = F.q[2];
+    uint32_t* qout = F.q[(it + 1) & 1];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < count; i0 += stride) {
+        uint32_t qi = i0 + lane_id();
         bool valid = qi < count;
-        uint32_t id = 0;
-        bool alive = false;
+        uint32_t slot = 0;
+        bool cont = false, ended = false;
+        float4 acc;
         if (valid) {
-            id = qsh[qi];
-            float4 so = F.sh_o[id], sd = F.sh_d[id];
-            bool occl = true;
-            if (so.w >= 0.0f) {
-                RayInv r = make_ray(ld3(so), ld3(sd));
-                occl = traverse<true, INSTR>(S, r, so.w, nullptr, F.status, &nvis, &ntri);
-            }
-            float4 hp = F.hit_p[id], hn = F.hit_n[id];
+            slot = qsh[qi];
+            float4 sd = F.sh_d[slot];
+            float4 hp = F.hit_p[slot], hn = F.hit_n[slot];
             uint32_t mi = __float_as_uint(hp.w);
             float mf[kMaterialFloats];
             const float4* mp = (const float4*)(S.mats + (size_t)kMaterialFloats * mi);
@@ -365,26 +548,41 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderPar
                 mf[4 * k] = q.x; mf[4 * k + 1] = q.y; mf[4 * k + 2] = q.z; mf[4 * k + 3] = q.w;
             }
             MaterialRec m = unpack_material(mf);
-            float4 rd = F.ray_d[id], tp4 = F.tp[id], rn = F.rnd[id], ps = F.psc[id], ac = F.accum[id];
-            ShadeOut o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), !occl, ld3(sd), ld3(ps), P.sp,
-                                   id, (uint32_t)path, bounce);
-            F.accum[id] = make_float4(ac.x + o.accum_add.x, ac.y + o.accum_add.y, ac.z + o.accum_add.z, 0.0f);
-            F.tp[id] = make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f);
-            F.ray_o[id] = make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX);
-            F.ray_d[id] = make_float4(o.dir.x, o.dir.y, o.dir.z, 0.0f);
-            alive = o.alive && !last;
+            uint32_t pbv = F.pb[slot];
+            int bounce = (int)(pbv & 1023u);
+            uint32_t path = pbv >> 10;
+            float4 rd = F.ray_d[slot], tp4 = F.tp[slot], rn = F.rnd[slot], ps = F.psc[slot];
+            acc = F.accum[slot];
+            ShadeOut o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps),
+                                   P.sp, F.pix[slot], path, bounce);
+            acc = make_float4(acc.x + o.accum_add.x, acc.y + o.accum_add.y, acc.z + o.accum_add.z, 0.0f);
+            cont = o.alive && bounce + 1 < P.L;
+            ended = !cont;
+            F.accum[slot] = acc;
+            if (cont) {
+                F.tp[slot] = make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f);
+                F.ray_o[slot] = make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX);
+                F.ray_d[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, 0.0f);
+                F.pb[slot] = pbv + 1u;
+            }
         }
-        push(alive, id, qout, cout_);
+        push(cont, slot, qout, cn);
+        end_paths(F, ended, slot, cn);
     }
-    if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
 }
 
-__global__ void k_finalize(Frame F, int path) {
+// new_path's moving average (util-kernels.cu:17-25) over the chunk's paths
+// p0 .. p1-1 of every pixel, in path order.
+__global__ void k_combine(Frame F, int p0, int p1) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
-    float4 o = F.out[i], a = F.accum[i];
-    v3 c = combine_sample(mk(o.x, o.y, o.z), mk(a.x, a.y, a.z), path);
-    F.out[i] = make_float4(c.x, c.y, c.z, 0.0f);
+    v3 o = mk(0.0f, 0.0f, 0.0f);
+    if (p0 > 0) { float4 c = F.out[i]; o = mk(c.x, c.y, c.z); }
+    for (int p = p0; p < p1; ++p) {
+        float4 s = F.samples[(size_t)(p - p0) * (size_t)F.n + (size_t)i];
+        o = combine_sample(o, mk(s.x, s.y, s.z), p);
+    }
+    F.out[i] = make_float4(o.x, o.y, o.z, 0.0f);
 }
 
 __global__ void k_pack_rgb(const float4* __restrict__ src, int n, float* dst) {
@@ -496,8 +694,6 @@ int persistent_blocks(K kernel) {
 
 }  // namespace
 
-int launch_grid_size() { return persistent_blocks(k_extend<false>); }
-
 cudaError_t k_launch_trace(const DevScene& S, int n, const float* orig, const float* dir, const float* tmax,
                            float4* hits, uint8_t* occluded, bool any, uint32_t* status, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
@@ -505,39 +701,53 @@ cudaError_t k_launch_trace(const DevScene& S, int n, const float* orig, const fl
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_rng_init(const Frame& F, uint32_t seed, cudaStream_t st) {
-    k_rng_init<<<blocks_for(F.n), kBlock, 0, st>>>(F.n, seed, (curandStateMRG32k3a*)F.rng,
-                                                   (curandStateMRG32k3a*)F.rngj, F.draws);
+cudaError_t k_launch_rng_init(int n, uint32_t seed, void* out, cudaStream_t st) {
+    k_rng_init<<<blocks_for(n), kBlock, 0, st>>>(n, seed, (curandStateMRG32k3a*)out);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_raygen(const Frame& F, const RenderParams& P, int path, cudaStream_t st) {
-    bool lens = P.cam.aperture != 0.0f;
-    if (lens) k_jitter_pool<<<blocks_for(F.n), kBlock, 0, st>>>(F);
-    k_raygen<<<blocks_for(F.n), kBlock, 0, st>>>(F, P, path, lens ? 1 : 0);
+cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cudaStream_t st) {
+    k_start<<<blocks_for(std::max(nstart, 1)), kBlock, 0, st>>>(F, P, nstart);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int path, int bounce,
-                            bool instrument, cudaStream_t st) {
+cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
+                            cudaStream_t st) {
     static int g0 = persistent_blocks(k_extend<false>);
     static int g1 = persistent_blocks(k_extend<true>);
-    if (instrument) k_extend<true><<<g1, kBlock, 0, st>>>(S, F, P, path, bounce);
-    else k_extend<false><<<g0, kBlock, 0, st>>>(S, F, P, path, bounce);
+    if (instrument) k_extend<true><<<g1, kBlock, 0, st>>>(S, F, P, it);
+    else k_extend<false><<<g0, kBlock, 0, st>>>(S, F, P, it);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_shade(const DevScene& S, const Frame& F, const RenderParams& P, int path, int bounce,
-                           bool instrument, cudaStream_t st) {
-    static int g0 = persistent_blocks(k_shade<false>);
-    static int g1 = persistent_blocks(k_shade<true>);
-    if (instrument) k_shade<true><<<g1, kBlock, 0, st>>>(S, F, P, path, bounce);
-    else k_shade<false><<<g0, kBlock, 0, st>>>(S, F, P, path, bounce);
+cudaError_t k_launch_shadow(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
+                            cudaStream_t st) {
+    static int g0 = persistent_blocks(k_shadow<false>);
+    static int g1 = persistent_blocks(k_shadow<true>);
+    if (instrument) k_shadow<true><<<g1, kBlock, 0, st>>>(S, F, P, it);
+    else k_shadow<false><<<g0, kBlock, 0, st>>>(S, F, P, it);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_finalize(const Frame& F, int path, cudaStream_t st) {
-    k_finalize<<<blocks_for(F.n), kBlock, 0, st>>>(F, path);
+cudaError_t k_launch_shade(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
+    static int g0 = persistent_blocks(k_shade);
+    k_shade<<<g0, kBlock, 0, st>>>(S, F, P, it);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
+    static int g0 = persistent_blocks(k_regen);
+    k_regen<<<g0, kBlock, 0, st>>>(F, P, it);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_jitter_pool(const Frame& F, int p0, int p1, cudaStream_t st) {
+    k_jitter_pool<<<blocks_for(F.n), kBlock, 0, st>>>(F, p0, p1);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_combine(const Frame& F, int p0, int p1, cudaStream_t st) {
+    k_combine<<<blocks_for(F.n), kBlock, 0, st>>>(F, p0, p1);
     return cudaGetLastError();
 }
 

@@ -24,26 +24,35 @@ struct DevScene {
 // Status bits written by the kernels (never a trap).
 enum { ST_STACK_OVERFLOW = 1u, ST_ITER_LIMIT = 2u };
 
-// Per-pixel wavefront state (SoA, one entry per pixel of the frame).
+// Wavefront state: per path slot (SoA) and per pixel.
 struct Frame {
-    int w, h, n;
+    int w, h, n;       // image and pixel count
+    int nslots;        // path slots in flight
+    // per slot
     float4* ray_o;     // origin xyz, t_max
     float4* ray_d;     // direction xyz
     float4* tp;        // throughput
-    float4* accum;     // col_accum of the current path
-    float4* out;       // output_color (moving average)
+    float4* accum;     // col_accum of the slot's path
     float4* sh_o;      // shadow origin xyz, max_t
-    float4* sh_d;      // shadow direction xyz (to_light)
+    float4* sh_d;      // shadow direction xyz (to_light), w = occluded
     float4* psc;       // potential_sample_contribution
     float4* rnd;       // path draw of this bounce
     float4* hit_p;     // hit point xyz | material index bits
     float4* hit_n;     // interpolated (unnormalised) normal
-    void* rng;         // curandStateMRG32k3a[n], light/path stream
-    void* rngj;        // curandStateMRG32k3a[n], camera-jitter stream
-    int* draws;        // updates consumed by `rng`
-    float4* jpool;     // jitter pool (thin lens only)
-    uint32_t* q[3];    // ray queues: extension (ping/pong) and shadow
-    uint32_t* ctr;     // per bounce: [4*b+0] ext count, +1 ext head, +2 shadow count, +3 shadow head
+    void* rng;         // curandStateMRG32k3a: light/path stream of the slot's path
+    uint32_t* pix;     // pixel of the slot's path
+    uint32_t* pb;      // path index << 10 | bounce
+    uint32_t* q[4];    // queues: extension (ping/pong), shadow, ended paths; nslots entries each
+    // per pixel
+    float4* out;       // output_color (moving average)
+    void* pristine;    // curandStateMRG32k3a after curand_init(seed, pixel, 0)
+    void* cursor;      // curandStateMRG32k3a: light/path stream at the pixel's next path
+    void* jcursor;     // curandStateMRG32k3a: camera-jitter stream at the pixel's next path
+    float4* samples;   // [chunk][n] sample of every path of the chunk
+    float4* jpool;     // [chunk][n] camera jitter of every path of the chunk
+    // control
+    uint32_t* ctr;     // 3 sets of 8 (by iteration % 3): count, ext head, shadow count, shadow head, ended
+    uint32_t* path_ctr;  // next path of the chunk to start
     unsigned long long* stats;  // 0 camera, 1 ext, 2 shadow rays; 3/4 closest, 5/6 shadow node visits / tri tests
     uint32_t* status;
 };
@@ -53,19 +62,23 @@ struct RenderParams {
     ShadeParams sp;
     int spp, L, rng_mode;
     uint32_t seed;
+    int refill;        // refill a warp's lanes once this many are idle (1..32)
+    int p0;            // first path sample of the chunk
+    int chunk_paths;   // paths in the chunk ((p1 - p0) * n)
 };
-
-int launch_grid_size();  // persistent grid (blocks) for the queue kernels
 
 cudaError_t k_launch_trace(const DevScene& S, int n, const float* orig, const float* dir, const float* tmax,
                            float4* hits, uint8_t* occluded, bool any, uint32_t* status, cudaStream_t st);
-cudaError_t k_launch_rng_init(const Frame& F, uint32_t seed, cudaStream_t st);
-cudaError_t k_launch_raygen(const Frame& F, const RenderParams& P, int path, cudaStream_t st);
-cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int path, int bounce,
-                            bool instrument, cudaStream_t st);
-cudaError_t k_launch_shade(const DevScene& S, const Frame& F, const RenderParams& P, int path, int bounce,
-                           bool instrument, cudaStream_t st);
-cudaError_t k_launch_finalize(const Frame& F, int path, cudaStream_t st);
+cudaError_t k_launch_rng_init(int n, uint32_t seed, void* out, cudaStream_t st);
+cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cudaStream_t st);
+cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
+                            cudaStream_t st);
+cudaError_t k_launch_shadow(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
+                            cudaStream_t st);
+cudaError_t k_launch_shade(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st);
+cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, int it, cudaStream_t st);
+cudaError_t k_launch_jitter_pool(const Frame& F, int p0, int p1, cudaStream_t st);
+cudaError_t k_launch_combine(const Frame& F, int p0, int p1, cudaStream_t st);
 cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t st);
 cudaError_t k_launch_mrg_pool(int npix, uint32_t seed, int first_update, int num_updates, float* out,
                               cudaStream_t st);

@@ -44,14 +44,18 @@ constexpr int kMaxDevices = 64;
 constexpr size_t kAlign = 256;
 
 constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
-constexpr size_t kV4 = align_up(sizeof(float4) * (size_t)kNoAllocMaxPixels);  // one float4 per pixel
-constexpr size_t kRng = align_up(48 * (size_t)kNoAllocMaxPixels);             // curandStateMRG32k3a per pixel
-constexpr size_t kU32 = align_up(4 * (size_t)kNoAllocMaxPixels);              // one 32-bit word per pixel
-constexpr size_t kCtr = align_up(4 * 4 * (size_t)(kNoAllocMaxBounces + 1));
+constexpr size_t kV4 = align_up(sizeof(float4) * (size_t)kNoAllocMaxPixels);  // one float4 per slot / pixel
+constexpr size_t kRng = align_up(48 * (size_t)kNoAllocMaxPixels);             // curandStateMRG32k3a per slot / pixel
+constexpr size_t kU32 = align_up(4 * (size_t)kNoAllocMaxPixels);              // one 32-bit word per slot
+constexpr size_t kCtr = align_up(4 * 32);
 constexpr size_t kStats = align_up(8 * 8);
 constexpr size_t kStatus = align_up(4);
-// 12 float4 planes, 2 RNG planes, draws + 3 queues, counters, stats, status
-constexpr size_t kScratchBytes = 12 * kV4 + 2 * kRng + 4 * kU32 + kCtr + kStats + kStatus;
+// One slot per pixel and one path sample per pass: 10 float4 slot planes,
+// slot RNG, pixel / path words, 4 queues; per pixel the image, the initial
+// RNG states, the two stream cursors, one sample and one jitter value;
+// counters, stats, status.
+constexpr size_t kScratchBytes = 10 * kV4 + kRng + 2 * kU32 + 4 * kU32 + kV4 + 3 * kRng + 2 * kV4 + kCtr + kCtr +
+                                 kStats + kStatus;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -74,15 +78,22 @@ cudaError_t scratch_on_device(int dev, unsigned char** out) {
 Frame carve(unsigned char* base, int w, int h) {
     Frame F{};
     F.w = w; F.h = h; F.n = w * h;
+    F.nslots = F.n;
     size_t off = 0;
-    float4** planes[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.out, &F.sh_o, &F.sh_d,
-                         &F.psc, &F.rnd, &F.hit_p, &F.hit_n, &F.jpool};
+    float4** planes[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
     for (float4** p : planes) { *p = (float4*)(base + off); off += kV4; }
     F.rng = base + off; off += kRng;
-    F.rngj = base + off; off += kRng;
-    F.draws = (int*)(base + off); off += kU32;
-    for (int k = 0; k < 3; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
+    F.pix = (uint32_t*)(base + off); off += kU32;
+    F.pb = (uint32_t*)(base + off); off += kU32;
+    for (int k = 0; k < 4; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
+    F.out = (float4*)(base + off); off += kV4;
+    F.pristine = base + off; off += kRng;
+    F.cursor = base + off; off += kRng;
+    F.jcursor = base + off; off += kRng;
+    F.samples = (float4*)(base + off); off += kV4;
+    F.jpool = (float4*)(base + off); off += kV4;
     F.ctr = (uint32_t*)(base + off); off += kCtr;
+    F.path_ctr = (uint32_t*)(base + off); off += kCtr;
     F.stats = (unsigned long long*)(base + off); off += kStats;
     F.status = (uint32_t*)(base + off); off += kStatus;
     return F;
@@ -126,17 +137,33 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
     P.L = d->max_bounces;
     P.rng_mode = d->rng_mode;
     P.seed = d->seed;
+    P.refill = 16;
     cudaError_t e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(F.status, 0, 4, st);
-    if (e == cudaSuccess) e = k_launch_rng_init(F, d->seed, st);
+    if (e == cudaSuccess) e = k_launch_rng_init(F.n, d->seed, F.pristine, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)F.n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)F.n, cudaMemcpyDeviceToDevice, st);
+    // one path sample of every pixel per pass; the host checks the queue
+    // count every 8 iterations (a path has at most max_bounces segments)
     for (int p = 0; p < P.spp && e == cudaSuccess; ++p) {
-        e = cudaMemsetAsync(F.ctr, 0, 4 * 4 * (size_t)(P.L + 1), st);
-        if (e == cudaSuccess) e = k_launch_raygen(F, P, p, st);
-        for (int b = 0; b < P.L && e == cudaSuccess; ++b) {
-            e = k_launch_extend(S, F, P, p, b, false, st);
-            if (e == cudaSuccess) e = k_launch_shade(S, F, P, p, b, false, st);
+        P.p0 = p;
+        P.chunk_paths = F.n;
+        e = cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, st);
+        if (e == cudaSuccess) e = k_launch_jitter_pool(F, p, p + 1, st);
+        if (e == cudaSuccess) e = k_launch_start(F, P, F.n, st);
+        uint32_t left = 1;
+        for (int it = 0; e == cudaSuccess && left != 0u && it <= P.L + 1; ++it) {
+            e = cudaMemsetAsync(F.ctr + 8 * ((it + 1) % 3), 0, sizeof(uint32_t) * 8, st);
+            if (e == cudaSuccess) e = k_launch_extend(S, F, P, it, false, st);
+            if (e == cudaSuccess) e = k_launch_shadow(S, F, P, it, false, st);
+            if (e == cudaSuccess) e = k_launch_shade(S, F, P, it, st);
+            if (e == cudaSuccess) e = k_launch_regen(F, P, it, st);
+            if (e == cudaSuccess && (it % 8 == 7 || it == P.L)) {
+                e = cudaMemcpyAsync(&left, F.ctr + 8 * ((it + 1) % 3), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            }
         }
-        if (e == cudaSuccess) e = k_launch_finalize(F, p, st);
+        if (e == cudaSuccess) e = k_launch_combine(F, p, p + 1, st);
     }
     if (e == cudaSuccess) e = k_launch_pack_rgb(F.out, F.n, out_rgb, st);
     uint32_t status = 0;

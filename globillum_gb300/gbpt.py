@@ -63,6 +63,10 @@ class RenderDesc(C.Structure):
                 ("shadow_offset", C.c_float), ("background", F3), ("rr_start", C.c_int)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("refill", C.c_int), ("slots", C.c_int), ("sample_mb", C.c_int)]
+
+
 class Hit(C.Structure):
     _fields_ = [("t", C.c_float), ("beta", C.c_float), ("gamma", C.c_float), ("ref", C.c_uint32)]
 
@@ -71,8 +75,8 @@ class Stats(C.Structure):
     _fields_ = [("camera_rays", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("closest_node_visits", C.c_uint64), ("closest_tri_tests", C.c_uint64),
                 ("shadow_node_visits", C.c_uint64), ("shadow_tri_tests", C.c_uint64),
-                ("kernel_launches", C.c_uint64), ("render_ms", C.c_double), ("stage_ms", C.c_double * 4),
-                ("stage_launches", C.c_uint64 * 4), ("paths_done", C.c_int)]
+                ("kernel_launches", C.c_uint64), ("render_ms", C.c_double), ("stage_ms", C.c_double * 6),
+                ("stage_launches", C.c_uint64 * 6), ("paths_done", C.c_int)]
 
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("beta", "<f4"), ("gamma", "<f4"), ("ref", "<u4")])
@@ -83,7 +87,7 @@ EXPORTS = [
     "gb_scene_get_info", "gb_render", "gb_render_begin", "gb_render_step", "gb_render_paths_done", "gb_render_read",
     "gb_trace_closest", "gb_trace_any", "gb_generate_arealight_sample", "gb_compute_path_contribution_and_bounce",
     "gb_mrg_pool", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
-    "gb_render_noalloc",
+    "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning",
 ]
 
 _lib = None
@@ -124,6 +128,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.gb_layout_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.gb_ctx_set_stage_timing.argtypes = [vp, ip]
+    lib.gb_ctx_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    lib.gb_ctx_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     lib.gb_render_noalloc.argtypes = [vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp]
     if path is None:
         _lib = lib
@@ -219,6 +225,14 @@ class Context:
         d["stage_ms"] = list(s.stage_ms)
         d["stage_launches"] = list(s.stage_launches)
         return d
+
+    def set_tuning(self, refill: int = 0, slots: int = 0, sample_mb: int = 0):
+        self.check(self.lib.gb_ctx_set_tuning(self.h, C.byref(Tuning(refill, slots, sample_mb))))
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self.check(self.lib.gb_ctx_get_tuning(self.h, C.byref(t)))
+        return {"refill": t.refill, "slots": t.slots, "sample_mb": t.sample_mb}
 
     def set_stage_timing(self, on: bool):
         self.check(self.lib.gb_ctx_set_stage_timing(self.h, 1 if on else 0))

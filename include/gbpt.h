@@ -219,11 +219,25 @@ typedef struct {
     uint64_t kernel_launches;                           /* launches of the last render */
     double render_ms;                                   /* device time, begin -> last step */
     /* per-stage device time when stage timing is on (gb_ctx_set_stage_timing):
-     * 0 raygen, 1 closest-hit + light sample, 2 any-hit + shade, 3 accumulate  */
-    double stage_ms[4];
-    uint64_t stage_launches[4];
+     * 0 path start, 1 closest-hit + light sample, 2 any-hit, 3 shade,
+     * 4 path end + restart, 5 moving average                                   */
+    double stage_ms[6];
+    uint64_t stage_launches[6];
     int paths_done;
 } gb_stats;
+
+/* Knobs of the wavefront (chosen by the autotuner); 0 keeps a value:
+ *   refill    idle lanes (1..32) at which a traversal warp fetches new rays
+ *   slots     paths in flight (queue capacity), default 2^20
+ *   sample_mb budget of the per-path sample buffer, which bounds how many
+ *             path samples per pixel one pass of the slot pool covers */
+typedef struct {
+    int refill;
+    int slots;
+    int sample_mb;
+} gb_tuning;
+int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* tuning);
+int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* tuning);
 
 /* Records CUDA events around every stage launch of later renders on the
  * context's stream (for per-kernel timing); off by default. */
@@ -241,7 +255,7 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
  * The scene is created beforehand (gb_scene_create allocates); this call
  * renders the same frame as gb_render into the caller's device buffer
  * `out_rgb` (w*h*3 floats) on `stream` (NULL = legacy default stream), with
- * its wavefront state in one fixed file-scope device array (about 19 MB,
+ * its wavefront state in one fixed file-scope device array (about 24 MB,
  * held by every GPU that loads the library until exit) instead of cudaMalloc.
  * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID.
  * The first call on a device looks the array up (cudaGetSymbolAddress) with
