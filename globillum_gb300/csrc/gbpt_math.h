@@ -487,6 +487,36 @@ struct ShadeOut {
     bool alive;
 };
 
+// sample_material of hybrid-pt.cpp:330-349 with the normal and tangent
+// frame of :430 and :525-528: the sampled world direction, its pdf and lobe,
+// and the (possibly flipped) shading normal.
+struct BsdfSample {
+    v3 org_dir, inv_org_dir, N, wi;
+    float pdf;
+    int lobe;
+    bool glass;
+};
+
+GB_HD BsdfSample sample_bsdf(const MaterialRec& m, v3 Nraw, v3 ray_dir, v3 rnd) {
+    BsdfSample s;
+    s.org_dir = normalize_div(ray_dir);
+    v3 N = normalize_div(Nraw);
+    v3 T, B;
+    make_tangent_frame(N, &T, &B);
+    T = normalize_div(T);
+    B = normalize_div(B);
+    s.inv_org_dir = -1.0f * s.org_dir;
+    s.glass = is_glass(m);
+    if (dot(s.org_dir, N) > 0.0f) N = N * -1.0f;
+    v3 wo_ts = to_tangent(s.inv_org_dir, T, B, N);
+    v3 wi;
+    material_sample(m, wo_ts, rnd, &wi, &s.pdf, &s.lobe);
+    wi = from_tangent(wi, T, B, N);
+    s.wi = normalize_div(wi);
+    s.N = N;
+    return s;
+}
+
 // One pixel of compute_path_contribution_and_bounce (hybrid-pt.cpp:465-564)
 // for a valid hit.  P, Nraw: interpolated hit point / normal; ray_dir: the
 // ray direction; rnd: the path-stream draw; unoccluded: shadow result;
@@ -495,21 +525,11 @@ GB_HD ShadeOut shade_hit(const MaterialRec& m, v3 P, v3 Nraw, v3 ray_dir, v3 tp,
                          bool unoccluded, v3 to_light, v3 psc, const ShadeParams& sp,
                          uint32_t pixel, uint32_t path, int bounce) {
     ShadeOut o;
-    v3 org_dir = normalize_div(ray_dir);
-    v3 N = normalize_div(Nraw);
-    v3 T, B;
-    make_tangent_frame(N, &T, &B);
-    T = normalize_div(T);
-    B = normalize_div(B);
-    // sample_material (hybrid-pt.cpp:330-349)
-    v3 inv_org_dir = -1.0f * org_dir;
-    bool glass = is_glass(m);
-    if (dot(org_dir, N) > 0.0f) N = N * -1.0f;
-    v3 wo_ts = to_tangent(inv_org_dir, T, B, N);
-    v3 wi; float pdf; int lobe;
-    material_sample(m, wo_ts, rnd, &wi, &pdf, &lobe);
-    wi = from_tangent(wi, T, B, N);
-    wi = normalize_div(wi);
+    BsdfSample bs = sample_bsdf(m, Nraw, ray_dir, rnd);
+    const v3 org_dir = bs.org_dir, inv_org_dir = bs.inv_org_dir, N = bs.N, wi = bs.wi;
+    const float pdf = bs.pdf;
+    const int lobe = bs.lobe;
+    const bool glass = bs.glass;
     // evaluate_material (hybrid-pt.cpp:351-371)
     o.accum_add = mk(0.0f, 0.0f, 0.0f);
     if (!glass && unoccluded) {

@@ -522,6 +522,28 @@ int orc_material_sample_eval(const gb_material* mat, const gb_principled_params*
     return 0;
 }
 
+// sample_bsdf + the two evaluations of evaluate_material, for the pinning
+// tests against the reference's own materialBRDF (same outputs as
+// ref_shade_eval in oracle/ref_glue.cpp): out[0..2] wi, [3] pdf, [4..6]
+// brdf(wi), [7..9] brdf(to_light), [10] glass.
+int orc_shade_eval(const gb_material* mat, const gb_principled_params* params, const float* n_raw,
+                   const float* ray_dir, const float* rnd, const float* to_light, float* out) {
+    float f[kMaterialFloats];
+    pack_material(make_material(*mat, params), f);
+    MaterialRec m = unpack_material(f);
+    BsdfSample s = sample_bsdf(m, mk(n_raw[0], n_raw[1], n_raw[2]), mk(ray_dir[0], ray_dir[1], ray_dir[2]),
+                               mk(rnd[0], rnd[1], rnd[2]));
+    v3 ld = normalize_div(mk(to_light[0], to_light[1], to_light[2]));
+    v3 fw = material_eval(m, s.lobe, s.inv_org_dir, s.wi, s.N);
+    v3 fl = material_eval(m, s.lobe, s.inv_org_dir, ld, s.N);
+    out[0] = s.wi.x; out[1] = s.wi.y; out[2] = s.wi.z;
+    out[3] = s.pdf;
+    out[4] = fw.x; out[5] = fw.y; out[6] = fw.z;
+    out[7] = fl.x; out[8] = fl.y; out[9] = fl.z;
+    out[10] = s.glass ? 1.0f : 0.0f;
+    return 0;
+}
+
 int orc_sincos_2pi(int n, const float* u, float* s, float* c) {
     for (int i = 0; i < n; ++i) sincos_2pi(u[i], &s[i], &c[i]);
     return 0;

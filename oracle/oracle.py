@@ -40,6 +40,7 @@ def load() -> C.CDLL:
         lib.orc_halton_pool.argtypes = [ip, vp]
         lib.orc_material_sample_eval.argtypes = [vp] * 12
         lib.orc_sincos_2pi.argtypes = [ip, vp, vp, vp]
+        lib.orc_shade_eval.argtypes = [vp] * 7
         lib.orc_threads.restype = ip
         lib.orc_set_threads.argtypes = [ip]
         lib.orc_set_threads.restype = None
@@ -165,6 +166,18 @@ def material_sample_eval(material: dict, params: dict | None, wo_ts, rnd, N, wo_
     lib.orc_material_sample_eval(C.byref(m), C.cast(pp, C.c_void_p), *[_p(a) for a in args], _p(wi), _p(pdf),
                                  _p(lobe), _p(fs), _p(fe))
     return wi, float(pdf[0]), int(lobe[0]), fs, fe
+
+
+def shade_eval(diffuse, principled: bool, params18, n_raw, ray_dir, rnd, to_light) -> np.ndarray:
+    """sample_bsdf + evaluations (same outputs as the reference glue's ref_shade_eval)."""
+    lib = load()
+    m = _gbpt.Material(_gbpt._f3(diffuse), 0 if principled else -1)
+    pp = _gbpt.PrincipledParams(*[float(x) for x in params18[:12]], _gbpt._f3(params18[12:15]),
+                                _gbpt._f3(params18[15:18]))
+    f = lambda v: np.ascontiguousarray(v, np.float32)
+    out = np.zeros(11, np.float32)
+    lib.orc_shade_eval(C.byref(m), C.byref(pp), _p(f(n_raw)), _p(f(ray_dir)), _p(f(rnd)), _p(f(to_light)), _p(out))
+    return out
 
 
 def threads() -> int:
