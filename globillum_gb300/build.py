@@ -20,6 +20,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libgbpt.so"
+HEADLESS = LIBDIR / "gi_headless"
 ORACLE_SRC = ROOT / "oracle" / "gbpt_oracle.cpp"
 ORACLE_LIB = ROOT / "oracle" / "_build" / "libgbpt_oracle.so"
 
@@ -91,6 +92,20 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     return LIB
 
 
+def build_headless(force: bool = False) -> Path:
+    """Builds the headless front-end over include/gb_hybrid_pt.h."""
+    lib = build_lib()
+    src = PKG / "host" / "gi_headless.cpp"
+    deps = [src, ROOT / "include" / "gb_hybrid_pt.h", ROOT / "include" / "gbpt.h", lib]
+    if not force and not _stale(HEADLESS, deps):
+        return HEADLESS
+    tmp = HEADLESS.with_suffix(".tmp")
+    _run_parallel([["g++", "-O2", "-std=c++17", str(src), "-o", str(tmp), "-L" + str(LIBDIR), "-lgbpt",
+                    "-Wl,-rpath,$ORIGIN"]])
+    os.replace(tmp, HEADLESS)
+    return HEADLESS
+
+
 def build_oracle(force: bool = False) -> Path:
     """Compiles the CPU oracle (test infrastructure) into oracle/_build."""
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
@@ -106,6 +121,7 @@ def build_oracle(force: bool = False) -> Path:
 
 def build_all(force: bool = False) -> None:
     build_lib(force)
+    build_headless(force)
     build_oracle(force)
     ref = ROOT / "oracle" / "build_ref.py"
     if ref.exists():

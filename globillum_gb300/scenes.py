@@ -243,3 +243,39 @@ def random_rays(scene: SceneData, n: int, seed: int = 0, spread: float = 0.2):
     d = tgt - o
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return o.astype(np.float32), d.astype(np.float32)
+
+
+def write_scene_bin(scene: SceneData, path) -> None:
+    """Binary scene file read by the headless front-end (host/gi_headless.cpp):
+    magic "GBSC", int32 version 1, triangles, materials, params, lights, then
+    the gb_scene_desc arrays and the gb_camera, little endian."""
+    import ctypes as C
+    from . import gbpt
+    desc, keep = gbpt.make_scene_desc(scene)
+    pos = np.ascontiguousarray(scene.positions, np.float32)
+    nrm = np.ascontiguousarray(scene.normals, np.float32)
+    mid = np.ascontiguousarray(scene.material_index, np.int32)
+    with open(path, "wb") as f:
+        f.write(b"GBSC")
+        f.write(np.array([1, pos.shape[0], len(scene.materials), len(scene.params), len(scene.lights)],
+                         np.int32).tobytes())
+        f.write(pos.tobytes())
+        f.write(nrm.tobytes())
+        f.write(mid.tobytes())
+        f.write(C.string_at(C.addressof(desc.materials.contents), C.sizeof(gbpt.Material) * len(scene.materials)))
+        if scene.params:
+            f.write(C.string_at(C.addressof(desc.params.contents), C.sizeof(gbpt.PrincipledParams) * len(scene.params)))
+        if scene.lights:
+            f.write(C.string_at(C.addressof(desc.lights.contents), C.sizeof(gbpt.Light) * len(scene.lights)))
+        cam = gbpt.make_camera(scene.camera)
+        f.write(C.string_at(C.addressof(cam), C.sizeof(gbpt.Camera)))
+
+
+def read_pfm(path) -> np.ndarray:
+    """Float PFM (as written by gi_headless) -> (h, w, 3) array, top row first."""
+    with open(path, "rb") as f:
+        assert f.readline().strip() == b"PF"
+        w, h = map(int, f.readline().split())
+        scale = float(f.readline())
+        data = np.frombuffer(f.read(), dtype="<f4" if scale < 0 else ">f4").reshape(h, w, 3)
+    return data[::-1].copy()

@@ -1,0 +1,29 @@
+"""The C++ drop-in (gb::hybrid_pt over the C ABI, driven like the
+reference's gi front-end: select -> compute -> update while in_progress)
+renders the same image as gb_render."""
+import subprocess
+
+import numpy as np
+import pytest
+
+from globillum_gb300 import build, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_headless_matches_gb_render(gpu_ctx, tmp_path):
+    exe = build.build_headless()
+    sc = scenes.cornell(width=48, height=40, spp=3, max_bounces=4)
+    scenes.write_scene_bin(sc, tmp_path / "s.bin")
+    r = sc.render
+    out = tmp_path / "o.pfm"
+    cmd = [str(exe), str(tmp_path / "s.bin"), str(out), "-r", f"{r['width']}x{r['height']}", "-s", str(r["spp"]),
+           "-l", str(r["max_bounces"]), "--offsets", repr(r["ray_offset"]), repr(r["shadow_offset"]), "--halton"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    img = scenes.read_pfm(out)
+    scene = gpu_ctx.scene(sc)
+    ref = scene.render(sc.camera, dict(r))
+    scene.close()
+    # the file is written like save_image: x and y mirrored
+    assert np.array_equal(img, ref[::-1, ::-1])
