@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refill", type=int, default=0, help="traversal refill threshold (0 = library default)")
     ap.add_argument("--slots", type=int, default=0, help="paths in flight (0 = library default)")
+    ap.add_argument("--tri-mode", type=int, default=0, help="traversal triangle policy 1..3 (0 = library default)")
     return ap.parse_args()
 
 
@@ -192,8 +193,8 @@ def run_gbpt(args, rank, world):
     W, H, spp = r["width"], r["height"], r["spp"]
     stream = torch.cuda.current_stream()
     ctx = gbpt.Context(local, stream.cuda_stream)
-    if args.refill or args.slots:
-        ctx.set_tuning(refill=args.refill, slots=args.slots)
+    if args.refill or args.slots or args.tri_mode:
+        ctx.set_tuning(refill=args.refill, slots=args.slots, tri_mode=args.tri_mode)
     t0 = time.perf_counter()
     scene = ctx.scene(sc)
     upload_s = time.perf_counter() - t0

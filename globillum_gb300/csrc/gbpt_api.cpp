@@ -46,6 +46,7 @@ struct gb_ctx {
     uint64_t launches = 0;
     bool stage_timing = false;
     int refill = 16;                    // idle lanes that trigger a warp refill
+    int tri_mode = 0;                   // traversal triangle policy (see gb_tuning)
     int slots = 1 << 20;                // path slots in flight (upper bound; at most one per pixel)
     int sample_mb = 1024;               // sample buffer budget (chunk size)
     // queue-count snapshots: pinned ring + events (host stays a few iterations ahead)
@@ -415,6 +416,7 @@ int gb_render_begin(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb
     P.rng_mode = d->rng_mode;
     P.seed = d->seed;
     P.refill = ctx->refill;
+    P.tri_mode = ctx->tri_mode;
     ctx->scene = scene;
     ctx->paths_done = 0;
     ctx->active = true;
@@ -602,6 +604,8 @@ int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* t) {
     if (!ctx || !t) return fail(ctx, GB_ERR_INVALID, "null argument");
     if (t->refill < 0 || t->refill > 32) return fail(ctx, GB_ERR_INVALID, "refill must be in 1..32");
     if (t->slots < 0 || t->sample_mb < 0) return fail(ctx, GB_ERR_INVALID, "negative tuning value");
+    if (t->tri_mode < 0 || t->tri_mode > 3) return fail(ctx, GB_ERR_INVALID, "tri_mode must be 1..3 (0 keeps)");
+    if (t->tri_mode) ctx->tri_mode = t->tri_mode - 1;
     if (t->refill) ctx->refill = t->refill;
     if (t->slots) ctx->slots = t->slots;
     if (t->sample_mb) ctx->sample_mb = t->sample_mb;
@@ -613,6 +617,7 @@ int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* t) {
     t->refill = ctx->refill;
     t->slots = ctx->slots;
     t->sample_mb = ctx->sample_mb;
+    t->tri_mode = ctx->tri_mode + 1;
     return GB_OK;
 }
 

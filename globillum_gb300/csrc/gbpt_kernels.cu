@@ -61,11 +61,58 @@ __device__ __forceinline__ RayInv make_ray(v3 o, v3 d) {
     return r;
 }
 
+// Packed FP32 (two lanes per 64-bit register) and 3-input min/max of sm_100+.
+__device__ __forceinline__ uint64_t pack2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpack2(uint64_t v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ float max3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Bits of an 8-bit mask moved from position i to i ^ x (x in 0..7).
+__device__ __forceinline__ uint32_t xor_permute8(uint32_t m, uint32_t x) {
+    if (x & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (x & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (x & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    return m;
+}
+
 // Intersects the 8 children of node `ni`; returns the node group (child
 // base, hit bits 24-31 in visit order | imask) and the triangle group.
 // Per axis the near and far planes are chosen once per node from the sign
 // of the inverse direction (fma is monotonic in the plane index, so this
-// equals taking min/max of the two plane distances per child).
+// equals taking min/max of the two plane distances per child); children are
+// tested two at a time with packed FP32.  The test is conservative: the
+// entry distance is shrunk and the exit distance grown by 1e-5 relative on
+// top of the outward-rounded boxes.  Empty slots (meta 0, imask bit 0) may
+// test positive; they add neither a node nor a triangle.
 __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes, uint32_t ni, const RayInv& r,
                                                float bound, uint2* ng, uint2* tg) {
     const float4* n = nodes + 5 * (size_t)ni;
@@ -74,14 +121,17 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
     float sx = __uint_as_float((ew & 0xffu) << 23);
     float sy = __uint_as_float(((ew >> 8) & 0xffu) << 23);
     float sz = __uint_as_float(((ew >> 16) & 0xffu) << 23);
-    uint32_t imask = ew >> 24;
-    float aix = sx * r.idir.x, aiy = sy * r.idir.y, aiz = sz * r.idir.z;
-    float aox = (n0.x - r.o.x) * r.idir.x, aoy = (n0.y - r.o.y) * r.idir.y, aoz = (n0.z - r.o.z) * r.idir.z;
+    const uint32_t imask = ew >> 24;
+    const float aix = sx * r.idir.x, aiy = sy * r.idir.y, aiz = sz * r.idir.z;
+    const uint64_t AX = pack2(aix, aix), AY = pack2(aiy, aiy), AZ = pack2(aiz, aiz);
+    const float aox = (n0.x - r.o.x) * r.idir.x, aoy = (n0.y - r.o.y) * r.idir.y, aoz = (n0.z - r.o.z) * r.idir.z;
+    const uint64_t OX = pack2(aox, aox), OY = pack2(aoy, aoy), OZ = pack2(aoz, aoz);
+    const uint64_t BIAS = pack2(-8388608.0f, -8388608.0f);
+    const uint64_t KN = pack2(0.99999f, 0.99999f), KF = pack2(1.00001f, 1.00001f);
     const bool fx = r.idir.x < 0.0f, fy = r.idir.y < 0.0f, fz = r.idir.z < 0.0f;
-    uint32_t hits_n = 0, hits_t = 0;
+    uint32_t hm = 0;  // child hits by slot
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
-        uint32_t meta_w = __float_as_uint(half ? n1.w : n1.z);
         uint32_t qlx = __float_as_uint(half ? n2.y : n2.x), qly = __float_as_uint(half ? n2.w : n2.z);
         uint32_t qlz = __float_as_uint(half ? n3.y : n3.x), qhx = __float_as_uint(half ? n3.w : n3.z);
         uint32_t qhy = __float_as_uint(half ? n4.y : n4.x), qhz = __float_as_uint(half ? n4.w : n4.z);
@@ -89,21 +139,40 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
         uint32_t ny = fy ? qhy : qly, fyw = fy ? qly : qhy;
         uint32_t nz = fz ? qhz : qlz, fzw = fz ? qlz : qhz;
 #pragma unroll
-        for (uint32_t j = 0; j < 4; ++j) {
+        for (uint32_t j = 0; j < 4; j += 2) {
+            // plane index bytes j, j+1 as floats 2^23 + q (PRMT), minus 2^23
+            // (exact), then the plane distance q * a + o (packed FMA)
+#define GB_PLANES(w, A, O) fma2(add2(pack2(__uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | j)),          \
+                                            __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | (j + 1u)))), \
+                                      BIAS), A, O)
+            float tnx0, tnx1, tny0, tny1, tnz0, tnz1, tfx0, tfx1, tfy0, tfy1, tfz0, tfz1;
+            unpack2(GB_PLANES(nx, AX, OX), tnx0, tnx1);
+            unpack2(GB_PLANES(ny, AY, OY), tny0, tny1);
+            unpack2(GB_PLANES(nz, AZ, OZ), tnz0, tnz1);
+            unpack2(GB_PLANES(fxw, AX, OX), tfx0, tfx1);
+            unpack2(GB_PLANES(fyw, AY, OY), tfy0, tfy1);
+            unpack2(GB_PLANES(fzw, AZ, OZ), tfz0, tfz1);
+#undef GB_PLANES
+            float lo0, lo1, hi0, hi1;
+            unpack2(mul2(pack2(max3(tnx0, tny0, fmaxf(tnz0, 0.0f)), max3(tnx1, tny1, fmaxf(tnz1, 0.0f))), KN), lo0,
+                    lo1);
+            unpack2(mul2(pack2(min3(tfx0, tfy0, tfz0), min3(tfx1, tfy1, tfz1)), KF), hi0, hi1);
             const int slot = 4 * half + (int)j;
-            uint32_t meta = (meta_w >> (8 * j)) & 0xffu;
-            float tnx = fmaf(byte_f(nx, j), aix, aox), tfx = fmaf(byte_f(fxw, j), aix, aox);
-            float tny = fmaf(byte_f(ny, j), aiy, aoy), tfy = fmaf(byte_f(fyw, j), aiy, aoy);
-            float tnz = fmaf(byte_f(nz, j), aiz, aoz), tfz = fmaf(byte_f(fzw, j), aiz, aoz);
-            float lo = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f)) * 0.99999f;
-            float hi = fminf(fminf(tfx, tfy), tfz) * 1.00001f;
-            if (meta != 0u && lo <= fminf(hi, bound)) {
-                if ((imask >> slot) & 1u) hits_n |= 1u << (24 + (slot ^ r.oxor));
-                else hits_t |= (meta >> 5) << (meta & 31u);
-            }
+            if (lo0 <= fminf(hi0, bound)) hm |= 1u << slot;
+            if (lo1 <= fminf(hi1, bound)) hm |= 2u << slot;
         }
     }
-    *ng = make_uint2(__float_as_uint(n1.x), hits_n | imask);
+    const uint32_t inner = hm & imask;
+    uint32_t leaf = hm & ~imask;
+    uint32_t hits_t = 0;
+    const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+    while (leaf) {
+        uint32_t slot = (uint32_t)__ffs(leaf) - 1u;
+        leaf &= leaf - 1u;
+        uint32_t meta = __byte_perm(slot < 4u ? meta_lo : meta_hi, 0u, 0x4440u | (slot & 3u));
+        hits_t |= (meta >> 5) << (meta & 31u);
+    }
+    *ng = make_uint2(__float_as_uint(n1.x), (xor_permute8(inner, r.oxor) << 24) | imask);
     *tg = make_uint2(__float_as_uint(n1.y), hits_t);
 }
 
@@ -125,25 +194,33 @@ __device__ __forceinline__ void trav_init(Trav& s, const RayInv& r) {
     s.bg = 0.0f;
 }
 
-// One traversal step: every pending triangle of the current group, then one
-// node (or a stack pop).  Returns true when the ray is finished; the result
-// is the (t, id)-minimum in s (any-hit: best_id != none when found).
+// Traversal steps.  The stack holds node groups (hit bits 24-31 set) and
+// postponed triangle groups (24-bit triangle mask, bits 24-31 clear).
+//
+// tri_step: one triangle of the current triangle group.  Returns true when
+// an any-hit query has found its hit.
 template <bool ANY, bool INSTR>
-__device__ __forceinline__ bool trav_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint2* stack,
-                                          uint32_t* status, uint32_t* nvis, uint32_t* ntri) {
-    while (s.tg.y != 0u) {
-        int b = __ffs(s.tg.y) - 1;
-        s.tg.y &= s.tg.y - 1u;
-        const float4* tp = S.tris + 3 * (size_t)(s.tg.x + (uint32_t)b);
-        float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
-        if (INSTR) ++*ntri;
-        float t, u, v;
-        if (intersect_tri(r.o, r.d, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= tmax) {
-            uint32_t id = __float_as_uint(a0.w);
-            if (ANY) { s.best_t = t; s.best_id = id; return true; }
-            if (closer(t, id, s.best_t, s.best_id)) { s.best_t = t; s.best_id = id; s.bb = u; s.bg = v; }
-        }
+__device__ __forceinline__ bool tri_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint32_t* ntri) {
+    int b = __ffs(s.tg.y) - 1;
+    s.tg.y &= s.tg.y - 1u;
+    const float4* tp = S.tris + 3 * (size_t)(s.tg.x + (uint32_t)b);
+    float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
+    if (INSTR) ++*ntri;
+    float t, u, v;
+    if (intersect_tri(r.o, r.d, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= tmax) {
+        uint32_t id = __float_as_uint(a0.w);
+        if (ANY) { s.best_t = t; s.best_id = id; return true; }
+        if (closer(t, id, s.best_t, s.best_id)) { s.best_t = t; s.best_id = id; s.bb = u; s.bg = v; }
     }
+    return false;
+}
+
+// node_step (current triangle group empty): one node of the current node
+// group, or a stack pop.  Returns true when the ray is finished; the result
+// is the (t, id)-minimum in s (any-hit: best_id != none when found).
+template <bool INSTR>
+__device__ __forceinline__ bool node_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint2* stack,
+                                          uint32_t* status, uint32_t* nvis) {
     if (s.ng.y > 0x00ffffffu) {
         uint32_t k = 31u - (uint32_t)__clz(s.ng.y);
         s.ng.y &= ~(1u << k);
@@ -158,8 +235,22 @@ __device__ __forceinline__ bool trav_step(const DevScene& S, const RayInv& r, fl
         intersect_node(S.nodes, child, r, fminf(s.best_t, tmax), &s.ng, &s.tg);
         return false;
     }
-    if (s.sp > 0) { s.ng = stack[--s.sp]; return false; }
+    if (s.sp > 0) {
+        uint2 g = stack[--s.sp];
+        if (g.y > 0x00ffffffu) s.ng = g;
+        else s.tg = g;
+        return false;
+    }
     return true;
+}
+
+// Whole traversal of one ray without warp cooperation.
+template <bool ANY, bool INSTR>
+__device__ __forceinline__ bool trav_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint2* stack,
+                                          uint32_t* status, uint32_t* nvis, uint32_t* ntri) {
+    while (s.tg.y != 0u)
+        if (tri_step<ANY, INSTR>(S, r, tmax, s, ntri)) return true;
+    return node_step<INSTR>(S, r, tmax, s, stack, status, nvis);
 }
 
 struct TraceOut {
@@ -354,7 +445,7 @@ __global__ void __launch_bounds__(kBlock) k_start(Frame F, RenderParams P, int n
 // exhausted), and traversal resumes where each lane stopped.  The first
 // wave is assigned by warp index (warp w takes entries [32w, 32w+32)); later
 // fetches take one atomic per warp on `head`.
-template <bool ANY, bool INSTR, typename Fetch, typename Finish>
+template <bool ANY, bool INSTR, int MODE, typename Fetch, typename Finish>
 __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint32_t* head, int refill,
                                          uint32_t* status, Fetch fetch, Finish finish, uint32_t* nvis,
                                          uint32_t* ntri) {
@@ -406,10 +497,40 @@ __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint
         }
         if (!__any_sync(0xffffffffu, act || fin)) break;
         while (true) {
-            if (act) {
-                bool done = trav_step<ANY, INSTR>(S, r, tmax, s, stack, status, nvis, ntri);
-                if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
-                if (done) { act = false; fin = true; }
+            if (MODE == 0) {
+                // every pending triangle, then one node
+                if (act) {
+                    bool done = trav_step<ANY, INSTR>(S, r, tmax, s, stack, status, nvis, ntri);
+                    if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
+                    if (done) { act = false; fin = true; }
+                }
+            } else {
+                // triangle postponing: when fewer than a fifth of the active
+                // lanes have triangles pending, those lanes stack their
+                // triangle group and keep traversing nodes with the rest of
+                // the warp; otherwise they test one (MODE 1) or all (MODE 2)
+                // of their pending triangles
+                const bool want_tri = act && s.tg.y != 0u;
+                const uint32_t mt = __ballot_sync(0xffffffffu, want_tri);
+                const uint32_t ma = __ballot_sync(0xffffffffu, act);
+                bool do_tri = want_tri;
+                if (want_tri && 5u * (uint32_t)__popc(mt) < (uint32_t)__popc(ma) && s.sp < kStack) {
+                    stack[s.sp++] = s.tg;
+                    s.tg.y = 0u;
+                    do_tri = false;
+                }
+                if (act) {
+                    bool done = false;
+                    if (do_tri) {
+                        if (MODE == 1) done = tri_step<ANY, INSTR>(S, r, tmax, s, ntri);
+                        else
+                            while (s.tg.y != 0u && !done) done = tri_step<ANY, INSTR>(S, r, tmax, s, ntri);
+                    } else {
+                        done = node_step<INSTR>(S, r, tmax, s, stack, status, nvis);
+                    }
+                    if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
+                    if (done) { act = false; fin = true; }
+                }
             }
             uint32_t nidle = (uint32_t)__popc(__ballot_sync(0xffffffffu, !act));
             if (nidle == 32u || (!exhausted && nidle >= (uint32_t)refill)) break;
@@ -424,7 +545,7 @@ __device__ __forceinline__ uint32_t* ctr_set(const Frame& F, int it) { return F.
 // Closest hit of the extension queue.  Misses add handle_no_hit's
 // contribution and end their path; hits draw the bounce's uniforms and emit
 // the area-light shadow ray (arealight-sampler-cpu.cpp:25-143).
-template <bool INSTR>
+template <bool INSTR, int MODE>
 __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderParams P, int it) {
     uint32_t* cs = ctr_set(F, it);
     uint32_t* cn = ctr_set(F, it + 1);
@@ -489,12 +610,12 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderPa
         push(fin && hit, slot, qsh, cs + 2);
         end_paths(F, ended, slot, cn);
     };
-    ray_loop<false, INSTR>(S, count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    ray_loop<false, INSTR, MODE>(S, count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[3], nvis); add_stats(&F.stats[4], ntri); }
 }
 
 // Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
-template <bool INSTR>
+template <bool INSTR, int MODE>
 __global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, Frame F, RenderParams P, int it) {
     uint32_t* cs = ctr_set(F, it);
     const uint32_t count = cs[2];
@@ -515,7 +636,7 @@ __global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, Frame F, RenderPa
             reinterpret_cast<float*>(F.sh_d + slot)[3] = occl ? 1.0f : 0.0f;
         }
     };
-    ray_loop<true, INSTR>(S, count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    ray_loop<true, INSTR, MODE>(S, count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
 }
 
@@ -711,21 +832,41 @@ cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cu
     return cudaGetLastError();
 }
 
+template <bool INSTR, int MODE>
+void launch_extend_t(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
+    static int g = persistent_blocks(k_extend<INSTR, MODE>);
+    k_extend<INSTR, MODE><<<g, kBlock, 0, st>>>(S, F, P, it);
+}
+
+template <bool INSTR, int MODE>
+void launch_shadow_t(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
+    static int g = persistent_blocks(k_shadow<INSTR, MODE>);
+    k_shadow<INSTR, MODE><<<g, kBlock, 0, st>>>(S, F, P, it);
+}
+
 cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
                             cudaStream_t st) {
-    static int g0 = persistent_blocks(k_extend<false>);
-    static int g1 = persistent_blocks(k_extend<true>);
-    if (instrument) k_extend<true><<<g1, kBlock, 0, st>>>(S, F, P, it);
-    else k_extend<false><<<g0, kBlock, 0, st>>>(S, F, P, it);
+    switch (P.tri_mode * 2 + (instrument ? 1 : 0)) {
+        case 0: launch_extend_t<false, 0>(S, F, P, it, st); break;
+        case 1: launch_extend_t<true, 0>(S, F, P, it, st); break;
+        case 2: launch_extend_t<false, 1>(S, F, P, it, st); break;
+        case 3: launch_extend_t<true, 1>(S, F, P, it, st); break;
+        case 4: launch_extend_t<false, 2>(S, F, P, it, st); break;
+        default: launch_extend_t<true, 2>(S, F, P, it, st); break;
+    }
     return cudaGetLastError();
 }
 
 cudaError_t k_launch_shadow(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
                             cudaStream_t st) {
-    static int g0 = persistent_blocks(k_shadow<false>);
-    static int g1 = persistent_blocks(k_shadow<true>);
-    if (instrument) k_shadow<true><<<g1, kBlock, 0, st>>>(S, F, P, it);
-    else k_shadow<false><<<g0, kBlock, 0, st>>>(S, F, P, it);
+    switch (P.tri_mode * 2 + (instrument ? 1 : 0)) {
+        case 0: launch_shadow_t<false, 0>(S, F, P, it, st); break;
+        case 1: launch_shadow_t<true, 0>(S, F, P, it, st); break;
+        case 2: launch_shadow_t<false, 1>(S, F, P, it, st); break;
+        case 3: launch_shadow_t<true, 1>(S, F, P, it, st); break;
+        case 4: launch_shadow_t<false, 2>(S, F, P, it, st); break;
+        default: launch_shadow_t<true, 2>(S, F, P, it, st); break;
+    }
     return cudaGetLastError();
 }
 

@@ -63,6 +63,7 @@ struct RenderParams {
     int spp, L, rng_mode;
     uint32_t seed;
     int refill;        // refill a warp's lanes once this many are idle (1..32)
+    int tri_mode;      // 0: all pending triangles then a node; 1/2: triangle postponing, one / all triangles
     int p0;            // first path sample of the chunk
     int chunk_paths;   // paths in the chunk ((p1 - p0) * n)
 };

@@ -138,6 +138,7 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
     P.rng_mode = d->rng_mode;
     P.seed = d->seed;
     P.refill = 16;
+    P.tri_mode = 0;
     cudaError_t e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(F.status, 0, 4, st);
     if (e == cudaSuccess) e = k_launch_rng_init(F.n, d->seed, F.pristine, st);

@@ -64,7 +64,7 @@ class RenderDesc(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("refill", C.c_int), ("slots", C.c_int), ("sample_mb", C.c_int)]
+    _fields_ = [("refill", C.c_int), ("slots", C.c_int), ("sample_mb", C.c_int), ("tri_mode", C.c_int)]
 
 
 class Hit(C.Structure):
@@ -226,13 +226,13 @@ class Context:
         d["stage_launches"] = list(s.stage_launches)
         return d
 
-    def set_tuning(self, refill: int = 0, slots: int = 0, sample_mb: int = 0):
-        self.check(self.lib.gb_ctx_set_tuning(self.h, C.byref(Tuning(refill, slots, sample_mb))))
+    def set_tuning(self, refill: int = 0, slots: int = 0, sample_mb: int = 0, tri_mode: int = 0):
+        self.check(self.lib.gb_ctx_set_tuning(self.h, C.byref(Tuning(refill, slots, sample_mb, tri_mode))))
 
     def get_tuning(self) -> dict:
         t = Tuning()
         self.check(self.lib.gb_ctx_get_tuning(self.h, C.byref(t)))
-        return {"refill": t.refill, "slots": t.slots, "sample_mb": t.sample_mb}
+        return {"refill": t.refill, "slots": t.slots, "sample_mb": t.sample_mb, "tri_mode": t.tri_mode}
 
     def set_stage_timing(self, on: bool):
         self.check(self.lib.gb_ctx_set_stage_timing(self.h, 1 if on else 0))

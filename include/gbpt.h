@@ -235,6 +235,9 @@ typedef struct {
     int refill;
     int slots;
     int sample_mb;
+    int tri_mode;   /* traversal triangle policy + 1: 1 = every pending triangle then a
+                       node; 2 / 3 = postpone triangle groups when fewer than a fifth of a
+                       warp's active lanes have any, else test one (2) / all (3) */
 } gb_tuning;
 int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* tuning);
 int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* tuning);
