@@ -232,13 +232,10 @@ def run_gbpt(args, rank, world):
         dist.barrier()
     clocks = sampler.stop()
     ctx.set_stage_timing(False)
-    total_ms = float(np.sum(times))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from globillum_gb300 import replicas
     paths = W * H * spp
-    value = paths * args.steps * world / (total_ms / 1e3) / 1e6
+    paths_total, total_ms = replicas.aggregate(paths * args.steps, float(np.sum(times)), dist, "cuda")
+    value = replicas.mpaths_per_s(paths_total, total_ms)
 
     # end to end: through the C ABI with a pinned host image, copies inside
     host = torch.empty((H, W, 3), dtype=torch.float32).pin_memory()

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -91,8 +92,13 @@ int cuda_fail(gb_ctx* c, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
     } while (0)
 
+// Host-side fault injection (gb_set_fault_injection): the k-th device
+// allocation from the moment it is armed fails as if the device were full.
+std::atomic<long long> g_alloc_countdown{-1};
+
 cudaError_t dalloc(std::vector<void*>& list, void** p, size_t bytes) {
     *p = nullptr;
+    if (g_alloc_countdown.load() >= 0 && g_alloc_countdown.fetch_sub(1) == 0) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(p, bytes == 0 ? 16 : bytes);
     if (e == cudaSuccess) list.push_back(*p);
     return e;
@@ -597,6 +603,11 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, c
 int gb_get_stats(const gb_ctx* ctx, gb_stats* stats) {
     if (!ctx || !stats) return GB_ERR_INVALID;
     *stats = ctx->stats;
+    return GB_OK;
+}
+
+int gb_set_fault_injection(int alloc_fail_after) {
+    g_alloc_countdown.store(alloc_fail_after < 0 ? -1 : (long long)alloc_fail_after);
     return GB_OK;
 }
 

@@ -87,7 +87,7 @@ EXPORTS = [
     "gb_scene_get_info", "gb_render", "gb_render_begin", "gb_render_step", "gb_render_paths_done", "gb_render_read",
     "gb_trace_closest", "gb_trace_any", "gb_generate_arealight_sample", "gb_compute_path_contribution_and_bounce",
     "gb_mrg_pool", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
-    "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning",
+    "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning", "gb_set_fault_injection",
 ]
 
 _lib = None
@@ -129,6 +129,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_layout_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.gb_ctx_set_stage_timing.argtypes = [vp, ip]
     lib.gb_ctx_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    lib.gb_set_fault_injection.argtypes = [ip]
     lib.gb_ctx_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     lib.gb_render_noalloc.argtypes = [vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp]
     if path is None:

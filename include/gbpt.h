@@ -269,6 +269,12 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
 int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
                       float* out_rgb, void* stream);
 
+/* Test hook (host-side fault injection): after `alloc_fail_after` further
+ * device allocations made by the library, the next one fails as if the
+ * device were out of memory (the call returns GB_ERR_OOM and the context
+ * stays usable).  A negative value disarms it.  Process-wide. */
+int gb_set_fault_injection(int alloc_fail_after);
+
 /* Bytes of one stored 8-wide node / triangle (for roofline arithmetic). */
 int gb_layout_sizes(int* node_bytes, int* tri_bytes);
 

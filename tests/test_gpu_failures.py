@@ -1,0 +1,99 @@
+"""Failure handling without faulting the GPU: every bad input and every
+injected allocation failure comes back as a status code and a message, and
+the context keeps working afterwards."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from globillum_gb300 import gbpt, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _expect(ctx, rc, code, text=None):
+    assert rc == code, (rc, ctx.lib.gb_last_error(ctx.h))
+    if text:
+        assert text in ctx.lib.gb_last_error(ctx.h).decode()
+
+
+def _create(ctx, sc):
+    desc, keep = gbpt.make_scene_desc(sc)
+    h = C.c_void_p()
+    rc = ctx.lib.gb_scene_create(ctx.h, C.byref(desc), C.byref(h))
+    return rc, h, keep
+
+
+def test_bad_scenes_are_rejected(gpu_ctx):
+    sc = scenes.cornell(width=16, height=16, spp=1, max_bounces=2)
+    bad = scenes.cornell()
+    bad.positions = bad.positions.copy()
+    bad.positions[3, 4] = np.nan
+    rc, _, _ = _create(gpu_ctx, bad)
+    _expect(gpu_ctx, rc, gbpt.GB_ERR_INVALID, "non-finite")
+    bad = scenes.cornell()
+    bad.material_index = bad.material_index.copy()
+    bad.material_index[0] = 99
+    rc, _, _ = _create(gpu_ctx, bad)
+    _expect(gpu_ctx, rc, gbpt.GB_ERR_INVALID, "material index")
+    bad = scenes.cornell()
+    bad.lights = [dict(bad.lights[0], type=gbpt.GB_LIGHT_SKY)]
+    rc, _, _ = _create(gpu_ctx, bad)
+    _expect(gpu_ctx, rc, gbpt.GB_ERR_UNSUPPORTED)
+    # the context still renders
+    scene = gpu_ctx.scene(sc)
+    img = scene.render(sc.camera, sc.render)
+    assert np.isfinite(img).all()
+    scene.close()
+
+
+def test_bad_render_requests_are_rejected(gpu_ctx):
+    sc = scenes.cornell(width=16, height=16, spp=1, max_bounces=2)
+    scene = gpu_ctx.scene(sc)
+    lib = gpu_ctx.lib
+    out = np.zeros(16 * 16 * 3, np.float32)
+    for change, text in [({"width": 0}, "resolution"), ({"width": 1 << 15, "height": 1 << 15}, "resolution"),
+                         ({"spp": 0}, "spp"), ({"max_bounces": 5000}, "spp"), ({"rng_mode": 7}, "rng_mode")]:
+        rd = gbpt.make_render_desc(dict(sc.render, **change))
+        rc = lib.gb_render(gpu_ctx.h, scene.h, C.byref(gbpt.make_camera(sc.camera)), C.byref(rd),
+                           out.ctypes.data_as(C.c_void_p), 0)
+        _expect(gpu_ctx, rc, gbpt.GB_ERR_INVALID, text)
+    cam = gbpt.make_camera(dict(sc.camera, fovy_deg=0.0))
+    rc = lib.gb_render(gpu_ctx.h, scene.h, C.byref(cam), C.byref(gbpt.make_render_desc(sc.render)),
+                       out.ctypes.data_as(C.c_void_p), 0)
+    _expect(gpu_ctx, rc, gbpt.GB_ERR_INVALID, "fovy")
+    rc = lib.gb_render_step(gpu_ctx.h, -1)
+    assert rc == gbpt.GB_ERR_INVALID
+    scene.close()
+
+
+def test_injected_allocation_failures():
+    """Each of the first allocations of a fresh render fails once in turn;
+    the call reports GB_ERR_OOM and the same context then renders the frame
+    correctly."""
+    ctx = gbpt.Context(0)
+    try:
+        sc = scenes.cornell(width=24, height=24, spp=2, max_bounces=3)
+        scene = ctx.scene(sc)
+        good = scene.render(sc.camera, sc.render)
+        lib = ctx.lib
+        for k in range(0, 12, 3):
+            ctx2 = gbpt.Context(0)
+            scene2 = ctx2.scene(sc)
+            lib.gb_set_fault_injection(k)
+            out = np.zeros_like(good)
+            rc = lib.gb_render(ctx2.h, scene2.h, C.byref(gbpt.make_camera(sc.camera)),
+                               C.byref(gbpt.make_render_desc(sc.render)), out.ctypes.data_as(C.c_void_p), 0)
+            lib.gb_set_fault_injection(-1)
+            assert rc == gbpt.GB_ERR_OOM, (k, rc)
+            assert np.array_equal(scene2.render(sc.camera, sc.render), good)
+            scene2.close()
+            ctx2.close()
+        lib.gb_set_fault_injection(0)
+        rc, h, keep = _create(ctx, sc)
+        lib.gb_set_fault_injection(-1)
+        assert rc == gbpt.GB_ERR_OOM
+        scene.close()
+    finally:
+        gbpt.load_library().gb_set_fault_injection(-1)
+        ctx.close()
