@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--refill", type=int, default=0, help="traversal refill threshold (0 = library default)")
     ap.add_argument("--slots", type=int, default=0, help="paths in flight (0 = library default)")
     ap.add_argument("--tri-mode", type=int, default=0, help="traversal triangle policy 1..3 (0 = library default)")
+    ap.add_argument("--graph", type=int, default=0, help="1 = host-driven slot-pool loop, 2 = CUDA graph per chunk")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the mixed batch leg (0 = skip it)")
     return ap.parse_args()
 
 
@@ -178,6 +180,74 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(ctx, args, torch, flush, dist):
+    """Mixed-scene batch (64 icosphere soups, log-uniform 1K-500K triangles,
+    64^2-512^2 pixels, 4/16/64 spp, 1-4 lights, 6 bounces): knobs picked by
+    gb_autotune on a 4-spp proxy frame, then the batched frame
+    (gb_render_batch) against the plain form (one gb_render per scene, in
+    sequence), both device-timed with L2 flushed between steps.  Images of
+    the two forms are bit-identical (checked here), so RMSE is equal."""
+    from globillum_gb300 import replicas, scenes
+    t0 = time.perf_counter()
+    mixed = scenes.mixed_set(args.batch_scenes)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    handles = [ctx.scene(sc) for sc in mixed]
+    build_s = time.perf_counter() - t0
+    jobs = [(h, sc.camera, sc.render) for h, sc in zip(handles, mixed)]
+    paths = sum(sc.render["width"] * sc.render["height"] * sc.render["spp"] for sc in mixed)
+    outs = [torch.empty((sc.render["height"], sc.render["width"], 3), device="cuda", dtype=torch.float32)
+            for sc in mixed]
+    ptrs = [o.data_ptr() for o in outs]
+    t0 = time.perf_counter()
+    tuning, tune_ms = ctx.autotune(jobs, proxy_spp=4, repeats=1)
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.sum(ts))
+
+    def plain():
+        for (h, cam, rd), p in zip(jobs, ptrs):
+            h.render_device(cam, rd, p)
+
+    def batched():
+        ctx.render_batch_device(jobs, ptrs)
+
+    plain_ms = timed(plain)
+    plain_imgs = [o.clone() for o in outs]
+    batch_ms = timed(batched)
+    launches = ctx.stats()["kernel_launches"]
+    same = all(torch.equal(a, b) for a, b in zip(plain_imgs, outs))
+    tot_b, ms_b = replicas.aggregate(paths * args.steps, batch_ms, dist, "cuda")
+    tot_p, ms_p = replicas.aggregate(paths * args.steps, plain_ms, dist, "cuda")
+    vb, vp = replicas.mpaths_per_s(tot_b, ms_b), replicas.mpaths_per_s(tot_p, ms_p)
+    for h in handles:
+        h.close()
+    tris = [sc.num_triangles for sc in mixed]
+    return {"value": vb, "unit": METRIC, "plain_value": vp, "batched_over_plain": vb / vp,
+            "ms_per_step": ms_b / args.steps, "plain_ms_per_step": ms_p / args.steps,
+            "images_identical": bool(same), "paths_per_step": paths, "launches_per_step": int(launches),
+            "workload": {"scenes": len(mixed), "triangles_total": int(sum(tris)), "triangles_min": int(min(tris)),
+                         "triangles_max": int(max(tris)), "resolutions": [64, 128, 256, 512], "spp": [4, 16, 64],
+                         "max_bounces": 6, "generate_s": gen_s, "bvh_build_and_upload_s": build_s},
+            "autotune": {"tuning": tuning, "proxy_frame_ms": tune_ms, "seconds": tune_s, "proxy_spp": 4}}
+
+
 def run_gbpt(args, rank, world):
     import torch
     from globillum_gb300 import build, gbpt
@@ -193,8 +263,8 @@ def run_gbpt(args, rank, world):
     W, H, spp = r["width"], r["height"], r["spp"]
     stream = torch.cuda.current_stream()
     ctx = gbpt.Context(local, stream.cuda_stream)
-    if args.refill or args.slots or args.tri_mode:
-        ctx.set_tuning(refill=args.refill, slots=args.slots, tri_mode=args.tri_mode)
+    if args.refill or args.slots or args.tri_mode or args.graph:
+        ctx.set_tuning(refill=args.refill, slots=args.slots, tri_mode=args.tri_mode, graph=args.graph)
     t0 = time.perf_counter()
     scene = ctx.scene(sc)
     upload_s = time.perf_counter() - t0
@@ -207,14 +277,12 @@ def run_gbpt(args, rank, world):
     torch.cuda.synchronize()
 
     # device-timed steps (scene resident, L2 flushed between steps)
-    ctx.set_stage_timing(True)
     sampler = ClockSampler(local)
     sampler.start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    times, stage_ms, stage_n, launches = [], np.zeros(6), np.zeros(6), 0
-    st_last = None
+    times, launches = [], 0
     for _ in range(args.steps):
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -223,14 +291,22 @@ def run_gbpt(args, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
-        st_last = ctx.stats()
-        stage_ms += np.array(st_last["stage_ms"])
-        stage_n += np.array(st_last["stage_launches"])
-        launches += st_last["kernel_launches"]
+        launches += ctx.stats()["kernel_launches"]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     clocks = sampler.stop()
+
+    # per-stage times of one more frame (CUDA events around every stage
+    # launch; the slot-pool loop then runs from the host)
+    ctx.set_stage_timing(True)
+    flush.zero_()
+    scene.render_device(sc.camera, r, out.data_ptr())
+    torch.cuda.synchronize()
+    st_stage = ctx.stats()
+    stage_ms = np.array(st_stage["stage_ms"])
+    stage_n = np.array(st_stage["stage_launches"])
+    stage_frame_ms = st_stage["render_ms"]
     ctx.set_stage_timing(False)
     from globillum_gb300 import replicas
     paths = W * H * spp
@@ -260,8 +336,8 @@ def run_gbpt(args, rank, world):
     node_b, tri_b = 80, 36
     ext_rays = ist["camera_rays"] + ist["extension_rays"]
     closest_bytes = ist["closest_node_visits"] * node_b + ist["closest_tri_tests"] * tri_b + ext_rays * 48
-    ext_ms = stage_ms[1] / max(1, args.steps)        # per frame
-    ext_launches = stage_n[1] / max(1, args.steps)
+    ext_ms = stage_ms[1]          # per frame
+    ext_launches = stage_n[1]
     peak, peak_kind = measured_peaks()
     achieved = closest_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
     rays = ist["camera_rays"] + ist["extension_rays"] + ist["shadow_rays"]
@@ -276,11 +352,10 @@ def run_gbpt(args, rank, world):
             "mrays_per_s": mrays,
             "rays_per_frame": {"camera": ist["camera_rays"], "extension": ist["extension_rays"],
                                "shadow": ist["shadow_rays"]},
-            "stage_ms_per_frame": {"path_start": stage_ms[0] / args.steps, "closest_hit+light_sample": ext_ms,
-                                   "any_hit": stage_ms[2] / args.steps, "shade": stage_ms[3] / args.steps,
-                                   "path_end+restart": stage_ms[4] / args.steps,
-                                   "moving_average": stage_ms[5] / args.steps},
-            "stage_launches_per_frame": [int(x / args.steps) for x in stage_n],
+            "stage_ms_per_frame": {"path_start": stage_ms[0], "closest_hit+light_sample": ext_ms,
+                                   "any_hit": stage_ms[2], "shade": stage_ms[3], "path_end+restart": stage_ms[4],
+                                   "moving_average": stage_ms[5], "frame_ms_with_stage_events": stage_frame_ms},
+            "stage_launches_per_frame": [int(x) for x in stage_n],
             "roofline": {"bound": "hbm", "kernel": "k_extend (closest-hit traversal + light sample)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": None,
@@ -291,6 +366,8 @@ def run_gbpt(args, rank, world):
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": W * H * 3 * 4},
             "gpu_launches": int(launches)}
+    if args.batch_scenes > 0:
+        line["batched"] = batch_leg(ctx, args, torch, flush, dist)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt, frames, cores = cpu_sample(sc, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",

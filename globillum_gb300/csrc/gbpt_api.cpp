@@ -23,32 +23,54 @@ struct DevBuf {
 };
 
 static const int kSnaps = 16;
+static const size_t kMaxGraphs = 16;
+
+// One scene of a frame as the host sees it.
+struct BatchScene {
+    gb_scene* scene = nullptr;
+    gb_camera cam{};
+    gb_render_desc desc{};
+    float* out = nullptr;   // gb_render_batch output (host or device)
+    int n = 0;              // pixels
+    uint32_t base = 0;      // first pixel of the scene in the frame
+};
+
+// An instantiated chunk graph and everything it was captured with.
+struct ChunkGraph {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec;
+};
 
 struct gb_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;         // capture stream of the chunk graphs
     bool own_stream = false;
     std::string err;
-    // frame: per-slot, per-pixel and sample-buffer capacities
+    // frame: per-slot, per-pixel, sample-buffer and scene-record capacities
     Frame F{};
-    size_t slot_cap = 0, pixel_cap = 0, sample_cap = 0;
+    size_t slot_cap = 0, pixel_cap = 0, sample_cap = 0, scenes_cap = 0;
     std::vector<void*> slot_allocs, pixel_allocs, sample_allocs;
-    int chunk = 1;                      // path samples per chunk of the current render
-    // progressive render
-    gb_scene* scene = nullptr;
-    RenderParams P{};
-    int paths_done = 0;
+    SceneRec* d_scenes = nullptr;
+    // current frame: one scene (gb_render*) or a batch, in layout order (spp descending)
+    std::vector<BatchScene> items;
+    std::vector<SceneRec> recs;
+    int max_spp = 0, max_L = 0;
+    int paths_done = 0;                 // rounds done
     bool active = false;
     bool instrument = false;
+    bool use_graph = false;             // run chunks as CUDA graphs (conditional while loop)
+    std::vector<ChunkGraph> graphs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t* d_status = nullptr;
     unsigned long long* d_stats = nullptr;
     gb_stats stats{};
-    uint64_t launches = 0;
+    uint64_t launches = 0;              // launches outside the slot-pool iterations
     bool stage_timing = false;
     int refill = 16;                    // idle lanes that trigger a warp refill
     int tri_mode = 0;                   // traversal triangle policy (see gb_tuning)
-    int slots = 1 << 20;                // path slots in flight (upper bound; at most one per pixel)
+    int blocks_per_sm = 0;              // resident traversal blocks per SM (0 = occupancy limit)
+    int slots = 1 << 20;                // path slots in flight (upper bound)
     int sample_mb = 1024;               // sample buffer budget (chunk size)
     // queue-count snapshots: pinned ring + events (host stays a few iterations ahead)
     uint32_t* snap_host = nullptr;
@@ -56,10 +78,9 @@ struct gb_ctx {
     std::vector<cudaEvent_t> ev_pool;   // stage timing events (pairs)
     std::vector<int> ev_stage;          // stage of each recorded pair
     size_t ev_used = 0;
-    // curand states right after curand_init(seed, pixel, 0) are kept in
-    // F.pristine while the seed and pixel buffer stay the same
-    size_t pristine_n = 0;
-    uint32_t pristine_seed = 0;
+    // layout (pixels and seed of each scene, in order) whose initial RNG
+    // states F.pristine and scene map F.pscene hold
+    std::vector<uint64_t> pristine_key;
     // scratch for API calls with host pointers
     DevBuf scratch[4];
     float* d_rgb = nullptr;
@@ -119,9 +140,10 @@ cudaError_t ensure_scratch(gb_ctx* ctx, int k, size_t bytes) {
     return e;
 }
 
-// Per-slot buffers for `nslots` slots, per-pixel buffers for `n` pixels and a
-// sample buffer of `samples` float4 entries; grown on demand.
-cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples) {
+// Per-slot buffers for `nslots` slots, per-pixel buffers for `n` pixels,
+// sample and jitter buffers of `samples` float4 entries and `nscenes` scene
+// records; grown on demand.
+cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nscenes) {
     Frame& F = ctx->F;
     cudaError_t e;
     if ((size_t)nslots > ctx->slot_cap) {
@@ -135,22 +157,34 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples) {
         if ((e = dalloc(ctx->slot_allocs, &F.rng, 48 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.pix, 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.pb, 4 * (size_t)nslots)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.ps, 4 * (size_t)nslots)) != cudaSuccess) return e;
         for (int k = 0; k < 4; ++k)
             if ((e = dalloc(ctx->slot_allocs, (void**)&F.q[k], 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.ctr, 4 * 32)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.path_ctr, 4 * 8)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.iter, 4 * 8)) != cudaSuccess) return e;
         ctx->slot_cap = (size_t)nslots;
     }
     if ((size_t)n > ctx->pixel_cap) {
         cudaStreamSynchronize(ctx->stream);
         free_all(ctx->pixel_allocs);
         ctx->pixel_cap = 0;
-        ctx->pristine_n = 0;
+        ctx->pristine_key.clear();
         if ((e = dalloc(ctx->pixel_allocs, (void**)&F.out, sizeof(float4) * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, (void**)&F.pscene, 4 * (size_t)n)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->pixel_allocs, &F.pristine, 48 * (size_t)n)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->pixel_allocs, &F.cursor, 48 * (size_t)n)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->pixel_allocs, &F.jcursor, 48 * (size_t)n)) != cudaSuccess) return e;
         ctx->pixel_cap = (size_t)n;
+    }
+    if ((size_t)nscenes > ctx->scenes_cap) {
+        cudaStreamSynchronize(ctx->stream);
+        if (ctx->d_scenes) cudaFree(ctx->d_scenes);
+        ctx->d_scenes = nullptr;
+        ctx->scenes_cap = 0;
+        std::vector<void*> tmp;
+        if ((e = dalloc(tmp, (void**)&ctx->d_scenes, sizeof(SceneRec) * (size_t)nscenes)) != cudaSuccess) return e;
+        ctx->scenes_cap = (size_t)nscenes;
     }
     if (samples > ctx->sample_cap) {
         cudaStreamSynchronize(ctx->stream);
@@ -228,6 +262,7 @@ int gb_ctx_create(const gb_ctx_desc* desc, gb_ctx** out) {
         if (desc && desc->stream) ctx->stream = (cudaStream_t)desc->stream;
         else { e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking); ctx->own_stream = true; }
     }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(uint32_t));
@@ -252,6 +287,9 @@ void gb_ctx_destroy(gb_ctx* ctx) {
     free_all(ctx->slot_allocs);
     free_all(ctx->pixel_allocs);
     free_all(ctx->sample_allocs);
+    for (ChunkGraph& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    if (ctx->d_scenes) cudaFree(ctx->d_scenes);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
     for (auto& s : ctx->scratch) if (s.p) cudaFree(s.p);
     if (ctx->snap_host) cudaFreeHost(ctx->snap_host);
     for (int k = 0; k < kSnaps; ++k) if (ctx->snap_ev[k]) cudaEventDestroy(ctx->snap_ev[k]);
@@ -379,7 +417,8 @@ void gb_scene_destroy(gb_scene* scene) {
     if (!scene) return;
     if (scene->ctx) {
         cudaSetDevice(scene->ctx->device);
-        if (scene->ctx->scene == scene) { scene->ctx->scene = nullptr; scene->ctx->active = false; }
+        for (const BatchScene& b : scene->ctx->items)
+            if (b.scene == scene) { scene->ctx->active = false; scene->ctx->items.clear(); break; }
         cudaStreamSynchronize(scene->ctx->stream);
     }
     free_all(scene->allocs);
@@ -392,103 +431,156 @@ int gb_scene_get_info(const gb_scene* scene, gb_scene_info* info) {
     return GB_OK;
 }
 
-int gb_render_begin(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* d) {
-    if (!ctx || !scene) return fail(ctx, GB_ERR_INVALID, "null context or scene");
-    int rc = check_render_desc(ctx, cam, d);
-    if (rc != GB_OK) return rc;
+namespace {
+
+// Pixels of the frame that take a sample in round p.  Scenes are laid out by
+// spp, largest first, so these pixels are a prefix of the frame.
+long long round_pixels(const gb_ctx* ctx, int p) {
+    long long n = 0;
+    for (const BatchScene& b : ctx->items) {
+        if (b.desc.spp <= p) break;
+        n += b.n;
+    }
+    return n;
+}
+
+// Path samples in the sample and jitter buffers (sample_mb budget).
+long long sample_budget(const gb_ctx* ctx) { return std::max(1ll, ((long long)ctx->sample_mb << 20) / 16); }
+
+// End of the chunk that starts at round p0 (exclusive, <= end): rounds are
+// added while the chunk's paths fit the sample budget and 2^31, the chunk
+// has at most kMaxRounds rounds, and a round keeps at least half the pixels
+// of the first one (the slot pool of a chunk holds at most one path per
+// pixel of its smallest round).
+int chunk_end(const gb_ctx* ctx, int p0, int end, long long* paths) {
+    const long long budget = sample_budget(ctx);
+    const long long n0 = round_pixels(ctx, p0);
+    long long tot = n0;
+    int p1 = p0 + 1;
+    while (p1 < end && p1 - p0 < kMaxRounds) {
+        long long np = round_pixels(ctx, p1);
+        if (tot + np > budget || tot + np >= (1ll << 31) || 2 * np < n0) break;
+        tot += np;
+        ++p1;
+    }
+    *paths = tot;
+    return p1;
+}
+
+// Lays out the scenes of a render (one scene, or a batch) in HBM and starts
+// it: scene records, pixel ranges, RNG streams.
+int begin_frame(gb_ctx* ctx, std::vector<BatchScene>& items) {
+    ctx->active = false;
+    if (items.empty()) return fail(ctx, GB_ERR_INVALID, "empty batch");
+    long long ntot = 0, total_paths = 0;
+    int max_spp = 0, max_L = 0;
+    for (BatchScene& b : items) {
+        if (!b.scene) return fail(ctx, GB_ERR_INVALID, "null scene");
+        if (b.scene->ctx != ctx) return fail(ctx, GB_ERR_INVALID, "scene belongs to another context");
+        int rc = check_render_desc(ctx, &b.cam, &b.desc);
+        if (rc != GB_OK) return rc;
+        b.n = b.desc.width * b.desc.height;
+        ntot += b.n;
+        total_paths += (long long)b.n * b.desc.spp;
+        max_spp = std::max(max_spp, b.desc.spp);
+        max_L = std::max(max_L, b.desc.max_bounces);
+    }
+    if (ntot > (1ll << 28)) return fail(ctx, GB_ERR_INVALID, "more than 2^28 pixels in one frame");
+    std::stable_sort(items.begin(), items.end(),
+                     [](const BatchScene& a, const BatchScene& b) { return a.desc.spp > b.desc.spp; });
     CK(cudaSetDevice(ctx->device));
-    const int n = d->width * d->height;
-    // chunk: path samples per pass of the slot pool (bounded by the sample
-    // buffer budget and by 2^31 paths); slots: paths in flight
-    long long budget = (long long)ctx->sample_mb << 20;
-    int chunk = (int)std::max(1ll, std::min<long long>(d->spp, budget / (16ll * n)));
-    chunk = (int)std::min<long long>(chunk, std::max(1ll, (1ll << 31) / n - 1));
-    long long chunk_paths = (long long)chunk * n;
-    // at most one slot per pixel: a launch then starts at most one path per
-    // pixel, which keeps the per-pixel stream cursors unshared
-    int nslots = (int)std::max(1ll, std::min<long long>(std::min<long long>(chunk_paths, n), ctx->slots));
-    CK(ensure_frame(ctx, n, nslots, (size_t)chunk_paths));
+    const long long samples = std::min(total_paths, std::max(ntot, sample_budget(ctx)));
+    const int nslots = (int)std::max(1ll, std::min<long long>(ntot, ctx->slots));
+    CK(ensure_frame(ctx, (int)ntot, nslots, (size_t)samples, (int)items.size()));
+    ctx->recs.assign(items.size(), SceneRec{});
+    uint32_t base = 0;
+    for (size_t i = 0; i < items.size(); ++i) {
+        BatchScene& b = items[i];
+        SceneRec& R = ctx->recs[i];
+        R.S = b.scene->S;
+        R.cam = make_camera(b.cam, b.desc.width, b.desc.height);
+        R.sp = make_shade_params(b.desc);
+        R.w = b.desc.width;
+        R.h = b.desc.height;
+        R.n = b.n;
+        R.spp = b.desc.spp;
+        R.L = b.desc.max_bounces;
+        R.rng_mode = b.desc.rng_mode;
+        R.pixel_base = base;
+        R.seed = b.desc.seed;
+        b.base = base;
+        base += (uint32_t)b.n;
+    }
+    ctx->items.swap(items);
+    ctx->max_spp = max_spp;
+    ctx->max_L = max_L;
     Frame& F = ctx->F;
-    F.w = d->width; F.h = d->height; F.n = n;
-    F.nslots = nslots;
+    F.ntot = (int)ntot;
+    F.scenes = ctx->d_scenes;
+    F.nscenes = (int)ctx->items.size();
     F.stats = ctx->d_stats;
     F.status = ctx->d_status;
-    ctx->chunk = chunk;
-    RenderParams& P = ctx->P;
-    P.cam = make_camera(*cam, d->width, d->height);
-    P.sp = make_shade_params(*d);
-    P.spp = d->spp;
-    P.L = d->max_bounces;
-    P.rng_mode = d->rng_mode;
-    P.seed = d->seed;
-    P.refill = ctx->refill;
-    P.tri_mode = ctx->tri_mode;
-    ctx->scene = scene;
     ctx->paths_done = 0;
-    ctx->active = true;
     ctx->launches = 0;
     ctx->ev_used = 0;
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * 8, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    if (!(ctx->pristine_seed == d->seed && ctx->pristine_n >= (size_t)n)) {
-        CK(k_launch_rng_init(n, d->seed, F.pristine, ctx->stream));
-        ctx->launches += 1;
-        ctx->pristine_n = (size_t)n;
-        ctx->pristine_seed = d->seed;
+    CK(cudaMemcpyAsync(ctx->d_scenes, ctx->recs.data(), sizeof(SceneRec) * ctx->recs.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    // F.pscene and the initial RNG states depend on the pixel counts, their
+    // order and the seeds only
+    std::vector<uint64_t> key;
+    key.push_back((uint64_t)ntot);
+    for (const BatchScene& b : ctx->items) key.push_back(((uint64_t)b.desc.seed << 32) | (uint32_t)b.n);
+    if (key != ctx->pristine_key) {
+        CK(k_launch_frame_init(F, true, ctx->stream));
+        ctx->launches += 2;
+        ctx->pristine_key = key;
     }
-    // both streams of pixel i restart at curand_init(seed, i, 0)
-    CK(cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+    // both streams of every pixel restart at curand_init(seed, pixel, 0)
+    CK(cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->active = true;
     return GB_OK;
 }
 
-namespace {
-
-// Path samples [p0, p1) of every pixel through the slot pool.
-int run_chunk(gb_ctx* ctx, int p0, int p1) {
-    RenderParams& P = ctx->P;
+// Slot-pool loop of one chunk driven by the host: every iteration launches
+// extend, shadow, shade, regen and step; the host reads the next queue count
+// through snapshots and stays at most kLead iterations ahead of the GPU.
+int run_chunk_loop(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters) {
     const Frame& F = ctx->F;
-    const DevScene& S = ctx->scene->S;
-    P.p0 = p0;
-    P.chunk_paths = (p1 - p0) * F.n;
-    const int nstart = std::min(F.nslots, P.chunk_paths);
     CK(cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, ctx->stream));
     CK(stage_mark(ctx, 0, true));
-    CK(k_launch_jitter_pool(F, p0, p1, ctx->stream));
+    CK(k_launch_jitter_pool(F, P, ctx->stream));
     CK(k_launch_start(F, P, nstart, ctx->stream));
     CK(stage_mark(ctx, 0, false));
     ctx->launches += 2;
-    // iterations until the next extension queue is empty; the host checks
-    // that count through snapshots and stays at most kLead iterations ahead
-    const long long max_iters = (long long)P.chunk_paths * P.L + 8;
     const int kEvery = 2, kLead = 12;
     int snap_it[kSnaps];
     int head = 0, tail = 0;  // pending snapshots [tail, head)
     bool done = false;
-    for (long long it = 0; !done; ++it) {
+    for (int it = 0; !done; ++it) {
         if (it >= max_iters) return fail(ctx, GB_ERR_TRAVERSAL, "path iteration bound exceeded");
-        const int ii = (int)(it % 3000000);
-        CK(cudaMemsetAsync(F.ctr + 8 * ((ii + 1) % 3), 0, sizeof(uint32_t) * 8, ctx->stream));
         CK(stage_mark(ctx, 1, true));
-        CK(k_launch_extend(S, F, P, ii, ctx->instrument, ctx->stream));
+        CK(k_launch_extend(F, P, ctx->instrument, ctx->stream));
         CK(stage_mark(ctx, 1, false));
         CK(stage_mark(ctx, 2, true));
-        CK(k_launch_shadow(S, F, P, ii, ctx->instrument, ctx->stream));
+        CK(k_launch_shadow(F, P, ctx->instrument, ctx->stream));
         CK(stage_mark(ctx, 2, false));
         CK(stage_mark(ctx, 3, true));
-        CK(k_launch_shade(S, F, P, ii, ctx->stream));
+        CK(k_launch_shade(F, P, ctx->stream));
         CK(stage_mark(ctx, 3, false));
         CK(stage_mark(ctx, 4, true));
-        CK(k_launch_regen(F, P, ii, ctx->stream));
+        CK(k_launch_regen(F, P, ctx->stream));
+        CK(k_launch_step(F, 0, false, max_iters, ctx->stream));
         CK(stage_mark(ctx, 4, false));
-        ctx->launches += 4;
         if (it % kEvery == kEvery - 1) {
             int k = head % kSnaps;
-            CK(cudaMemcpyAsync(ctx->snap_host + k, F.ctr + 8 * ((ii + 1) % 3), sizeof(uint32_t),
+            CK(cudaMemcpyAsync(ctx->snap_host + k, F.ctr + 8 * ((it + 1) % 3), sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaEventRecord(ctx->snap_ev[k], ctx->stream));
-            snap_it[k] = (int)it;
+            snap_it[k] = it;
             ++head;
         }
         while (tail < head) {
@@ -505,21 +597,145 @@ int run_chunk(gb_ctx* ctx, int p0, int p1) {
         }
     }
     CK(stage_mark(ctx, 5, true));
-    CK(k_launch_combine(F, p0, p1, ctx->stream));
+    CK(k_launch_combine(F, P, ctx->stream));
     CK(stage_mark(ctx, 5, false));
     ctx->launches += 1;
     return GB_OK;
 }
 
-}  // namespace
+// Everything a captured chunk graph depends on: the frame's buffers and
+// sizes, the chunk parameters and the kernel variants.
+std::vector<uint64_t> graph_key(const gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters) {
+    const Frame& F = ctx->F;
+    std::vector<uint64_t> k;
+    k.push_back(((uint64_t)(uint32_t)F.ntot << 32) | (uint32_t)F.nslots);
+    k.push_back(((uint64_t)(uint32_t)F.nscenes << 32) | (uint32_t)nstart);
+    k.push_back(((uint64_t)(uint32_t)max_iters << 32) | (ctx->instrument ? 1u : 0u));
+    const void* ptrs[] = {F.scenes, F.ray_o, F.ray_d, F.tp, F.accum, F.sh_o, F.sh_d, F.psc, F.rnd, F.hit_p,
+                          F.hit_n, F.rng, F.pix, F.ps, F.pb, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
+                          F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr,
+                          F.iter, F.stats, F.status};
+    for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
+    static_assert(sizeof(RenderParams) % 4 == 0, "RenderParams is made of 32-bit words");
+    uint32_t w[sizeof(RenderParams) / 4];
+    std::memcpy(w, &P, sizeof(P));
+    for (uint32_t x : w) k.push_back(x);
+    return k;
+}
 
-int gb_render_step(gb_ctx* ctx, int paths) {
-    if (!ctx || !ctx->active || !ctx->scene) return fail(ctx, GB_ERR_INVALID, "no render in progress");
+// One chunk as a CUDA graph: counter reset, jitter pool and first paths,
+// then a conditional WHILE node whose body (extend, shadow, shade, regen,
+// step) repeats until k_step finds the next extension queue empty, then the
+// moving average.  Captured on the context's second stream.
+int build_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters, cudaGraphExec_t* out) {
+    const Frame& F = ctx->F;
+    cudaStream_t a = ctx->aux;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(a, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+    cudaGraphNodeParams np{};
+    if (e == cudaSuccess) e = cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, a);
+    if (e == cudaSuccess) e = k_launch_jitter_pool(F, P, a);
+    if (e == cudaSuccess) e = k_launch_start(F, P, nstart, a);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(a, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    cudaGraphConditionalHandle h = 0;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault);
+    cudaGraphNode_t loop = nullptr;
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&loop, cg, deps, nullptr, nd, &np);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(a, &loop, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) e = k_launch_combine(F, P, a);
+    cudaError_t e2 = cudaStreamEndCapture(a, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(a, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            e = k_launch_extend(F, P, ctx->instrument, a);
+            if (e == cudaSuccess) e = k_launch_shadow(F, P, ctx->instrument, a);
+            if (e == cudaSuccess) e = k_launch_shade(F, P, a);
+            if (e == cudaSuccess) e = k_launch_regen(F, P, a);
+            if (e == cudaSuccess) e = k_launch_step(F, (unsigned long long)h, true, max_iters, a);
+            cudaGraph_t body_out = nullptr;
+            e2 = cudaStreamEndCapture(a, &body_out);
+            if (e == cudaSuccess) e = e2;
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "chunk graph");
+    return GB_OK;
+}
+
+int run_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters) {
+    std::vector<uint64_t> key = graph_key(ctx, P, nstart, max_iters);
+    size_t hit = ctx->graphs.size();
+    for (size_t i = 0; i < ctx->graphs.size(); ++i)
+        if (ctx->graphs[i].key == key) { hit = i; break; }
+    if (hit == ctx->graphs.size()) {
+        cudaGraphExec_t ex = nullptr;
+        int rc = build_chunk_graph(ctx, P, nstart, max_iters, &ex);
+        if (rc != GB_OK) return rc;
+        if (ctx->graphs.size() >= kMaxGraphs) {
+            cudaGraphExecDestroy(ctx->graphs.front().exec);
+            ctx->graphs.erase(ctx->graphs.begin());
+        }
+        ctx->graphs.push_back(ChunkGraph{std::move(key), ex});
+        hit = ctx->graphs.size() - 1;
+    }
+    CK(cudaGraphLaunch(ctx->graphs[hit].exec, ctx->stream));
+    ctx->launches += 3;
+    return GB_OK;
+}
+
+// Rounds [p0, p1) of every pixel that takes them, through the slot pool.
+int run_chunk(gb_ctx* ctx, int p0, int p1) {
+    RenderParams P{};
+    P.refill = ctx->refill;
+    P.tri_mode = ctx->tri_mode;
+    P.blocks_per_sm = ctx->blocks_per_sm;
+    P.p0 = p0;
+    P.rounds = p1 - p0;
+    long long acc = 0, n_last = 0;
+    for (int r = 0; r < P.rounds; ++r) {
+        P.round_start[r] = (uint32_t)acc;
+        n_last = round_pixels(ctx, p0 + r);
+        acc += n_last;
+    }
+    P.round_start[P.rounds] = (uint32_t)acc;
+    P.chunk_paths = (uint32_t)acc;
+    // a launch starts at most nslots consecutive paths, at most one per pixel
+    Frame& F = ctx->F;
+    F.nslots = (int)std::max(1ll, std::min({(long long)ctx->slot_cap, (long long)ctx->slots, n_last}));
+    const int nstart = (int)std::min<long long>(F.nslots, acc);
+    // Every iteration moves each busy slot's path one bounce (at most L + 1
+    // per path), and all slots stay busy until the chunk's last path has
+    // started, so the loop ends within acc (L + 1) / nslots + L + 1
+    // iterations; twice that (plus slack) bounds it.
+    const long long L1 = ctx->max_L + 1;
+    const int max_iters =
+        (int)std::min<long long>(1ll << 30, 2 * ((acc * L1 + F.nslots - 1) / F.nslots + L1) + 16);
+    if (ctx->use_graph && !ctx->stage_timing) return run_chunk_graph(ctx, P, nstart, max_iters);
+    return run_chunk_loop(ctx, P, nstart, max_iters);
+}
+
+int step_frame(gb_ctx* ctx, int paths) {
+    if (!ctx || !ctx->active || ctx->items.empty()) return fail(ctx, GB_ERR_INVALID, "no render in progress");
     if (paths < 0) return fail(ctx, GB_ERR_INVALID, "negative path count");
     CK(cudaSetDevice(ctx->device));
-    int end = std::min(ctx->P.spp, ctx->paths_done + paths);
+    const int end = (int)std::min<long long>(ctx->max_spp, (long long)ctx->paths_done + paths);
     while (ctx->paths_done < end) {
-        int p1 = std::min(end, ctx->paths_done + ctx->chunk);
+        long long cp = 0;
+        int p1 = chunk_end(ctx, ctx->paths_done, end, &cp);
         int rc = run_chunk(ctx, ctx->paths_done, p1);
         if (rc != GB_OK) return rc;
         ctx->paths_done = p1;
@@ -528,34 +744,33 @@ int gb_render_step(gb_ctx* ctx, int paths) {
     return GB_OK;
 }
 
-int gb_render_paths_done(const gb_ctx* ctx, int* done) {
-    if (!ctx || !done) return GB_ERR_INVALID;
-    *done = ctx->paths_done;
+// Packs the frame's colours into RGB triples (device scratch of 3 * ntot floats).
+int pack_frame(gb_ctx* ctx) {
+    const size_t bytes = sizeof(float) * 3 * (size_t)ctx->F.ntot;
+    if (ctx->rgb_cap < bytes) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (ctx->d_rgb) cudaFree(ctx->d_rgb);
+        ctx->d_rgb = nullptr;
+        ctx->rgb_cap = 0;
+        std::vector<void*> tmp;
+        CK(dalloc(tmp, (void**)&ctx->d_rgb, bytes));
+        ctx->rgb_cap = bytes;
+    }
+    if (ctx->paths_done == 0) CK(cudaMemsetAsync(ctx->F.out, 0, sizeof(float4) * (size_t)ctx->F.ntot, ctx->stream));
+    CK(k_launch_pack_rgb(ctx->F.out, ctx->F.ntot, ctx->d_rgb, ctx->stream));
+    ctx->launches += 1;
     return GB_OK;
 }
 
-int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device) {
-    if (!ctx || !ctx->active) return fail(ctx, GB_ERR_INVALID, "no render in progress");
-    if (!out_rgb) return fail(ctx, GB_ERR_INVALID, "null output");
-    CK(cudaSetDevice(ctx->device));
-    int n = ctx->F.n;
-    size_t bytes = sizeof(float) * 3 * (size_t)n;
-    if (ctx->paths_done == 0) CK(cudaMemsetAsync(ctx->F.out, 0, sizeof(float4) * (size_t)n, ctx->stream));
-    if (out_is_device) {
-        CK(k_launch_pack_rgb(ctx->F.out, n, out_rgb, ctx->stream));
-        ctx->launches += 1;
-    } else {
-        if (ctx->rgb_cap < bytes) {
-            if (ctx->d_rgb) cudaFree(ctx->d_rgb);
-            ctx->d_rgb = nullptr;
-            ctx->rgb_cap = 0;
-            CK(cudaMalloc(&ctx->d_rgb, bytes));
-            ctx->rgb_cap = bytes;
-        }
-        CK(k_launch_pack_rgb(ctx->F.out, n, ctx->d_rgb, ctx->stream));
-        ctx->launches += 1;
-        CK(cudaMemcpyAsync(out_rgb, ctx->d_rgb, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    }
+// Copies the packed colours of one scene of the frame to `out`.
+int copy_scene(gb_ctx* ctx, const BatchScene& b, float* out, int out_is_device) {
+    CK(cudaMemcpyAsync(out, ctx->d_rgb + 3 * (size_t)b.base, sizeof(float) * 3 * (size_t)b.n,
+                       out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    return GB_OK;
+}
+
+// Waits for the frame, gathers its statistics and reports kernel status.
+int finish_frame(gb_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     unsigned long long st[8];
     CK(cudaMemcpy(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost));
@@ -566,7 +781,8 @@ int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device) {
     ctx->stats.closest_tri_tests = st[4];
     ctx->stats.shadow_node_visits = st[5];
     ctx->stats.shadow_tri_tests = st[6];
-    ctx->stats.kernel_launches = ctx->launches;
+    // every slot-pool iteration (counted by k_step in st[7]) is 5 launches
+    ctx->stats.kernel_launches = ctx->launches + 5 * st[7];
     ctx->stats.paths_done = ctx->paths_done;
     for (int k = 0; k < 6; ++k) { ctx->stats.stage_ms[k] = 0.0; ctx->stats.stage_launches[k] = 0; }
     for (size_t i = 0; i < ctx->ev_used; ++i) {
@@ -580,6 +796,37 @@ int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device) {
     if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->stats.render_ms = ms;
     cudaGetLastError();
     return check_status(ctx);
+}
+
+}  // namespace
+
+int gb_render_begin(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* d) {
+    if (!ctx || !scene) return fail(ctx, GB_ERR_INVALID, "null context or scene");
+    if (!cam || !d) return fail(ctx, GB_ERR_INVALID, "null camera or render desc");
+    std::vector<BatchScene> items(1);
+    items[0].scene = scene;
+    items[0].cam = *cam;
+    items[0].desc = *d;
+    return begin_frame(ctx, items);
+}
+
+int gb_render_step(gb_ctx* ctx, int paths) { return step_frame(ctx, paths); }
+
+int gb_render_paths_done(const gb_ctx* ctx, int* done) {
+    if (!ctx || !done) return GB_ERR_INVALID;
+    *done = ctx->paths_done;
+    return GB_OK;
+}
+
+int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device) {
+    if (!ctx || !ctx->active || ctx->items.empty()) return fail(ctx, GB_ERR_INVALID, "no render in progress");
+    if (!out_rgb) return fail(ctx, GB_ERR_INVALID, "null output");
+    if (ctx->items.size() != 1) return fail(ctx, GB_ERR_INVALID, "gb_render_read reads single-scene renders");
+    CK(cudaSetDevice(ctx->device));
+    int rc = pack_frame(ctx);
+    if (rc == GB_OK) rc = copy_scene(ctx, ctx->items[0], out_rgb, out_is_device);
+    if (rc != GB_OK) return rc;
+    return finish_frame(ctx);
 }
 
 int gb_render(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc, float* out_rgb,
@@ -600,6 +847,113 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, c
     return rc;
 }
 
+int gb_render_batch(gb_ctx* ctx, int n, const gb_batch_item* items, int out_is_device, int graph_capture) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (n <= 0 || !items) return fail(ctx, GB_ERR_INVALID, "empty batch");
+    std::vector<BatchScene> v((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        if (!items[i].out_rgb) return fail(ctx, GB_ERR_INVALID, "null output");
+        v[i].scene = items[i].scene;
+        v[i].cam = items[i].camera;
+        v[i].desc = items[i].desc;
+        v[i].out = items[i].out_rgb;
+    }
+    const bool saved = ctx->use_graph;
+    if (graph_capture >= 0) ctx->use_graph = graph_capture != 0;
+    int rc = begin_frame(ctx, v);
+    if (rc == GB_OK) rc = step_frame(ctx, ctx->max_spp);
+    ctx->use_graph = saved;
+    if (rc == GB_OK) rc = pack_frame(ctx);
+    for (size_t i = 0; rc == GB_OK && i < ctx->items.size(); ++i)
+        rc = copy_scene(ctx, ctx->items[i], ctx->items[i].out, out_is_device);
+    if (rc != GB_OK) return rc;
+    return finish_frame(ctx);
+}
+
+namespace {
+
+// One autotuner trial: the frame runs as gb_render_batch runs it, without
+// writing images; one warm-up frame (buffers, graph capture), then the
+// median device time of `repeats` frames.
+int tune_trial(gb_ctx* ctx, const std::vector<BatchScene>& base, int repeats, double* ms) {
+    std::vector<double> t;
+    for (int r = 0; r <= repeats; ++r) {
+        std::vector<BatchScene> v = base;
+        int rc = begin_frame(ctx, v);
+        if (rc == GB_OK) rc = step_frame(ctx, ctx->max_spp);
+        if (rc == GB_OK) rc = finish_frame(ctx);
+        if (rc != GB_OK) return rc;
+        if (r > 0) t.push_back(ctx->stats.render_ms);
+    }
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return GB_OK;
+}
+
+}  // namespace
+
+int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, int repeats, gb_tuning* best,
+                double* best_ms) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (n <= 0 || !items) return fail(ctx, GB_ERR_INVALID, "empty batch");
+    if (repeats < 1) repeats = 1;
+    std::vector<BatchScene> v((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        v[i].scene = items[i].scene;
+        v[i].cam = items[i].camera;
+        v[i].desc = items[i].desc;
+        if (proxy_spp > 0) v[i].desc.spp = std::min(v[i].desc.spp, proxy_spp);
+    }
+    gb_tuning cur{};
+    gb_ctx_get_tuning(ctx, &cur);
+    double cur_ms = 0.0;
+    int rc = tune_trial(ctx, v, repeats, &cur_ms);
+    if (rc != GB_OK) return rc;
+    // coordinate descent: one knob at a time over its candidates (gb_tuning
+    // encoding), keeping a value only when it is at least 1% faster
+    struct Knob {
+        int gb_tuning::*field;
+        std::vector<int> vals;
+    };
+    const Knob knobs[] = {
+        {&gb_tuning::graph, {1, 2}},
+        {&gb_tuning::slots, {1 << 18, 1 << 19, 1 << 20, 1 << 21}},
+        {&gb_tuning::refill, {8, 16, 24, 32}},
+        {&gb_tuning::tri_mode, {1, 2, 3}},
+        {&gb_tuning::blocks_per_sm, {1, 3, 4, 5, 6}},
+    };
+    for (int pass = 0; pass < 2; ++pass) {
+        bool changed = false;
+        for (const Knob& k : knobs) {
+            for (int val : k.vals) {
+                if (cur.*(k.field) == val) continue;
+                gb_tuning t = cur;
+                t.*(k.field) = val;
+                gb_ctx_set_tuning(ctx, &t);
+                double ms = 0.0;
+                rc = tune_trial(ctx, v, repeats, &ms);
+                if (rc != GB_OK) {
+                    gb_ctx_set_tuning(ctx, &cur);
+                    return rc;
+                }
+                if (ms < 0.99 * cur_ms) {
+                    cur = t;
+                    cur_ms = ms;
+                    changed = true;
+                }
+            }
+            gb_ctx_set_tuning(ctx, &cur);
+        }
+        if (!changed) break;
+    }
+    gb_ctx_set_tuning(ctx, &cur);
+    ctx->active = false;
+    ctx->items.clear();
+    if (best) *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return GB_OK;
+}
+
 int gb_get_stats(const gb_ctx* ctx, gb_stats* stats) {
     if (!ctx || !stats) return GB_ERR_INVALID;
     *stats = ctx->stats;
@@ -616,7 +970,12 @@ int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* t) {
     if (t->refill < 0 || t->refill > 32) return fail(ctx, GB_ERR_INVALID, "refill must be in 1..32");
     if (t->slots < 0 || t->sample_mb < 0) return fail(ctx, GB_ERR_INVALID, "negative tuning value");
     if (t->tri_mode < 0 || t->tri_mode > 3) return fail(ctx, GB_ERR_INVALID, "tri_mode must be 1..3 (0 keeps)");
+    if (t->graph < 0 || t->graph > 2) return fail(ctx, GB_ERR_INVALID, "graph must be 1 or 2 (0 keeps)");
+    if (t->blocks_per_sm < 0 || t->blocks_per_sm > 65)
+        return fail(ctx, GB_ERR_INVALID, "blocks_per_sm must be 1..65 (0 keeps)");
+    if (t->blocks_per_sm) ctx->blocks_per_sm = t->blocks_per_sm - 1;
     if (t->tri_mode) ctx->tri_mode = t->tri_mode - 1;
+    if (t->graph) ctx->use_graph = t->graph == 2;
     if (t->refill) ctx->refill = t->refill;
     if (t->slots) ctx->slots = t->slots;
     if (t->sample_mb) ctx->sample_mb = t->sample_mb;
@@ -629,6 +988,8 @@ int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* t) {
     t->slots = ctx->slots;
     t->sample_mb = ctx->sample_mb;
     t->tri_mode = ctx->tri_mode + 1;
+    t->graph = ctx->use_graph ? 2 : 1;
+    t->blocks_per_sm = ctx->blocks_per_sm + 1;
     return GB_OK;
 }
 

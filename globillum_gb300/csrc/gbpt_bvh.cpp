@@ -259,11 +259,10 @@ bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err) {
     std::vector<float> cen(3 * (size_t)n);
     for (int t = 0; t < n; ++t) {
         Box b; b.empty();
+        for (int k = 0; k < 9; ++k)  // min/max would drop a NaN coordinate silently
+            if (!std::isfinite(pos[9 * (size_t)t + k])) { *err = "non-finite vertex"; return false; }
         for (int v = 0; v < 3; ++v) b.grow(pos + 9 * (size_t)t + 3 * v);
-        for (int a = 0; a < 3; ++a) {
-            if (!std::isfinite(b.lo[a]) || !std::isfinite(b.hi[a])) { *err = "non-finite vertex"; return false; }
-            cen[3 * (size_t)t + a] = 0.5f * (b.lo[a] + b.hi[a]);
-        }
+        for (int a = 0; a < 3; ++a) cen[3 * (size_t)t + a] = 0.5f * (b.lo[a] + b.hi[a]);
         tb[t] = b;
     }
     std::vector<int> order(n);

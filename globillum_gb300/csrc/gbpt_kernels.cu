@@ -200,10 +200,11 @@ __device__ __forceinline__ void trav_init(Trav& s, const RayInv& r) {
 // tri_step: one triangle of the current triangle group.  Returns true when
 // an any-hit query has found its hit.
 template <bool ANY, bool INSTR>
-__device__ __forceinline__ bool tri_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint32_t* ntri) {
+__device__ __forceinline__ bool tri_step(const float4* __restrict__ tris, const RayInv& r, float tmax, Trav& s,
+                                         uint32_t* ntri) {
     int b = __ffs(s.tg.y) - 1;
     s.tg.y &= s.tg.y - 1u;
-    const float4* tp = S.tris + 3 * (size_t)(s.tg.x + (uint32_t)b);
+    const float4* tp = tris + 3 * (size_t)(s.tg.x + (uint32_t)b);
     float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
     if (INSTR) ++*ntri;
     float t, u, v;
@@ -219,8 +220,8 @@ __device__ __forceinline__ bool tri_step(const DevScene& S, const RayInv& r, flo
 // group, or a stack pop.  Returns true when the ray is finished; the result
 // is the (t, id)-minimum in s (any-hit: best_id != none when found).
 template <bool INSTR>
-__device__ __forceinline__ bool node_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint2* stack,
-                                          uint32_t* status, uint32_t* nvis) {
+__device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, const RayInv& r, float tmax, Trav& s,
+                                          uint2* stack, uint32_t* status, uint32_t* nvis) {
     if (s.ng.y > 0x00ffffffu) {
         uint32_t k = 31u - (uint32_t)__clz(s.ng.y);
         s.ng.y &= ~(1u << k);
@@ -232,7 +233,7 @@ __device__ __forceinline__ bool node_step(const DevScene& S, const RayInv& r, fl
             stack[s.sp++] = s.ng;
         }
         if (INSTR) ++*nvis;
-        intersect_node(S.nodes, child, r, fminf(s.best_t, tmax), &s.ng, &s.tg);
+        intersect_node(nodes, child, r, fminf(s.best_t, tmax), &s.ng, &s.tg);
         return false;
     }
     if (s.sp > 0) {
@@ -246,11 +247,12 @@ __device__ __forceinline__ bool node_step(const DevScene& S, const RayInv& r, fl
 
 // Whole traversal of one ray without warp cooperation.
 template <bool ANY, bool INSTR>
-__device__ __forceinline__ bool trav_step(const DevScene& S, const RayInv& r, float tmax, Trav& s, uint2* stack,
-                                          uint32_t* status, uint32_t* nvis, uint32_t* ntri) {
+__device__ __forceinline__ bool trav_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                          const RayInv& r, float tmax, Trav& s, uint2* stack, uint32_t* status,
+                                          uint32_t* nvis, uint32_t* ntri) {
     while (s.tg.y != 0u)
-        if (tri_step<ANY, INSTR>(S, r, tmax, s, ntri)) return true;
-    return node_step<INSTR>(S, r, tmax, s, stack, status, nvis);
+        if (tri_step<ANY, INSTR>(tris, r, tmax, s, ntri)) return true;
+    return node_step<INSTR>(nodes, r, tmax, s, stack, status, nvis);
 }
 
 struct TraceOut {
@@ -267,7 +269,7 @@ __device__ __forceinline__ bool traverse(const DevScene& S, const RayInv& r, flo
     uint2 stack[kStack];
     uint32_t nv = 0, nt = 0;
     int iters = 0;
-    while (!trav_step<ANY, false>(S, r, tmax, s, stack, status, &nv, &nt)) {
+    while (!trav_step<ANY, false>(S.nodes, S.tris, r, tmax, s, stack, status, &nv, &nt)) {
         if (++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); break; }
     }
     if (out) { out->t = s.best_t; out->beta = s.bb; out->gamma = s.bg; out->id = s.best_id; }
@@ -327,65 +329,101 @@ __device__ __forceinline__ v3 draw3(curandStateMRG32k3a* s) {
     return mk(x, y, z);
 }
 
-// curand states right after curand_init(seed, pixel, 0) (util-kernels.cu:277-285).
-__global__ void k_rng_init(int n, uint32_t seed, curandStateMRG32k3a* out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// curand states right after curand_init(seed, pixel, 0) (util-kernels.cu:277-285)
+// for every pixel of every scene of the frame (pixel = index within its scene).
+__global__ void k_rng_init_frame(Frame F) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= F.ntot) return;
+    const SceneRec& R = F.scenes[F.pscene[g]];
     curandStateMRG32k3a s;
-    curand_init((unsigned long long)seed, (unsigned long long)i, 0ull, &s);
-    out[i] = s;
+    curand_init((unsigned long long)R.seed, (unsigned long long)(g - (int)R.pixel_base), 0ull, &s);
+    ((curandStateMRG32k3a*)F.pristine)[g] = s;
+}
+
+// Scene of every global pixel.
+__global__ void k_fill_pscene(Frame F) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= F.ntot) return;
+    int lo = 0, hi = F.nscenes - 1;
+    while (lo < hi) {  // last scene whose pixel_base <= g
+        int mid = (lo + hi + 1) >> 1;
+        if ((int)F.scenes[mid].pixel_base <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    F.pscene[g] = (uint32_t)lo;
 }
 
 // ------------------------------------------------------------ path slots --
-// A slot carries one path (pixel, sample p) at a time; path l of a chunk is
-// (p, pixel) = (p0 + l / n, l % n).  The reference's three identically
-// seeded per-pixel pools (hybrid-pt.cpp:83-95, util-kernels.cu:284) become:
+// A slot carries one path (scene, pixel, sample p) at a time.  The frame's
+// pixels are laid out scene after scene with scenes sorted by spp (largest
+// first), so the pixels that still take a sample in round p form the prefix
+// [0, N_p) and a chunk's paths enumerate without holes: path l of the chunk
+// is (p0 + r, l - round_start[r]) for the round r holding l.  The
+// reference's three identically seeded per-pixel pools
+// (hybrid-pt.cpp:83-95, util-kernels.cu:284) become:
 //   camera jitter  = update p of the pixel's stream, read from the chunk's
 //                    jitter pool (k_jitter_pool walks each pixel's stream)
 //   lens sample    = update p of pixel (pixel+17)%n (raygen.cu:100-106)
 //   light/path     = updates pL, pL+1, ... one per bounce (hybrid-pt.h:229-233),
-//                    handed out by a per-pixel stream cursor that is advanced
-//                    by L updates whenever a path of the pixel starts.
-// A launch starts at most one path per pixel (the slot pool never holds more
-// paths than pixels and paths are started in path order), so the cursor is
-// never shared within a launch.
-__global__ void k_jitter_pool(Frame F, int p0, int p1) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= F.n) return;
+//                    handed out by a per-pixel stream cursor that advances by
+//                    L updates whenever a path of the pixel starts.
+// A launch starts paths from a contiguous range of at most nslots <= min_r
+// N_r paths, so it starts at most one path per pixel and never shares a
+// cursor; paths of a pixel start in sample order.
+__global__ void k_jitter_pool(Frame F, RenderParams P) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= F.ntot) return;
+    const int spp = F.scenes[F.pscene[g]].spp;
     curandStateMRG32k3a* jc = (curandStateMRG32k3a*)F.jcursor;
-    curandStateMRG32k3a s = jc[i];
-    for (int p = p0; p < p1; ++p) {
+    curandStateMRG32k3a s = jc[g];
+    const int pe = min(P.p0 + P.rounds, spp);
+    for (int p = P.p0; p < pe; ++p) {
         v3 j = draw3(&s);
-        F.jpool[(size_t)(p - p0) * (size_t)F.n + (size_t)i] = make_float4(j.x, j.y, j.z, 0.0f);
+        F.jpool[P.round_start[p - P.p0] + (uint32_t)g] = make_float4(j.x, j.y, j.z, 0.0f);
     }
-    jc[i] = s;
+    jc[g] = s;
 }
 
 __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t l) {
-    const uint32_t pixel = l % (uint32_t)F.n;
-    const uint32_t pc = l / (uint32_t)F.n;  // path within the chunk
-    const float4* jp = F.jpool + (size_t)pc * (size_t)F.n;
-    float4 j = jp[pixel];
+    int lo = 0, hi = P.rounds - 1;
+    while (lo < hi) {  // round holding path l
+        int mid = (lo + hi + 1) >> 1;
+        if (P.round_start[mid] <= l) lo = mid;
+        else hi = mid - 1;
+    }
+    const uint32_t gpix = l - P.round_start[lo];
+    const uint32_t sc = F.pscene[gpix];
+    const SceneRec& R = F.scenes[sc];
+    const uint32_t lp = gpix - R.pixel_base;
+    const float4* jp = F.jpool + P.round_start[lo];
+    float4 j = jp[gpix];
     float lx = 0.0f, ly = 0.0f;
-    if (P.cam.aperture != 0.0f) {
-        float4 lj = jp[(pixel + 17u) % (uint32_t)F.n];
+    if (R.cam.aperture != 0.0f) {
+        float4 lj = jp[R.pixel_base + (lp + 17u) % (uint32_t)R.n];
         lx = lj.z - 0.5f;
         ly = lj.y - 0.5f;
     }
     curandStateMRG32k3a* cur = (curandStateMRG32k3a*)F.cursor;
-    curandStateMRG32k3a bs = cur[pixel];
+    curandStateMRG32k3a bs = cur[gpix];
     ((curandStateMRG32k3a*)F.rng)[slot] = bs;
-    for (int u = 0; u < P.L; ++u) (void)draw3(&bs);
-    cur[pixel] = bs;
+    for (int u = 0; u < R.L; ++u) (void)draw3(&bs);
+    cur[gpix] = bs;
     v3 o, d;
-    camera_ray(P.cam, (int)(pixel % (uint32_t)F.w), (int)(pixel / (uint32_t)F.w), j.x, j.y, lx, ly, &o, &d);
+    camera_ray(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w), j.x, j.y, lx, ly, &o, &d);
     F.ray_o[slot] = make_float4(o.x, o.y, o.z, FLT_MAX);
     F.ray_d[slot] = make_float4(d.x, d.y, d.z, 0.0f);
     F.tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     F.accum[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    F.pix[slot] = pixel;
-    F.pb[slot] = ((uint32_t)P.p0 + pc) << 10;
+    F.pix[slot] = gpix;
+    F.ps[slot] = sc;
+    F.pb[slot] = ((uint32_t)P.p0 + (uint32_t)lo) << 10;
 }
+
+// Counter set of iteration `it`: [0] queue count, [1] extension head,
+// [2] shadow count, [3] shadow head, [4] ended paths (free queue count).
+// The iteration index lives in F.iter (device), so an iteration's launches
+// are the same every time (graph-capturable).
+__device__ __forceinline__ uint32_t* ctr_set(const Frame& F, int it) { return F.ctr + 8 * (it % 3); }
 
 // Slots whose path ended go to the free queue; k_regen stores their
 // samples and starts the next paths.
@@ -396,8 +434,9 @@ __device__ __forceinline__ void end_paths(const Frame& F, bool ended, uint32_t s
 // Stores the sample of every ended path (new_path's input to the moving
 // average) and starts the next paths of the chunk on the freed slots,
 // appending them to the next extension queue.
-__global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P, int it) {
-    uint32_t* cn = F.ctr + 8 * ((it + 1) % 3);
+__global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P) {
+    const int it = *F.iter;
+    uint32_t* cn = ctr_set(F, it + 1);
     const uint32_t count = cn[4];
     uint32_t* qout = F.q[(it + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -407,9 +446,8 @@ __global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P, int i
         uint32_t slot = 0;
         if (ended) {
             slot = F.q[3][qi];
-            uint32_t pixel = F.pix[slot];
             uint32_t p = F.pb[slot] >> 10;
-            F.samples[(size_t)(p - (uint32_t)P.p0) * (size_t)F.n + pixel] = F.accum[slot];
+            F.samples[P.round_start[p - (uint32_t)P.p0] + F.pix[slot]] = F.accum[slot];
         }
         uint32_t m = __ballot_sync(0xffffffffu, ended);
         uint32_t leader = (uint32_t)__ffs(m) - 1u;
@@ -419,7 +457,7 @@ __global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P, int i
         bool started = false;
         if (ended) {
             uint32_t l = base + (uint32_t)__popc(m & ((1u << lane_id()) - 1u));
-            if (l < (uint32_t)P.chunk_paths) {
+            if (l < P.chunk_paths) {
                 start_path(F, P, slot, l);
                 started = true;
             }
@@ -429,14 +467,28 @@ __global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P, int i
     }
 }
 
-// First paths of a chunk: slot s takes path s.
+// First paths of a chunk: slot s takes path s.  Resets the iteration index.
 __global__ void __launch_bounds__(kBlock) k_start(Frame F, RenderParams P, int nstart) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) *F.path_ctr = (uint32_t)nstart;
+    if (s == 0) { *F.path_ctr = (uint32_t)nstart; *F.iter = 0; }
     bool go = s < (uint32_t)nstart;
     if (go) start_path(F, P, s, s);
     add_stats(&F.stats[0], go ? 1u : 0u);
     push(go, s, F.q[0], F.ctr + 0);  // queue of iteration 0
+}
+
+// End of an iteration: clears the counter set two iterations ahead, moves
+// the iteration index, counts the iteration (stats[7]) and tells the graph's loop (when there is one)
+// whether the next extension queue has work.
+__global__ void k_step(Frame F, unsigned long long cond, int has_cond, int max_iters) {
+    const int it = *F.iter;
+    uint32_t* c2 = ctr_set(F, it + 2);
+    for (int k = 0; k < 8; ++k) c2[k] = 0u;
+    const uint32_t next = ctr_set(F, it + 1)[0];
+    *F.iter = it + 1;
+    F.stats[7] += 1ull;
+    if (next != 0u && it + 1 >= max_iters) atomicOr(F.status, (uint32_t)ST_ITER_LIMIT);
+    if (has_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, (next != 0u && it + 1 < max_iters) ? 1u : 0u);
 }
 
 // Persistent-warp ray loop shared by the traversal kernels: lanes whose ray
@@ -444,11 +496,11 @@ __global__ void __launch_bounds__(kBlock) k_start(Frame F, RenderParams P, int n
 // as soon as `refill` lanes are idle (all lanes once the queue is
 // exhausted), and traversal resumes where each lane stopped.  The first
 // wave is assigned by warp index (warp w takes entries [32w, 32w+32)); later
-// fetches take one atomic per warp on `head`.
+// fetches take one atomic per warp on `head`.  Each lane carries the
+// geometry of its own scene.
 template <bool ANY, bool INSTR, int MODE, typename Fetch, typename Finish>
-__device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint32_t* head, int refill,
-                                         uint32_t* status, Fetch fetch, Finish finish, uint32_t* nvis,
-                                         uint32_t* ntri) {
+__device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int refill, uint32_t* status, Fetch fetch,
+                                         Finish finish, uint32_t* nvis, uint32_t* ntri) {
     const uint32_t lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t dyn0 = nwarps * 32u;
@@ -460,6 +512,8 @@ __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint
     float tmax = 0.0f;
     Trav s;
     uint2 stack[kStack];
+    const float4* nodes = nullptr;
+    const float4* tris = nullptr;
     while (true) {
         finish(fin, qi, s);
         fin = false;
@@ -483,7 +537,7 @@ __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint
                 if (q < count) {
                     qi = q;
                     v3 o, d;
-                    if (fetch(q, &o, &d, &tmax)) {
+                    if (fetch(q, &o, &d, &tmax, &nodes, &tris)) {
                         r = make_ray(o, d);
                         trav_init(s, r);
                         iters = 0;
@@ -500,7 +554,7 @@ __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint
             if (MODE == 0) {
                 // every pending triangle, then one node
                 if (act) {
-                    bool done = trav_step<ANY, INSTR>(S, r, tmax, s, stack, status, nvis, ntri);
+                    bool done = trav_step<ANY, INSTR>(nodes, tris, r, tmax, s, stack, status, nvis, ntri);
                     if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
                     if (done) { act = false; fin = true; }
                 }
@@ -522,11 +576,11 @@ __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint
                 if (act) {
                     bool done = false;
                     if (do_tri) {
-                        if (MODE == 1) done = tri_step<ANY, INSTR>(S, r, tmax, s, ntri);
+                        if (MODE == 1) done = tri_step<ANY, INSTR>(tris, r, tmax, s, ntri);
                         else
-                            while (s.tg.y != 0u && !done) done = tri_step<ANY, INSTR>(S, r, tmax, s, ntri);
+                            while (s.tg.y != 0u && !done) done = tri_step<ANY, INSTR>(tris, r, tmax, s, ntri);
                     } else {
-                        done = node_step<INSTR>(S, r, tmax, s, stack, status, nvis);
+                        done = node_step<INSTR>(nodes, r, tmax, s, stack, status, nvis);
                     }
                     if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
                     if (done) { act = false; fin = true; }
@@ -538,15 +592,12 @@ __device__ __forceinline__ void ray_loop(const DevScene& S, uint32_t count, uint
     }
 }
 
-// Counter set of iteration `it`: [0] queue count, [1] extension head,
-// [2] shadow count, [3] shadow head, [4] ended paths (free queue count).
-__device__ __forceinline__ uint32_t* ctr_set(const Frame& F, int it) { return F.ctr + 8 * (it % 3); }
-
 // Closest hit of the extension queue.  Misses add handle_no_hit's
 // contribution and end their path; hits draw the bounce's uniforms and emit
 // the area-light shadow ray (arealight-sampler-cpu.cpp:25-143).
 template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderParams P, int it) {
+__global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
+    const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     uint32_t* cn = ctr_set(F, it + 1);
     const uint32_t count = cs[0];
@@ -554,28 +605,32 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderPa
     uint32_t* qsh = F.q[2];
     uint32_t nvis = 0, ntri = 0;
     curandStateMRG32k3a* rs = (curandStateMRG32k3a*)F.rng;
-    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax) {
+    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris) {
         uint32_t slot = qin[q];
         float4 ro = F.ray_o[slot], rd = F.ray_d[slot];
+        const SceneRec& R = F.scenes[F.ps[slot]];
+        *nodes = R.S.nodes;
+        *tris = R.S.tris;
         *o = ld3(ro); *d = ld3(rd); *tmax = ro.w;
         return true;
     };
     auto finish = [&](bool fin, uint32_t q, const Trav& h) {
         bool hit = false, ended = false;
         uint32_t slot = 0;
-        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (fin) {
             slot = qin[q];
             hit = h.best_id != 0xffffffffu;
+            const SceneRec& R = F.scenes[F.ps[slot]];
             uint32_t pbv = F.pb[slot];
             if ((pbv & 1023u) > 0u) add_stats_lane(&F.stats[1]);
             if (!hit) {
                 float4 tp4 = F.tp[slot];
-                acc = F.accum[slot];
-                v3 add = miss_contribution(ld3(tp4), P.sp);
-                acc = make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f);
+                float4 acc = F.accum[slot];
+                v3 add = miss_contribution(ld3(tp4), R.sp);
+                F.accum[slot] = make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f);
                 ended = true;
             } else {
+                const DevScene& S = R.S;
                 const float4* sh = S.shade + 6 * (size_t)h.best_id;
                 float4 a = __ldg(sh + 0), b = __ldg(sh + 1), c = __ldg(sh + 2);
                 float4 na = __ldg(sh + 3), nb = __ldg(sh + 4), nc = __ldg(sh + 5);
@@ -585,8 +640,8 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderPa
                 v3 rnd = draw3(&st);
                 rs[slot] = st;
                 v3 lr = rnd;
-                if (P.rng_mode == 1) {
-                    int pid = (int)F.pix[slot] + 1;
+                if (R.rng_mode == 1) {
+                    int pid = (int)(F.pix[slot] - R.pixel_base) + 1;
                     float hy = halton(pid, 3);
                     lr = mk(halton(pid, 2), hy, hy);
                 }
@@ -595,7 +650,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderPa
                 if (S.n_lights > 0) {
                     int l = pick_light(S.lights, S.n_lights, S.overall_power, lr.z);
                     LightRec L = S.lights[l];
-                    rect_light_sample(L, S.overall_power, Pp, Nr, lr.x, lr.y, P.sp.shadow_offset, &so, &sd, &smax,
+                    rect_light_sample(L, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset, &so, &sd, &smax,
                                       &psc);
                 }
                 F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
@@ -606,25 +661,28 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevScene S, Frame F, RenderPa
                 F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, 0.0f);
             }
         }
-        if (ended) F.accum[slot] = acc;
         push(fin && hit, slot, qsh, cs + 2);
         end_paths(F, ended, slot, cn);
     };
-    ray_loop<false, INSTR, MODE>(S, count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    ray_loop<false, INSTR, MODE>(count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[3], nvis); add_stats(&F.stats[4], ntri); }
 }
 
 // Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
 template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, Frame F, RenderParams P, int it) {
+__global__ void __launch_bounds__(kBlock) k_shadow(Frame F, RenderParams P) {
+    const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     const uint32_t count = cs[2];
     const uint32_t* qsh = F.q[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&F.stats[2], (unsigned long long)count);
     uint32_t nvis = 0, ntri = 0;
-    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax) {
+    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris) {
         uint32_t slot = qsh[q];
         float4 so = F.sh_o[slot], sd = F.sh_d[slot];
+        const SceneRec& R = F.scenes[F.ps[slot]];
+        *nodes = R.S.nodes;
+        *tris = R.S.tris;
         *o = ld3(so); *d = ld3(sd); *tmax = so.w;
         return so.w >= 0.0f;
     };
@@ -636,14 +694,15 @@ __global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, Frame F, RenderPa
             reinterpret_cast<float*>(F.sh_d + slot)[3] = occl ? 1.0f : 0.0f;
         }
     };
-    ray_loop<true, INSTR, MODE>(S, count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    ray_loop<true, INSTR, MODE>(count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
 }
 
 // BRDF sample/eval, NEE accumulation and next ray for every shadow-queue
 // entry (compute_path_contribution_and_bounce for the hits); paths that end
-// store their sample and their slots start new paths.
-__global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderParams P, int it) {
+// go to the free queue.
+__global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
+    const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     uint32_t* cn = ctr_set(F, it + 1);
     const uint32_t count = cs[2];
@@ -655,14 +714,14 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderPar
         bool valid = qi < count;
         uint32_t slot = 0;
         bool cont = false, ended = false;
-        float4 acc;
         if (valid) {
             slot = qsh[qi];
+            const SceneRec& R = F.scenes[F.ps[slot]];
             float4 sd = F.sh_d[slot];
             float4 hp = F.hit_p[slot], hn = F.hit_n[slot];
             uint32_t mi = __float_as_uint(hp.w);
             float mf[kMaterialFloats];
-            const float4* mp = (const float4*)(S.mats + (size_t)kMaterialFloats * mi);
+            const float4* mp = (const float4*)(R.S.mats + (size_t)kMaterialFloats * mi);
 #pragma unroll
             for (int k = 0; k < 7; ++k) {
                 float4 q = __ldg(mp + k);
@@ -673,11 +732,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderPar
             int bounce = (int)(pbv & 1023u);
             uint32_t path = pbv >> 10;
             float4 rd = F.ray_d[slot], tp4 = F.tp[slot], rn = F.rnd[slot], ps = F.psc[slot];
-            acc = F.accum[slot];
+            float4 acc = F.accum[slot];
             ShadeOut o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps),
-                                   P.sp, F.pix[slot], path, bounce);
+                                   R.sp, F.pix[slot] - R.pixel_base, path, bounce);
             acc = make_float4(acc.x + o.accum_add.x, acc.y + o.accum_add.y, acc.z + o.accum_add.z, 0.0f);
-            cont = o.alive && bounce + 1 < P.L;
+            cont = o.alive && bounce + 1 < R.L;
             ended = !cont;
             F.accum[slot] = acc;
             if (cont) {
@@ -693,17 +752,20 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene S, Frame F, RenderPar
 }
 
 // new_path's moving average (util-kernels.cu:17-25) over the chunk's paths
-// p0 .. p1-1 of every pixel, in path order.
-__global__ void k_combine(Frame F, int p0, int p1) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= F.n) return;
+// p0 .. min(p0 + rounds, spp)-1 of every pixel, in path order.
+__global__ void k_combine(Frame F, RenderParams P) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= F.ntot) return;
+    const int p0 = P.p0;
+    const int pe = min(p0 + P.rounds, F.scenes[F.pscene[g]].spp);
+    if (p0 >= pe) return;
     v3 o = mk(0.0f, 0.0f, 0.0f);
-    if (p0 > 0) { float4 c = F.out[i]; o = mk(c.x, c.y, c.z); }
-    for (int p = p0; p < p1; ++p) {
-        float4 s = F.samples[(size_t)(p - p0) * (size_t)F.n + (size_t)i];
+    if (p0 > 0) { float4 c = F.out[g]; o = mk(c.x, c.y, c.z); }
+    for (int p = p0; p < pe; ++p) {
+        float4 s = F.samples[P.round_start[p - p0] + (uint32_t)g];
         o = combine_sample(o, mk(s.x, s.y, s.z), p);
     }
-    F.out[i] = make_float4(o.x, o.y, o.z, 0.0f);
+    F.out[g] = make_float4(o.x, o.y, o.z, 0.0f);
 }
 
 __global__ void k_pack_rgb(const float4* __restrict__ src, int n, float* dst) {
@@ -803,14 +865,32 @@ __global__ void k_shade_stage(DevScene S, int n, ShadeParams sp, float* ray_orig
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
+// SMs and resident blocks per SM of a persistent kernel.
+struct Grid {
+    int sms, per;
+};
+
 template <typename K>
-int persistent_blocks(K kernel) {
+Grid persistent_grid(K kernel) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, 0);
+    if (sms < 1) sms = 1;
     if (per < 1) per = 1;
-    return sms * per;
+    return Grid{sms, per};
+}
+
+template <typename K>
+int persistent_blocks(K kernel) {
+    Grid g = persistent_grid(kernel);
+    return g.sms * g.per;
+}
+
+// Grid of a persistent traversal kernel: every SM holds min(occupancy
+// limit, blocks_per_sm) blocks (all it can hold when blocks_per_sm is 0).
+inline int traversal_grid(const Grid& g, int blocks_per_sm) {
+    return g.sms * (blocks_per_sm > 0 ? std::min(g.per, blocks_per_sm) : g.per);
 }
 
 }  // namespace
@@ -822,8 +902,9 @@ cudaError_t k_launch_trace(const DevScene& S, int n, const float* orig, const fl
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_rng_init(int n, uint32_t seed, void* out, cudaStream_t st) {
-    k_rng_init<<<blocks_for(n), kBlock, 0, st>>>(n, seed, (curandStateMRG32k3a*)out);
+cudaError_t k_launch_frame_init(const Frame& F, bool rng, cudaStream_t st) {
+    k_fill_pscene<<<blocks_for(F.ntot), kBlock, 0, st>>>(F);
+    if (rng) k_rng_init_frame<<<blocks_for(F.ntot), kBlock, 0, st>>>(F);
     return cudaGetLastError();
 }
 
@@ -833,62 +914,65 @@ cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cu
 }
 
 template <bool INSTR, int MODE>
-void launch_extend_t(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
-    static int g = persistent_blocks(k_extend<INSTR, MODE>);
-    k_extend<INSTR, MODE><<<g, kBlock, 0, st>>>(S, F, P, it);
+void launch_extend_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    static Grid g = persistent_grid(k_extend<INSTR, MODE>);
+    k_extend<INSTR, MODE><<<traversal_grid(g, P.blocks_per_sm), kBlock, 0, st>>>(F, P);
 }
 
 template <bool INSTR, int MODE>
-void launch_shadow_t(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
-    static int g = persistent_blocks(k_shadow<INSTR, MODE>);
-    k_shadow<INSTR, MODE><<<g, kBlock, 0, st>>>(S, F, P, it);
+void launch_shadow_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    static Grid g = persistent_grid(k_shadow<INSTR, MODE>);
+    k_shadow<INSTR, MODE><<<traversal_grid(g, P.blocks_per_sm), kBlock, 0, st>>>(F, P);
 }
 
-cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
-                            cudaStream_t st) {
+cudaError_t k_launch_extend(const Frame& F, const RenderParams& P, bool instrument, cudaStream_t st) {
     switch (P.tri_mode * 2 + (instrument ? 1 : 0)) {
-        case 0: launch_extend_t<false, 0>(S, F, P, it, st); break;
-        case 1: launch_extend_t<true, 0>(S, F, P, it, st); break;
-        case 2: launch_extend_t<false, 1>(S, F, P, it, st); break;
-        case 3: launch_extend_t<true, 1>(S, F, P, it, st); break;
-        case 4: launch_extend_t<false, 2>(S, F, P, it, st); break;
-        default: launch_extend_t<true, 2>(S, F, P, it, st); break;
+        case 0: launch_extend_t<false, 0>(F, P, st); break;
+        case 1: launch_extend_t<true, 0>(F, P, st); break;
+        case 2: launch_extend_t<false, 1>(F, P, st); break;
+        case 3: launch_extend_t<true, 1>(F, P, st); break;
+        case 4: launch_extend_t<false, 2>(F, P, st); break;
+        default: launch_extend_t<true, 2>(F, P, st); break;
     }
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_shadow(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
-                            cudaStream_t st) {
+cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrument, cudaStream_t st) {
     switch (P.tri_mode * 2 + (instrument ? 1 : 0)) {
-        case 0: launch_shadow_t<false, 0>(S, F, P, it, st); break;
-        case 1: launch_shadow_t<true, 0>(S, F, P, it, st); break;
-        case 2: launch_shadow_t<false, 1>(S, F, P, it, st); break;
-        case 3: launch_shadow_t<true, 1>(S, F, P, it, st); break;
-        case 4: launch_shadow_t<false, 2>(S, F, P, it, st); break;
-        default: launch_shadow_t<true, 2>(S, F, P, it, st); break;
+        case 0: launch_shadow_t<false, 0>(F, P, st); break;
+        case 1: launch_shadow_t<true, 0>(F, P, st); break;
+        case 2: launch_shadow_t<false, 1>(F, P, st); break;
+        case 3: launch_shadow_t<true, 1>(F, P, st); break;
+        case 4: launch_shadow_t<false, 2>(F, P, st); break;
+        default: launch_shadow_t<true, 2>(F, P, st); break;
     }
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_shade(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
+cudaError_t k_launch_shade(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g0 = persistent_blocks(k_shade);
-    k_shade<<<g0, kBlock, 0, st>>>(S, F, P, it);
+    k_shade<<<g0, kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, int it, cudaStream_t st) {
+cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g0 = persistent_blocks(k_regen);
-    k_regen<<<g0, kBlock, 0, st>>>(F, P, it);
+    k_regen<<<g0, kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_jitter_pool(const Frame& F, int p0, int p1, cudaStream_t st) {
-    k_jitter_pool<<<blocks_for(F.n), kBlock, 0, st>>>(F, p0, p1);
+cudaError_t k_launch_step(const Frame& F, unsigned long long cond, bool has_cond, int max_iters, cudaStream_t st) {
+    k_step<<<1, 1, 0, st>>>(F, cond, has_cond ? 1 : 0, max_iters);
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_combine(const Frame& F, int p0, int p1, cudaStream_t st) {
-    k_combine<<<blocks_for(F.n), kBlock, 0, st>>>(F, p0, p1);
+cudaError_t k_launch_jitter_pool(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    k_jitter_pool<<<blocks_for(F.ntot), kBlock, 0, st>>>(F, P);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_combine(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    k_combine<<<blocks_for(F.ntot), kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
 }
 

@@ -24,10 +24,26 @@ struct DevScene {
 // Status bits written by the kernels (never a trap).
 enum { ST_STACK_OVERFLOW = 1u, ST_ITER_LIMIT = 2u };
 
-// Wavefront state: per path slot (SoA) and per pixel.
+// One scene of a frame (single renders are a frame of one scene; batches
+// have many): geometry, camera, shading parameters and its pixel range.
+struct SceneRec {
+    DevScene S;
+    CameraRec cam;
+    ShadeParams sp;
+    int w, h, n;        // resolution, pixels
+    int spp, L, rng_mode;
+    uint32_t pixel_base;  // first global pixel of the scene
+    uint32_t seed;
+};
+
+constexpr int kMaxRounds = 64;  // path samples per chunk
+
+// Wavefront state: per path slot (SoA) and per global pixel.
 struct Frame {
-    int w, h, n;       // image and pixel count
+    int ntot;          // pixels of all scenes
     int nslots;        // path slots in flight
+    const SceneRec* scenes;  // device array
+    int nscenes;
     // per slot
     float4* ray_o;     // origin xyz, t_max
     float4* ray_d;     // direction xyz
@@ -40,46 +56,47 @@ struct Frame {
     float4* hit_p;     // hit point xyz | material index bits
     float4* hit_n;     // interpolated (unnormalised) normal
     void* rng;         // curandStateMRG32k3a: light/path stream of the slot's path
-    uint32_t* pix;     // pixel of the slot's path
+    uint32_t* pix;     // global pixel of the slot's path
+    uint32_t* ps;      // scene of the slot's path
     uint32_t* pb;      // path index << 10 | bounce
     uint32_t* q[4];    // queues: extension (ping/pong), shadow, ended paths; nslots entries each
-    // per pixel
+    // per global pixel
     float4* out;       // output_color (moving average)
     void* pristine;    // curandStateMRG32k3a after curand_init(seed, pixel, 0)
     void* cursor;      // curandStateMRG32k3a: light/path stream at the pixel's next path
     void* jcursor;     // curandStateMRG32k3a: camera-jitter stream at the pixel's next path
-    float4* samples;   // [chunk][n] sample of every path of the chunk
-    float4* jpool;     // [chunk][n] camera jitter of every path of the chunk
+    uint32_t* pscene;  // scene of each pixel
+    float4* samples;   // sample of path l of the chunk (l = round_start[r] + pixel)
+    float4* jpool;     // camera jitter of path l of the chunk
     // control
     uint32_t* ctr;     // 3 sets of 8 (by iteration % 3): count, ext head, shadow count, shadow head, ended
     uint32_t* path_ctr;  // next path of the chunk to start
+    int* iter;         // iteration index of the chunk's slot-pool loop
     unsigned long long* stats;  // 0 camera, 1 ext, 2 shadow rays; 3/4 closest, 5/6 shadow node visits / tri tests
     uint32_t* status;
 };
 
+// Launch-wide parameters of one chunk.
 struct RenderParams {
-    CameraRec cam;
-    ShadeParams sp;
-    int spp, L, rng_mode;
-    uint32_t seed;
     int refill;        // refill a warp's lanes once this many are idle (1..32)
     int tri_mode;      // 0: all pending triangles then a node; 1/2: triangle postponing, one / all triangles
-    int p0;            // first path sample of the chunk
-    int chunk_paths;   // paths in the chunk ((p1 - p0) * n)
+    int blocks_per_sm; // resident blocks per SM of the traversal kernels (0 = occupancy limit)
+    int p0, rounds;    // path samples p0 .. p0+rounds-1
+    uint32_t chunk_paths;  // paths of the chunk
+    uint32_t round_start[kMaxRounds + 1];  // first path index of each round (prefix sums of N_p)
 };
 
 cudaError_t k_launch_trace(const DevScene& S, int n, const float* orig, const float* dir, const float* tmax,
                            float4* hits, uint8_t* occluded, bool any, uint32_t* status, cudaStream_t st);
-cudaError_t k_launch_rng_init(int n, uint32_t seed, void* out, cudaStream_t st);
+cudaError_t k_launch_frame_init(const Frame& F, bool rng, cudaStream_t st);
 cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cudaStream_t st);
-cudaError_t k_launch_extend(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
-                            cudaStream_t st);
-cudaError_t k_launch_shadow(const DevScene& S, const Frame& F, const RenderParams& P, int it, bool instrument,
-                            cudaStream_t st);
-cudaError_t k_launch_shade(const DevScene& S, const Frame& F, const RenderParams& P, int it, cudaStream_t st);
-cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, int it, cudaStream_t st);
-cudaError_t k_launch_jitter_pool(const Frame& F, int p0, int p1, cudaStream_t st);
-cudaError_t k_launch_combine(const Frame& F, int p0, int p1, cudaStream_t st);
+cudaError_t k_launch_extend(const Frame& F, const RenderParams& P, bool instrument, cudaStream_t st);
+cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrument, cudaStream_t st);
+cudaError_t k_launch_shade(const Frame& F, const RenderParams& P, cudaStream_t st);
+cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st);
+cudaError_t k_launch_step(const Frame& F, unsigned long long cond, bool has_cond, int max_iters, cudaStream_t st);
+cudaError_t k_launch_jitter_pool(const Frame& F, const RenderParams& P, cudaStream_t st);
+cudaError_t k_launch_combine(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t st);
 cudaError_t k_launch_mrg_pool(int npix, uint32_t seed, int first_update, int num_updates, float* out,
                               cudaStream_t st);

@@ -50,12 +50,14 @@ constexpr size_t kU32 = align_up(4 * (size_t)kNoAllocMaxPixels);              //
 constexpr size_t kCtr = align_up(4 * 32);
 constexpr size_t kStats = align_up(8 * 8);
 constexpr size_t kStatus = align_up(4);
+constexpr size_t kRec = align_up(sizeof(SceneRec));
 // One slot per pixel and one path sample per pass: 10 float4 slot planes,
-// slot RNG, pixel / path words, 4 queues; per pixel the image, the initial
-// RNG states, the two stream cursors, one sample and one jitter value;
-// counters, stats, status.
-constexpr size_t kScratchBytes = 10 * kV4 + kRng + 2 * kU32 + 4 * kU32 + kV4 + 3 * kRng + 2 * kV4 + kCtr + kCtr +
-                                 kStats + kStatus;
+// slot RNG, pixel / scene / path words, 4 queues; per pixel the image, the
+// initial RNG states, the two stream cursors, the scene word, one sample and
+// one jitter value; counters, path counter, iteration, stats, status and the
+// scene record.
+constexpr size_t kScratchBytes = 10 * kV4 + kRng + 3 * kU32 + 4 * kU32 + kV4 + 3 * kRng + kU32 + 2 * kV4 + kCtr +
+                                 kCtr + kCtr + kStats + kStatus + kRec;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -75,27 +77,33 @@ cudaError_t scratch_on_device(int dev, unsigned char** out) {
     return cudaSuccess;
 }
 
-Frame carve(unsigned char* base, int w, int h) {
+Frame carve(unsigned char* base, int n, SceneRec** rec) {
     Frame F{};
-    F.w = w; F.h = h; F.n = w * h;
-    F.nslots = F.n;
+    F.ntot = n;
+    F.nslots = n;
+    F.nscenes = 1;
     size_t off = 0;
     float4** planes[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
     for (float4** p : planes) { *p = (float4*)(base + off); off += kV4; }
     F.rng = base + off; off += kRng;
     F.pix = (uint32_t*)(base + off); off += kU32;
     F.pb = (uint32_t*)(base + off); off += kU32;
+    F.ps = (uint32_t*)(base + off); off += kU32;
     for (int k = 0; k < 4; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
     F.out = (float4*)(base + off); off += kV4;
     F.pristine = base + off; off += kRng;
     F.cursor = base + off; off += kRng;
     F.jcursor = base + off; off += kRng;
+    F.pscene = (uint32_t*)(base + off); off += kU32;
     F.samples = (float4*)(base + off); off += kV4;
     F.jpool = (float4*)(base + off); off += kV4;
     F.ctr = (uint32_t*)(base + off); off += kCtr;
     F.path_ctr = (uint32_t*)(base + off); off += kCtr;
+    F.iter = (int*)(base + off); off += kCtr;
     F.stats = (unsigned long long*)(base + off); off += kStats;
     F.status = (uint32_t*)(base + off); off += kStatus;
+    *rec = (SceneRec*)(base + off);
+    F.scenes = *rec;
     return F;
 }
 
@@ -128,45 +136,58 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
         return fail(scene, GB_ERR_CUDA, "gb_render_noalloc: cudaGetSymbolAddress of the scratch array failed");
     }
     cudaStream_t st = (cudaStream_t)stream;
-    const DevScene& S = *scene_device_view(scene);
-    Frame F = carve(base, d->width, d->height);
+    const int n = d->width * d->height;
+    SceneRec* d_rec = nullptr;
+    Frame F = carve(base, n, &d_rec);
+    SceneRec R{};
+    R.S = *scene_device_view(scene);
+    R.cam = make_camera(*cam, d->width, d->height);
+    R.sp = make_shade_params(*d);
+    R.w = d->width;
+    R.h = d->height;
+    R.n = n;
+    R.spp = d->spp;
+    R.L = d->max_bounces;
+    R.rng_mode = d->rng_mode;
+    R.pixel_base = 0;
+    R.seed = d->seed;
     RenderParams P{};
-    P.cam = make_camera(*cam, d->width, d->height);
-    P.sp = make_shade_params(*d);
-    P.spp = d->spp;
-    P.L = d->max_bounces;
-    P.rng_mode = d->rng_mode;
-    P.seed = d->seed;
     P.refill = 16;
     P.tri_mode = 0;
-    cudaError_t e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
+    P.blocks_per_sm = 0;
+    P.rounds = 1;
+    P.round_start[0] = 0;
+    P.round_start[1] = (uint32_t)n;
+    P.chunk_paths = (uint32_t)n;
+    cudaError_t e = cudaMemcpyAsync(d_rec, &R, sizeof(R), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(F.status, 0, 4, st);
-    if (e == cudaSuccess) e = k_launch_rng_init(F.n, d->seed, F.pristine, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)F.n, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)F.n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = k_launch_frame_init(F, true, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, st);
     // one path sample of every pixel per pass; the host checks the queue
     // count every 8 iterations (a path has at most max_bounces segments)
-    for (int p = 0; p < P.spp && e == cudaSuccess; ++p) {
+    const int max_iters = n * (d->max_bounces + 1) + 8;
+    for (int p = 0; p < d->spp && e == cudaSuccess; ++p) {
         P.p0 = p;
-        P.chunk_paths = F.n;
         e = cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, st);
-        if (e == cudaSuccess) e = k_launch_jitter_pool(F, p, p + 1, st);
-        if (e == cudaSuccess) e = k_launch_start(F, P, F.n, st);
+        if (e == cudaSuccess) e = k_launch_jitter_pool(F, P, st);
+        if (e == cudaSuccess) e = k_launch_start(F, P, n, st);
         uint32_t left = 1;
-        for (int it = 0; e == cudaSuccess && left != 0u && it <= P.L + 1; ++it) {
-            e = cudaMemsetAsync(F.ctr + 8 * ((it + 1) % 3), 0, sizeof(uint32_t) * 8, st);
-            if (e == cudaSuccess) e = k_launch_extend(S, F, P, it, false, st);
-            if (e == cudaSuccess) e = k_launch_shadow(S, F, P, it, false, st);
-            if (e == cudaSuccess) e = k_launch_shade(S, F, P, it, st);
-            if (e == cudaSuccess) e = k_launch_regen(F, P, it, st);
-            if (e == cudaSuccess && (it % 8 == 7 || it == P.L)) {
+        for (int it = 0; e == cudaSuccess && left != 0u && it <= d->max_bounces + 1; ++it) {
+            e = k_launch_extend(F, P, false, st);
+            if (e == cudaSuccess) e = k_launch_shadow(F, P, false, st);
+            if (e == cudaSuccess) e = k_launch_shade(F, P, st);
+            if (e == cudaSuccess) e = k_launch_regen(F, P, st);
+            if (e == cudaSuccess) e = k_launch_step(F, 0, false, max_iters, st);
+            if (e == cudaSuccess && (it % 8 == 7 || it == d->max_bounces)) {
                 e = cudaMemcpyAsync(&left, F.ctr + 8 * ((it + 1) % 3), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             }
         }
-        if (e == cudaSuccess) e = k_launch_combine(F, p, p + 1, st);
+        if (e == cudaSuccess) e = k_launch_combine(F, P, st);
     }
-    if (e == cudaSuccess) e = k_launch_pack_rgb(F.out, F.n, out_rgb, st);
+    if (e == cudaSuccess) e = k_launch_pack_rgb(F.out, n, out_rgb, st);
     uint32_t status = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, F.status, 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

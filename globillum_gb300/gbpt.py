@@ -64,7 +64,12 @@ class RenderDesc(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("refill", C.c_int), ("slots", C.c_int), ("sample_mb", C.c_int), ("tri_mode", C.c_int)]
+    _fields_ = [("refill", C.c_int), ("slots", C.c_int), ("sample_mb", C.c_int), ("tri_mode", C.c_int),
+                ("graph", C.c_int), ("blocks_per_sm", C.c_int)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("desc", RenderDesc), ("out_rgb", C.c_void_p)]
 
 
 class Hit(C.Structure):
@@ -87,7 +92,8 @@ EXPORTS = [
     "gb_scene_get_info", "gb_render", "gb_render_begin", "gb_render_step", "gb_render_paths_done", "gb_render_read",
     "gb_trace_closest", "gb_trace_any", "gb_generate_arealight_sample", "gb_compute_path_contribution_and_bounce",
     "gb_mrg_pool", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
-    "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning", "gb_set_fault_injection",
+    "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning", "gb_set_fault_injection", "gb_render_batch",
+    "gb_autotune",
 ]
 
 _lib = None
@@ -132,6 +138,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_set_fault_injection.argtypes = [ip]
     lib.gb_ctx_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     lib.gb_render_noalloc.argtypes = [vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp]
+    lib.gb_render_batch.argtypes = [vp, ip, C.POINTER(BatchItem), ip, ip]
+    lib.gb_autotune.argtypes = [vp, ip, C.POINTER(BatchItem), ip, ip, C.POINTER(Tuning), C.POINTER(C.c_double)]
     if path is None:
         _lib = lib
     return lib
@@ -227,13 +235,50 @@ class Context:
         d["stage_launches"] = list(s.stage_launches)
         return d
 
-    def set_tuning(self, refill: int = 0, slots: int = 0, sample_mb: int = 0, tri_mode: int = 0):
-        self.check(self.lib.gb_ctx_set_tuning(self.h, C.byref(Tuning(refill, slots, sample_mb, tri_mode))))
+    def set_tuning(self, refill: int = 0, slots: int = 0, sample_mb: int = 0, tri_mode: int = 0, graph: int = 0,
+                   blocks_per_sm: int = 0):
+        t = Tuning(refill, slots, sample_mb, tri_mode, graph, blocks_per_sm)
+        self.check(self.lib.gb_ctx_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self) -> dict:
         t = Tuning()
         self.check(self.lib.gb_ctx_get_tuning(self.h, C.byref(t)))
-        return {"refill": t.refill, "slots": t.slots, "sample_mb": t.sample_mb, "tri_mode": t.tri_mode}
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    @staticmethod
+    def _items(jobs: list, outs: list | None):
+        items = (BatchItem * max(1, len(jobs)))()
+        for i, (sc, cam, rdesc) in enumerate(jobs):
+            items[i] = BatchItem(sc.h, make_camera(cam), make_render_desc(rdesc),
+                                 None if outs is None else _ptr(outs[i]))
+        return items
+
+    def render_batch(self, jobs: list, graph: bool | None = True, outs: list | None = None) -> list:
+        """Renders [(Scene, cam dict, render-desc dict), ...] as one frame
+        (gb_render_batch); returns one (h, w, 3) image per job.  graph=None
+        follows the context's tuning."""
+        if outs is None:
+            outs = [np.empty((int(r["height"]), int(r["width"]), 3), dtype=np.float32) for _, _, r in jobs]
+        g = -1 if graph is None else (1 if graph else 0)
+        self.check(self.lib.gb_render_batch(self.h, len(jobs), self._items(jobs, outs), 0, g))
+        return outs
+
+    def render_batch_device(self, jobs: list, out_ptrs: list, graph: bool | None = None) -> None:
+        """gb_render_batch into device buffers (one pointer per job)."""
+        items = self._items(jobs, None)
+        for i, p in enumerate(out_ptrs):
+            items[i].out_rgb = C.c_void_p(p)
+        g = -1 if graph is None else (1 if graph else 0)
+        self.check(self.lib.gb_render_batch(self.h, len(jobs), items, 1, g))
+
+    def autotune(self, jobs: list, proxy_spp: int = 0, repeats: int = 2) -> tuple[dict, float]:
+        """gb_autotune over the batch; returns (best tuning, its frame ms)
+        and leaves that tuning set."""
+        t = Tuning()
+        ms = C.c_double()
+        self.check(self.lib.gb_autotune(self.h, len(jobs), self._items(jobs, None), proxy_spp, repeats,
+                                        C.byref(t), C.byref(ms)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}, ms.value
 
     def set_stage_timing(self, on: bool):
         self.check(self.lib.gb_ctx_set_stage_timing(self.h, 1 if on else 0))

@@ -231,6 +231,33 @@ def icospheres(n_spheres: int = 800, level: int = 3, width: int = 1280, height: 
                      name=f"icospheres-{n_spheres}x{nf}+10tri")
 
 
+def mixed_set(n_scenes: int = 64, seed: int = 42, tri_range: tuple = (1_000, 500_000),
+              resolutions: tuple = (64, 128, 256, 512), spp_choices: tuple = (4, 16, 64), max_bounces: int = 6,
+              n_materials: int = 256, rr_start: int = 3) -> list:
+    """The mixed-scene batch workload: icosphere soups whose triangle counts
+    are log-uniform in `tri_range`, square resolutions, spp and 1-4 lights
+    drawn per scene.  Spheres have 1280 triangles (320 below 1280 triangles
+    per scene); the box shrinks with the sphere count so that density stays
+    that of the 800-sphere scene."""
+    rng = np.random.default_rng(seed)
+    out = []
+    lo, hi = np.log(tri_range[0]), np.log(tri_range[1])
+    for i in range(n_scenes):
+        tris = int(np.exp(rng.uniform(lo, hi)))
+        level, per = (3, 1280) if tris >= 1280 else (2, 320)
+        ns = max(1, int(round((tris - 10) / per)))
+        res = int(rng.choice(resolutions))
+        spp = int(rng.choice(spp_choices))
+        nl = int(rng.integers(1, 5))
+        box = 100.0 * (ns / 800.0) ** (1.0 / 3.0)
+        sc = icospheres(n_spheres=ns, level=level, width=res, height=res, spp=spp, max_bounces=max_bounces,
+                        n_materials=n_materials, n_lights=nl, box=box, seed_geometry=1000 + i,
+                        seed_materials=2000 + i, seed_lights=3000 + i, rr_start=rr_start)
+        sc.render["seed"] = i
+        out.append(sc)
+    return out
+
+
 def random_rays(scene: SceneData, n: int, seed: int = 0, spread: float = 0.2):
     """Seeded rays from points around the scene's bounding box towards random
     points inside it (traversal parity tests)."""

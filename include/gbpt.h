@@ -160,6 +160,27 @@ int gb_render_step(gb_ctx* ctx, int paths);
 int gb_render_paths_done(const gb_ctx* ctx, int* done);
 int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device);
 
+/* ------------------------------------------------------------ batching */
+/* One scene of a batch: its own camera, resolution, spp, bounces, RNG mode
+ * and seed; out_rgb receives width*height*3 floats as in gb_render. */
+typedef struct {
+    gb_scene* scene;
+    gb_camera camera;
+    gb_render_desc desc;
+    float* out_rgb;
+} gb_batch_item;
+
+/* Renders n scenes of one context as one wavefront frame: their pixels share
+ * the slot pool, so small scenes fill the GPU together and every traversal
+ * lane carries the geometry of its own scene.  Each scene's image is
+ * bit-identical to a gb_render of that scene alone.  graph_capture = 1 runs
+ * each chunk of path samples as one CUDA graph whose slot-pool loop is a
+ * conditional while node (captured once per frame layout and reused);
+ * 0 drives the loop from the host; -1 follows the context's tuning.  The reference renders one scene per
+ * gi_algorithm (hybrid_pt::activate/compute, hybrid-pt.cpp:65-174); this
+ * call has no counterpart there. */
+int gb_render_batch(gb_ctx* ctx, int n, const gb_batch_item* items, int out_is_device, int graph_capture);
+
 /* -------------------------------------------------------------- tracing */
 /* triangle_intersection (t, beta, gamma, ref): ref = canonical triangle id,
  * 0xffffffff and t = FLT_MAX for a miss. */
@@ -238,9 +259,25 @@ typedef struct {
     int tri_mode;   /* traversal triangle policy + 1: 1 = every pending triangle then a
                        node; 2 / 3 = postpone triangle groups when fewer than a fifth of a
                        warp's active lanes have any, else test one (2) / all (3) */
+    int graph;      /* 1 = the host drives the slot-pool loop of single renders; 2 = each
+                       chunk runs as one CUDA graph with a conditional while loop */
+    int blocks_per_sm; /* resident 128-thread blocks per SM of the persistent traversal
+                          kernels + 1: 1 = as many as occupancy allows, k + 1 = at most k */
 } gb_tuning;
 int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* tuning);
 int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* tuning);
+
+/* Autotuner of the wavefront knobs (gb_tuning: graph capture, slot-pool
+ * capacity, refill threshold, triangle policy, resident traversal blocks per
+ * SM) for a batch (or one scene, n = 1): coordinate descent from the
+ * context's current tuning, two passes at most, each candidate timed as the
+ * median device time of `repeats` frames after a warm-up frame.  With
+ * proxy_spp > 0 every scene renders min(spp, proxy_spp) samples per trial
+ * (a cheaper frame of the same layout).  Leaves the best tuning set on the
+ * context and returns it with its frame time; out_rgb of the items is not
+ * used.  The reference has no tunable launch parameters; no counterpart. */
+int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, int repeats,
+                gb_tuning* best, double* best_ms);
 
 /* Records CUDA events around every stage launch of later renders on the
  * context's stream (for per-kernel timing); off by default. */

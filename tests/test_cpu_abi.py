@@ -59,3 +59,43 @@ def test_context_without_gpu(lib_path):
     lib = gbpt.load_library()
     h = C.c_void_p()
     assert lib.gb_ctx_create(C.byref(gbpt.CtxDesc(0, None)), C.byref(h)) == gbpt.GB_ERR_UNSUPPORTED
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors have the size and field offsets of the C structs
+    (compiled with gcc from include/gbpt.h)."""
+    import shutil
+    import subprocess
+    from globillum_gb300 import gbpt
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    pairs = {"gb_principled_params": gbpt.PrincipledParams, "gb_material": gbpt.Material, "gb_light": gbpt.Light,
+             "gb_scene_desc": gbpt.SceneDesc, "gb_scene_info": gbpt.SceneInfo, "gb_camera": gbpt.Camera,
+             "gb_render_desc": gbpt.RenderDesc, "gb_batch_item": gbpt.BatchItem, "gb_hit": gbpt.Hit,
+             "gb_stats": gbpt.Stats, "gb_tuning": gbpt.Tuning, "gb_ctx_desc": gbpt.CtxDesc}
+    c_fields = {"gb_batch_item": ["scene", "camera", "desc", "out_rgb"],
+                "gb_tuning": ["refill", "slots", "sample_mb", "tri_mode", "graph", "blocks_per_sm"],
+                "gb_render_desc": ["width", "height", "spp", "max_bounces", "rng_mode", "seed", "ray_offset",
+                                   "shadow_offset", "background", "rr_start"],
+                "gb_stats": ["camera_rays", "kernel_launches", "render_ms", "stage_ms", "stage_launches",
+                             "paths_done"]}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{ROOT / "include" / "gbpt.h"}"',
+             "int main(void) {"]
+    for name in pairs:
+        lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')
+    for name, fields in c_fields.items():
+        for f in fields:
+            lines.append(f'  printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                   check=True).stdout.splitlines())
+    for name, cls in pairs.items():
+        assert int(got[name]) == C.sizeof(cls), name
+    for name, fields in c_fields.items():
+        for f in fields:
+            assert int(got[f"{name}.{f}"]) == getattr(pairs[name], f).offset, f"{name}.{f}"
