@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--tri-mode", type=int, default=0, help="traversal triangle policy 1..3 (0 = library default)")
     ap.add_argument("--graph", type=int, default=0, help="1 = host-driven slot-pool loop, 2 = CUDA graph per chunk")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the mixed batch leg (0 = skip it)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the path-replay adjoint leg")
+    ap.add_argument("--inverse-iters", type=int, default=200, help="Adam iterations of the inverse leg (0 = skip)")
     return ap.parse_args()
 
 
@@ -248,6 +250,182 @@ def batch_leg(ctx, args, torch, flush, dist):
             "autotune": {"tuning": tuning, "proxy_frame_ms": tune_ms, "seconds": tune_s, "proxy_spp": 4}}
 
 
+def adjoint_leg(ctx, scene, sc, args, torch, flush, orc):
+    """Path-replay adjoint on the 1M-triangle scene at 512x512, 16 spp, 4
+    bounces: L2 loss against a target rendered from the same geometry with
+    independently seeded material parameters; gradients for all materials'
+    base colour, roughness, metallic and all lights' emission.  Times
+    forward (gb_render) and backward (gb_backward) on the device, checks the
+    gradient on 32 seeded parameters against central differences (h = 1e-3)
+    of gb_forward(eval_params) at common random numbers and, on the CPU,
+    against the oracle's FP64 dual-number replay of the same paths."""
+    from globillum_gb300 import scenes
+    rd = dict(sc.render, width=512, height=512, spp=16, max_bounces=4)
+    H, W = rd["height"], rd["width"]
+    x0 = scene.get_params()
+    tgt_sc = scenes.icospheres(n_spheres=1, seed_materials=97)  # materials only; geometry unused
+    xt = x0.copy()
+    xt[:5 * len(sc.materials)] = scenes.param_vector(tgt_sc)[:5 * len(sc.materials)]
+    scene.set_params(xt)
+    target = torch.empty((H, W, 3), device="cuda", dtype=torch.float32)
+    scene.render_device(sc.camera, rd, target.data_ptr())
+    scene.set_params(x0)
+    img = torch.empty_like(target)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    fwd_ms = timed(lambda: scene.render_device(sc.camera, rd, img.data_ptr()))
+    dimg = (2.0 * (img - target)).contiguous()
+    grad_box = {}
+
+    def bwd():
+        grad_box["g"] = scene.backward_device(sc.camera, rd, dimg.data_ptr())
+
+    bwd_ms = timed(bwd)
+    grad = grad_box["g"]
+    loss0 = float(((img - target) ** 2).sum().item())
+    # finite differences of the frozen-sampling forward, 32 seeded parameters
+    rng = np.random.default_rng(2024)
+    live = np.flatnonzero(np.abs(grad) > 1e-4 * np.abs(grad).max())
+    sel = np.sort(rng.choice(live, size=min(32, live.size), replace=False))
+    tgt_np = target.cpu().numpy().astype(np.float64)
+    h = 1e-3
+    fd = []
+    for i in sel:
+        xp, xm = x0.copy(), x0.copy()
+        xp[i] += h
+        xm[i] -= h
+        lp = float(((scene.forward(sc.camera, rd, xp).astype(np.float64) - tgt_np) ** 2).sum())
+        lm = float(((scene.forward(sc.camera, rd, xm).astype(np.float64) - tgt_np) ** 2).sum())
+        fd.append((lp - lm) / (2 * h))
+    fd = np.array(fd)
+    rel_fd = np.abs(grad[sel] - fd) / np.maximum(np.abs(fd), 1e-12)
+    out = {"workload": {"scene": sc.name, "width": W, "height": H, "spp": rd["spp"], "max_bounces": rd["max_bounces"],
+                        "params": int(x0.size), "loss": "L2 to a target from materials seeded 97"},
+           "forward_ms": fwd_ms, "backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms, "loss": loss0,
+           "adjoint_record_bytes": int(80 * rd["max_bounces"] * min(W * H, 1 << 20)),
+           "finite_differences": {"h": h, "params": int(sel.size), "median_rel_err": float(np.median(rel_fd)),
+                                  "max_rel_err": float(rel_fd.max()),
+                                  "chosen_from": "parameters with |grad| > 1e-4 max|grad|, seeded",
+                                  "sampling": "frozen at the current parameters (gb_forward eval_params)"}}
+    if orc is not None:
+        pool = ctx.mrg_pool(W * H, rd["spp"] * rd["max_bounces"], seed=rd["seed"])
+        t0 = time.perf_counter()
+        ref = orc.adjoint_f64(sc.camera, rd, pool, dimg.cpu().numpy(), sel)
+        rel64 = np.abs(grad[sel].astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-12)
+        out["fp64_replay"] = {"params": int(sel.size), "median_rel_err": float(np.median(rel64)),
+                              "max_rel_err": float(rel64.max()), "cpu_seconds": time.perf_counter() - t0}
+    return out
+
+
+def inverse_leg(ctx, args, torch, dist):
+    """Batched inverse rendering: 16 icosphere scenes (10K-200K triangles,
+    256x256, 8 spp, 4 bounces, 64 principled materials, 1-4 lights).  Each
+    scene's 64 materials (base colour, roughness, metallic) are recovered
+    from a target rendered with hidden seeded parameters: Adam (lr 1e-2) on
+    the summed L2 image losses, starting from the scenes' own seeded
+    materials.  One iteration = parameters uploaded, one batched forward
+    frame (gb_render_batch) and one batched adjoint frame
+    (gb_backward_batch), each run as CUDA-graph chunks.  The same iteration
+    is also timed as 16 sequential plain runs (gb_render + gb_backward per
+    scene)."""
+    from globillum_gb300 import replicas, scenes
+    n_sc = 16
+    mixed = scenes.mixed_set(n_sc, seed=77, tri_range=(10_000, 200_000), resolutions=(256,), spp_choices=(8,),
+                             max_bounces=4, n_materials=64)
+    handles = [ctx.scene(sc) for sc in mixed]
+    jobs = [(h, sc.camera, sc.render) for h, sc in zip(handles, mixed)]
+    nmp = 5 * 64
+    x_init = [h.get_params() for h in handles]
+    x_hidden = []
+    for i, (h, x0) in enumerate(zip(handles, x_init)):
+        xh = x0.copy()
+        xh[:nmp] = scenes.param_vector(scenes.icospheres(n_spheres=1, n_materials=64,
+                                                         seed_materials=5000 + i))[:nmp]
+        x_hidden.append(xh)
+    # targets with the hidden parameters
+    targets = []
+    for h, xh, (_, cam, rd) in zip(handles, x_hidden, jobs):
+        h.set_params(xh)
+        targets.append(torch.from_numpy(h.render(cam, rd)).cuda())
+    for h, x0 in zip(handles, x_init):
+        h.set_params(x0)
+    outs = [torch.empty_like(t) for t in targets]
+    ptrs = [o.data_ptr() for o in outs]
+    x = torch.tensor(np.stack(x_init), requires_grad=True)
+    opt = torch.optim.Adam([x], lr=1e-2)
+    free = torch.zeros_like(x)
+    free[:, :nmp] = 1.0
+    paths = sum(sc.render["width"] * sc.render["height"] * sc.render["spp"] for sc in mixed)
+
+    def param_err(xs):
+        xs = np.asarray(xs)
+        e = {}
+        for name, k in (("colour", [0, 1, 2]), ("roughness", [3]), ("metallic", [4])):
+            idx = np.array([5 * m + j for m in range(64) for j in k])
+            e[name] = float(np.sqrt(np.mean([(xs[i][idx] - x_hidden[i][idx]) ** 2 for i in range(n_sc)])))
+        return e
+
+    err0 = param_err(x.detach().numpy())
+    losses = []
+    t_iter = []
+    for it in range(args.inverse_iters):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xs = x.detach().numpy()
+        for h, xi in zip(handles, xs):
+            h.set_params(xi)
+        ctx.render_batch_device(jobs, ptrs, graph=True)
+        dimgs = [(2.0 * (o - t)).contiguous() for o, t in zip(outs, targets)]
+        g = ctx.backward_batch(jobs, [d.cpu().numpy() for d in dimgs], graph=True)
+        torch.cuda.synchronize()
+        t_iter.append(time.perf_counter() - t0)
+        losses.append(float(sum(((o - t) ** 2).sum().item() for o, t in zip(outs, targets))))
+        x.grad = torch.from_numpy(np.stack(g)) * free
+        opt.step()
+        with torch.no_grad():
+            x[:, :nmp] = x[:, :nmp].clamp(0.0, 1.0)
+    err1 = param_err(x.detach().numpy())
+    # the same iteration as 16 sequential plain runs (gb_render + gb_backward per scene)
+    seq = []
+    for _ in range(max(3, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for (h, cam, rd), p, t in zip(jobs, ptrs, targets):
+            h.render_device(cam, rd, p)
+        for (h, cam, rd), o, t in zip(jobs, outs, targets):
+            h.backward(cam, rd, (2.0 * (o - t)).cpu().numpy())
+        torch.cuda.synchronize()
+        seq.append(time.perf_counter() - t0)
+    for h, x0 in zip(handles, x_init):
+        h.close()
+    it_s = float(np.median(t_iter[1:] if len(t_iter) > 1 else t_iter))
+    seq_s = float(np.median(seq))
+    return {"workload": {"scenes": n_sc, "triangles": [int(sc.num_triangles) for sc in mixed], "resolution": 256,
+                         "spp": 8, "max_bounces": 4, "materials_per_scene": 64, "iterations": args.inverse_iters,
+                         "optimizer": "Adam lr 1e-2 on base colour, roughness, metallic"},
+            "param_rmse_initial": err0, "param_rmse_final": err1,
+            "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None,
+            "iteration_ms": it_s * 1e3, "sequential_iteration_ms": seq_s * 1e3,
+            "batched_over_sequential": seq_s / it_s,
+            "mpaths_per_s_fwd_plus_bwd": 2 * paths / it_s / 1e6,
+            "note": "wall-clock per iteration including parameter upload and host gradient copies"}
+
+
 def run_gbpt(args, rank, world):
     import torch
     from globillum_gb300 import build, gbpt
@@ -368,11 +546,20 @@ def run_gbpt(args, rank, world):
             "gpu_launches": int(launches)}
     if args.batch_scenes > 0:
         line["batched"] = batch_leg(ctx, args, torch, flush, dist)
+    orc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, dt, frames, cores = cpu_sample(sc, args.cpu_seconds)
+        from oracle import oracle
+        orc = oracle.OracleScene(sc, use_bvh=True)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_leg(ctx, scene, sc, args, torch, flush, orc)
+    if args.inverse_iters > 0:
+        line["inverse"] = inverse_leg(ctx, args, torch, dist)
+    if orc is not None:
+        v, dt, frames, cores = cpu_sample(sc, args.cpu_seconds, orc=orc)
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
                                 "sample": f"{frames} whole {W}x{H} frames at 1 spp ({dt:.1f} s of CPU time, "
                                           f"BVH build excluded)"}
+        orc.close()
     scene.close()
     ctx.close()
     if rank == 0:

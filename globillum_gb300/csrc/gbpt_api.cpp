@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,14 @@ struct BatchScene {
     float* out = nullptr;   // gb_render_batch output (host or device)
     int n = 0;              // pixels
     uint32_t base = 0;      // first pixel of the scene in the frame
+    // frozen-sampling replay: records the BRDFs / emission are evaluated with
+    const float* mats_eval = nullptr;
+    const LightRec* lights_eval = nullptr;
+    // adjoint: loss gradient of the image, parameter gradient output and the
+    // scene's first record-gradient float
+    const float* dimg = nullptr;
+    float* grad_out = nullptr;
+    uint32_t grad_base = 0;
 };
 
 // An instantiated chunk graph and everything it was captured with.
@@ -60,6 +69,14 @@ struct gb_ctx {
     bool active = false;
     bool instrument = false;
     bool use_graph = false;             // run chunks as CUDA graphs (conditional while loop)
+    int mode = MODE_FORWARD;            // render mode of the next chunks
+    // frozen-sampling replay and adjoint buffers
+    std::vector<void*> adj_allocs;
+    size_t tp0_cap = 0, adj_cap = 0, dimg_cap = 0, grad_cap = 0, gsum_cap = 0;
+    double* d_gsum = nullptr;
+    float* d_eval_mats = nullptr;
+    LightRec* d_eval_lights = nullptr;
+    size_t eval_mats_cap = 0, eval_lights_cap = 0;
     std::vector<ChunkGraph> graphs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t* d_status = nullptr;
@@ -92,6 +109,10 @@ struct gb_scene {
     DevScene S{};
     std::vector<void*> allocs;
     gb_scene_info info{};
+    // host copies of the descriptions the differentiable parameters change
+    std::vector<gb_material> mats;
+    std::vector<gb_principled_params> params;
+    std::vector<gb_light> lights;
 };
 
 namespace {
@@ -288,6 +309,7 @@ void gb_ctx_destroy(gb_ctx* ctx) {
     free_all(ctx->pixel_allocs);
     free_all(ctx->sample_allocs);
     for (ChunkGraph& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    free_all(ctx->adj_allocs);
     if (ctx->d_scenes) cudaFree(ctx->d_scenes);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
     for (auto& s : ctx->scratch) if (s.p) cudaFree(s.p);
@@ -402,6 +424,11 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     sc->S.overall_power = overall_power(lights.data(), (int)lights.size());
     sc->S.n_nodes = bvh.n_nodes;
     sc->S.n_tris = bvh.n_tris;
+    sc->S.mats_eval = sc->S.mats;
+    sc->S.lights_eval = sc->S.lights;
+    sc->mats.assign(d->materials, d->materials + d->num_materials);
+    if (d->num_params > 0) sc->params.assign(d->params, d->params + d->num_params);
+    if (d->num_lights > 0) sc->lights.assign(d->lights, d->lights + d->num_lights);
     sc->info.num_triangles = n;
     sc->info.num_nodes = bvh.n_nodes;
     sc->info.depth = bvh.depth;
@@ -508,6 +535,11 @@ int begin_frame(gb_ctx* ctx, std::vector<BatchScene>& items) {
         R.rng_mode = b.desc.rng_mode;
         R.pixel_base = base;
         R.seed = b.desc.seed;
+        mrg_jump_matrices(3ull * (uint64_t)R.L, R.jump1, R.jump2);
+        if (b.mats_eval) R.S.mats_eval = b.mats_eval;
+        if (b.lights_eval) R.S.lights_eval = b.lights_eval;
+        R.n_mats = (int)b.scene->mats.size();
+        R.grad_base = b.grad_base;
         b.base = base;
         base += (uint32_t)b.n;
     }
@@ -572,6 +604,7 @@ int run_chunk_loop(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters
         CK(k_launch_shade(F, P, ctx->stream));
         CK(stage_mark(ctx, 3, false));
         CK(stage_mark(ctx, 4, true));
+        if (P.mode == MODE_ADJOINT) CK(k_launch_adjoint(F, P, ctx->stream));
         CK(k_launch_regen(F, P, ctx->stream));
         CK(k_launch_step(F, 0, false, max_iters, ctx->stream));
         CK(stage_mark(ctx, 4, false));
@@ -614,8 +647,9 @@ std::vector<uint64_t> graph_key(const gb_ctx* ctx, const RenderParams& P, int ns
     const void* ptrs[] = {F.scenes, F.ray_o, F.ray_d, F.tp, F.accum, F.sh_o, F.sh_d, F.psc, F.rnd, F.hit_p,
                           F.hit_n, F.rng, F.pix, F.ps, F.pb, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
                           F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr,
-                          F.iter, F.stats, F.status};
+                          F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad};
     for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
+    k.push_back(((uint64_t)(uint32_t)F.grad_stride << 32) | (uint32_t)F.grad_replicas);
     static_assert(sizeof(RenderParams) % 4 == 0, "RenderParams is made of 32-bit words");
     uint32_t w[sizeof(RenderParams) / 4];
     std::memcpy(w, &P, sizeof(P));
@@ -663,6 +697,7 @@ int build_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_it
             e = k_launch_extend(F, P, ctx->instrument, a);
             if (e == cudaSuccess) e = k_launch_shadow(F, P, ctx->instrument, a);
             if (e == cudaSuccess) e = k_launch_shade(F, P, a);
+            if (e == cudaSuccess && P.mode == MODE_ADJOINT) e = k_launch_adjoint(F, P, a);
             if (e == cudaSuccess) e = k_launch_regen(F, P, a);
             if (e == cudaSuccess) e = k_launch_step(F, (unsigned long long)h, true, max_iters, a);
             cudaGraph_t body_out = nullptr;
@@ -703,6 +738,7 @@ int run_chunk(gb_ctx* ctx, int p0, int p1) {
     P.refill = ctx->refill;
     P.tri_mode = ctx->tri_mode;
     P.blocks_per_sm = ctx->blocks_per_sm;
+    P.mode = ctx->mode;
     P.p0 = p0;
     P.rounds = p1 - p0;
     long long acc = 0, n_last = 0;
@@ -781,8 +817,9 @@ int finish_frame(gb_ctx* ctx) {
     ctx->stats.closest_tri_tests = st[4];
     ctx->stats.shadow_node_visits = st[5];
     ctx->stats.shadow_tri_tests = st[6];
-    // every slot-pool iteration (counted by k_step in st[7]) is 5 launches
-    ctx->stats.kernel_launches = ctx->launches + 5 * st[7];
+    // every slot-pool iteration (counted by k_step in st[7]) is 5 launches,
+    // 6 with the adjoint sweep
+    ctx->stats.kernel_launches = ctx->launches + (ctx->mode == MODE_ADJOINT ? 6 : 5) * st[7];
     ctx->stats.paths_done = ctx->paths_done;
     for (int k = 0; k < 6; ++k) { ctx->stats.stage_ms[k] = 0.0; ctx->stats.stage_launches[k] = 0; }
     for (size_t i = 0; i < ctx->ev_used; ++i) {
@@ -868,6 +905,261 @@ int gb_render_batch(gb_ctx* ctx, int n, const gb_batch_item* items, int out_is_d
         rc = copy_scene(ctx, ctx->items[i], ctx->items[i].out, out_is_device);
     if (rc != GB_OK) return rc;
     return finish_frame(ctx);
+}
+
+namespace {
+
+int param_count(const gb_scene* s) {
+    return kMatParams * (int)s->mats.size() + kLightParams * (int)s->lights.size();
+}
+
+size_t grad_floats(const gb_scene* s) { return kMatGradFloats * s->mats.size() + 3 * s->lights.size(); }
+
+// Copies of the scene's descriptions with the parameter vector x applied
+// (base colour, roughness, metallic per material; emission per light).  A
+// principled parameter set shared by several materials takes the values of
+// the last of them.
+void apply_params(const gb_scene* s, const float* x, std::vector<gb_material>* mats,
+                  std::vector<gb_principled_params>* params, std::vector<gb_light>* lights) {
+    *mats = s->mats;
+    *params = s->params;
+    *lights = s->lights;
+    for (size_t m = 0; m < mats->size(); ++m) {
+        const float* v = x + kMatParams * m;
+        gb_material& mt = (*mats)[m];
+        if (mt.principled >= 0) {
+            gb_principled_params& p = (*params)[mt.principled];
+            for (int c = 0; c < 3; ++c) p.color[c] = v[c];
+            p.roughness = v[3];
+            p.metallic = v[4];
+        } else {
+            for (int c = 0; c < 3; ++c) mt.diffuse[c] = v[c];
+        }
+    }
+    const float* lx = x + kMatParams * mats->size();
+    for (size_t l = 0; l < lights->size(); ++l)
+        for (int c = 0; c < 3; ++c) (*lights)[l].col[c] = lx[kLightParams * l + c];
+}
+
+void build_records(const std::vector<gb_material>& mats, const std::vector<gb_principled_params>& params,
+                   const std::vector<gb_light>& lights, std::vector<float>* mrec, std::vector<LightRec>* lrec) {
+    mrec->assign(mats.size() * kMaterialFloats, 0.0f);
+    for (size_t m = 0; m < mats.size(); ++m)
+        pack_material(make_material(mats[m], params.empty() ? nullptr : params.data()), &(*mrec)[m * kMaterialFloats]);
+    lrec->clear();
+    for (const gb_light& l : lights) lrec->push_back(make_light(l));
+}
+
+bool all_finite(const float* x, int n) {
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(x[i])) return false;
+    return true;
+}
+
+cudaError_t ensure_buf(gb_ctx* ctx, void** p, size_t* cap, size_t bytes) {
+    if (bytes <= *cap) return cudaSuccess;
+    cudaStreamSynchronize(ctx->stream);
+    if (*p) {
+        auto it = std::find(ctx->adj_allocs.begin(), ctx->adj_allocs.end(), *p);
+        if (it != ctx->adj_allocs.end()) ctx->adj_allocs.erase(it);
+        cudaFree(*p);
+    }
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = dalloc(ctx->adj_allocs, p, bytes);
+    if (e == cudaSuccess) *cap = bytes;
+    return e;
+}
+
+}  // namespace
+
+int gb_scene_param_count(const gb_scene* scene, int* n) {
+    if (!scene || !n) return GB_ERR_INVALID;
+    *n = param_count(scene);
+    return GB_OK;
+}
+
+int gb_scene_get_params(const gb_scene* scene, float* x) {
+    if (!scene || !x) return GB_ERR_INVALID;
+    for (size_t m = 0; m < scene->mats.size(); ++m) {
+        float* v = x + kMatParams * m;
+        const gb_material& mt = scene->mats[m];
+        if (mt.principled >= 0) {
+            const gb_principled_params& p = scene->params[mt.principled];
+            for (int c = 0; c < 3; ++c) v[c] = p.color[c];
+            v[3] = p.roughness;
+            v[4] = p.metallic;
+        } else {
+            for (int c = 0; c < 3; ++c) v[c] = mt.diffuse[c];
+            v[3] = 0.0f;
+            v[4] = 0.0f;
+        }
+    }
+    float* lx = x + kMatParams * scene->mats.size();
+    for (size_t l = 0; l < scene->lights.size(); ++l)
+        for (int c = 0; c < 3; ++c) lx[kLightParams * l + c] = scene->lights[l].col[c];
+    return GB_OK;
+}
+
+int gb_scene_set_params(gb_scene* scene, const float* x) {
+    if (!scene || !x) return GB_ERR_INVALID;
+    gb_ctx* ctx = scene->ctx;
+    if (!all_finite(x, param_count(scene))) return fail(ctx, GB_ERR_INVALID, "non-finite parameter");
+    std::vector<gb_material> mats;
+    std::vector<gb_principled_params> params;
+    std::vector<gb_light> lights;
+    apply_params(scene, x, &mats, &params, &lights);
+    std::vector<float> mrec;
+    std::vector<LightRec> lrec;
+    build_records(mats, params, lights, &mrec, &lrec);
+    for (const LightRec& l : lrec)
+        if (!(l.power > 0.0f)) return fail(ctx, GB_ERR_INVALID, "light power must be positive");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));  // kernels in flight read the records
+    CK(cudaMemcpy((void*)scene->S.mats, mrec.data(), sizeof(float) * mrec.size(), cudaMemcpyHostToDevice));
+    if (!lrec.empty())
+        CK(cudaMemcpy((void*)scene->S.lights, lrec.data(), sizeof(LightRec) * lrec.size(), cudaMemcpyHostToDevice));
+    scene->mats.swap(mats);
+    scene->params.swap(params);
+    scene->lights.swap(lights);
+    scene->S.overall_power = overall_power(lrec.data(), (int)lrec.size());
+    scene->info.overall_light_power = scene->S.overall_power;
+    return GB_OK;
+}
+
+int gb_forward(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+               const float* eval_params, float* out_rgb, int out_is_device) {
+    if (!eval_params) return gb_render(ctx, scene, cam, desc, out_rgb, out_is_device);
+    if (!ctx || !scene || !cam || !desc) return fail(ctx, GB_ERR_INVALID, "null argument");
+    if (scene->ctx != ctx) return fail(ctx, GB_ERR_INVALID, "scene belongs to another context");
+    if (!all_finite(eval_params, param_count(scene))) return fail(ctx, GB_ERR_INVALID, "non-finite parameter");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<gb_material> mats;
+    std::vector<gb_principled_params> params;
+    std::vector<gb_light> lights;
+    apply_params(scene, eval_params, &mats, &params, &lights);
+    std::vector<float> mrec;
+    std::vector<LightRec> lrec;
+    build_records(mats, params, lights, &mrec, &lrec);
+    CK(ensure_buf(ctx, (void**)&ctx->d_eval_mats, &ctx->eval_mats_cap, sizeof(float) * mrec.size()));
+    CK(ensure_buf(ctx, (void**)&ctx->d_eval_lights, &ctx->eval_lights_cap,
+                  sizeof(LightRec) * std::max<size_t>(1, lrec.size())));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(ctx->d_eval_mats, mrec.data(), sizeof(float) * mrec.size(), cudaMemcpyHostToDevice));
+    if (!lrec.empty())
+        CK(cudaMemcpy(ctx->d_eval_lights, lrec.data(), sizeof(LightRec) * lrec.size(), cudaMemcpyHostToDevice));
+    std::vector<BatchScene> items(1);
+    items[0].scene = scene;
+    items[0].cam = *cam;
+    items[0].desc = *desc;
+    items[0].mats_eval = ctx->d_eval_mats;
+    items[0].lights_eval = ctx->d_eval_lights;
+    int rc = begin_frame(ctx, items);
+    if (rc == GB_OK) {
+        cudaError_t e = ensure_buf(ctx, (void**)&ctx->F.tp0, &ctx->tp0_cap, sizeof(float4) * ctx->slot_cap);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "replay buffers");
+    }
+    ctx->mode = MODE_FROZEN;
+    if (rc == GB_OK) rc = step_frame(ctx, ctx->max_spp);
+    ctx->mode = MODE_FORWARD;
+    if (rc == GB_OK) rc = pack_frame(ctx);
+    if (rc == GB_OK) rc = copy_scene(ctx, ctx->items[0], out_rgb, out_is_device);
+    if (rc == GB_OK) rc = finish_frame(ctx);
+    ctx->active = false;  // the frame's records are the context's scratch
+    return rc;
+}
+
+int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg_is_device, int graph_capture) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (n <= 0 || !items) return fail(ctx, GB_ERR_INVALID, "empty batch");
+    std::vector<BatchScene> v((size_t)n);
+    std::vector<uint32_t> gbase((size_t)n);
+    uint32_t gtot = 0;
+    for (int i = 0; i < n; ++i) {
+        if (!items[i].scene || !items[i].dL_dimg || !items[i].dL_dparams)
+            return fail(ctx, GB_ERR_INVALID, "null scene, image gradient or parameter gradient");
+        if (items[i].desc.max_bounces > kMaxAdjBounces)
+            return fail(ctx, GB_ERR_INVALID, "the adjoint records at most 16 bounces per path");
+        v[i].scene = items[i].scene;
+        v[i].cam = items[i].camera;
+        v[i].desc = items[i].desc;
+        v[i].dimg = items[i].dL_dimg;
+        v[i].grad_out = items[i].dL_dparams;
+        v[i].grad_base = gtot;
+        gtot += (uint32_t)grad_floats(items[i].scene);
+    }
+    CK(cudaSetDevice(ctx->device));
+    int rc = begin_frame(ctx, v);
+    if (rc != GB_OK) return rc;
+    Frame& F = ctx->F;
+    const int replicas = k_adjoint_grid();
+    const int stride = (int)std::max<uint32_t>(1, gtot);
+    cudaError_t e = ensure_buf(ctx, (void**)&F.adj, &ctx->adj_cap,
+                               sizeof(float4) * kAdjPlanes * (size_t)ctx->max_L * ctx->slot_cap);
+    if (e == cudaSuccess) e = ensure_buf(ctx, (void**)&F.dimg, &ctx->dimg_cap, sizeof(float4) * (size_t)F.ntot);
+    if (e == cudaSuccess)
+        e = ensure_buf(ctx, (void**)&F.grad, &ctx->grad_cap, sizeof(float) * (size_t)replicas * (size_t)stride);
+    if (e == cudaSuccess) e = ensure_buf(ctx, (void**)&ctx->d_gsum, &ctx->gsum_cap, sizeof(double) * (size_t)stride);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "adjoint buffers");
+    F.grad_stride = stride;
+    F.grad_replicas = replicas;
+    for (const BatchScene& b : ctx->items) {
+        const float* src = b.dimg;
+        if (!dimg_is_device) {
+            CK(ensure_scratch(ctx, 0, sizeof(float) * 3 * (size_t)b.n));
+            CK(cudaMemcpyAsync(ctx->scratch[0].p, b.dimg, sizeof(float) * 3 * (size_t)b.n, cudaMemcpyHostToDevice,
+                               ctx->stream));
+            src = (const float*)ctx->scratch[0].p;
+        }
+        CK(k_launch_dimg_pack(src, b.n, 1.0f / (float)b.desc.spp, F.dimg + b.base, ctx->stream));
+        ctx->launches += 1;
+    }
+    CK(cudaMemsetAsync(F.grad, 0, sizeof(float) * (size_t)replicas * (size_t)stride, ctx->stream));
+    const bool saved = ctx->use_graph;
+    if (graph_capture >= 0) ctx->use_graph = graph_capture != 0;
+    ctx->mode = MODE_ADJOINT;
+    rc = step_frame(ctx, ctx->max_spp);
+    ctx->use_graph = saved;
+    std::vector<double> gsum((size_t)stride);
+    if (rc == GB_OK) {
+        cudaError_t e2 = k_launch_grad_reduce(F.grad, replicas, stride, ctx->d_gsum, ctx->stream);
+        if (e2 == cudaSuccess) e2 = cudaMemcpyAsync(gsum.data(), ctx->d_gsum, sizeof(double) * (size_t)stride,
+                                                    cudaMemcpyDeviceToHost, ctx->stream);
+        if (e2 != cudaSuccess) rc = cuda_fail(ctx, e2, "gradient reduction");
+        ctx->launches += 1;
+    }
+    if (rc == GB_OK) rc = finish_frame(ctx);
+    ctx->mode = MODE_FORWARD;
+    ctx->active = false;
+    if (rc != GB_OK) return rc;
+    // record-field gradients to parameter gradients (host, double)
+    for (const BatchScene& b : ctx->items) {
+        const gb_scene* sc = b.scene;
+        const double* gm = gsum.data() + b.grad_base;
+        for (size_t m = 0; m < sc->mats.size(); ++m) {
+            double out[kMatParams];
+            material_param_vjp(sc->mats[m], sc->params.empty() ? nullptr : sc->params.data(),
+                               gm + kMatGradFloats * m, out);
+            for (int k = 0; k < kMatParams; ++k) b.grad_out[kMatParams * m + k] = (float)out[k];
+        }
+        const double* gl = gm + kMatGradFloats * sc->mats.size();
+        float* lo = b.grad_out + kMatParams * sc->mats.size();
+        for (size_t l = 0; l < sc->lights.size(); ++l)
+            for (int c = 0; c < 3; ++c) lo[kLightParams * l + c] = (float)gl[3 * l + c];
+    }
+    return GB_OK;
+}
+
+int gb_backward(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+                const float* dL_dimg, int dimg_is_device, float* dL_dparams) {
+    if (!ctx || !scene || !cam || !desc) return fail(ctx, GB_ERR_INVALID, "null argument");
+    gb_adjoint_item it;
+    it.scene = scene;
+    it.camera = *cam;
+    it.desc = *desc;
+    it.dL_dimg = dL_dimg;
+    it.dL_dparams = dL_dparams;
+    return gb_backward_batch(ctx, 1, &it, dimg_is_device, -1);
 }
 
 namespace {

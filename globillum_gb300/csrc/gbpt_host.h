@@ -56,6 +56,55 @@ static inline MaterialRec make_material(const gb_material& m, const gb_principle
     return r;
 }
 
+// Differentiable parameters of a material: base colour (3), roughness,
+// metallic; of a light: emission (3).
+static const int kMatParams = 5;
+static const int kLightParams = 3;
+
+// Chain rule from the record-field gradient of a material (MatGrad order,
+// kMatGradFloats doubles) to its parameters (kMatParams doubles), following
+// make_material: cdlin = color^2.2, Ctint = cdlin / lum(cdlin), csheen =
+// mix(1, Ctint, sheenTint), cspec0 = mix(0.08 specular mix(1, Ctint,
+// specularTint), cdlin, metallic).  Lambert materials take the colour
+// gradient from `diffuse`; their roughness and metallic entries are 0.
+static inline void material_param_vjp(const gb_material& mat, const gb_principled_params* params,
+                                      const double* gr, double* out) {
+    for (int k = 0; k < kMatParams; ++k) out[k] = 0.0;
+    if (mat.principled < 0) {
+        for (int c = 0; c < 3; ++c) out[c] = gr[11 + c];
+        return;
+    }
+    const gb_principled_params& p = params[mat.principled];
+    double cd[3], dcd[3];
+    for (int c = 0; c < 3; ++c) {
+        cd[c] = std::pow((double)p.color[c], 2.2);
+        dcd[c] = p.color[c] > 0.0f ? 2.2 * std::pow((double)p.color[c], 1.2) : 0.0;
+    }
+    const double w[3] = {.3, .6, .1};
+    const double lum = w[0] * cd[0] + w[1] * cd[1] + w[2] * cd[2];
+    const double met = p.metallic, st = p.specular_tint, sh = p.sheen_tint, spec08 = (double)p.specular * .08;
+    // gradient with respect to cdlin[i]
+    double gcd[3];
+    for (int i = 0; i < 3; ++i) gcd[i] = gr[0 + i] + met * gr[6 + i];
+    if (lum > 0.0) {
+        for (int k = 0; k < 3; ++k) {
+            double gt = sh * gr[3 + k] + (1.0 - met) * spec08 * st * gr[6 + k];  // gradient of Ctint[k]
+            for (int i = 0; i < 3; ++i) {
+                double dct = ((k == i ? lum : 0.0) - cd[k] * w[i]) / (lum * lum);
+                gcd[i] += gt * dct;
+            }
+        }
+    }
+    for (int c = 0; c < 3; ++c) out[c] = gcd[c] * dcd[c];
+    out[3] = gr[10];
+    double gm = gr[9];
+    for (int k = 0; k < 3; ++k) {
+        double ctint = lum > 0.0 ? cd[k] / lum : 1.0;
+        gm += gr[6 + k] * (cd[k] - spec08 * ((1.0 - st) + st * ctint));
+    }
+    out[4] = gm;
+}
+
 // Flattened device record (kMaterialFloats floats).
 static inline void pack_material(const MaterialRec& r, float* f) {
     std::memset(f, 0, sizeof(float) * kMaterialFloats);
@@ -103,6 +152,38 @@ static inline CameraRec make_camera(const gb_camera& c, int w, int h) {
     r.focus = c.focus_distance;
     r.w = w; r.h = h;
     return r;
+}
+
+// A1^k and A2^k of the MRG32k3a recurrence (mrg_jump): square-and-multiply
+// of 3x3 matrices mod m.
+static inline void mrg_matmul(const uint32_t* A, const uint32_t* B, uint32_t* C, uint32_t c, uint32_t m) {
+    uint32_t r[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            uint64_t acc = 0;
+            for (int k = 0; k < 3; ++k) acc += mrg_reduce((uint64_t)A[3 * i + k] * B[3 * k + j], c, m);
+            r[3 * i + j] = mrg_reduce(acc, c, m);
+        }
+    std::memcpy(C, r, sizeof(r));
+}
+
+static inline void mrg_power(const uint32_t* A, uint64_t k, uint32_t* out, uint32_t c, uint32_t m) {
+    uint32_t base[9], acc[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    std::memcpy(base, A, sizeof(base));
+    while (k) {
+        if (k & 1) mrg_matmul(acc, base, acc, c, m);
+        mrg_matmul(base, base, base, c, m);
+        k >>= 1;
+    }
+    std::memcpy(out, acc, sizeof(acc));
+}
+
+// Jump matrices for `steps` MRG32k3a steps.
+static inline void mrg_jump_matrices(uint64_t steps, uint32_t J1[9], uint32_t J2[9]) {
+    const uint32_t A1[9] = {0, 1, 0, 0, 0, 1, kMrgM1 - 810728u, 1403580u, 0};
+    const uint32_t A2[9] = {0, 1, 0, 0, 0, 1, kMrgM2 - 1370589u, 0, 527612u};
+    mrg_power(A1, steps, J1, 209u, kMrgM1);
+    mrg_power(A2, steps, J2, 22853u, kMrgM2);
 }
 
 static inline ShadeParams make_shade_params(const gb_render_desc& d) {

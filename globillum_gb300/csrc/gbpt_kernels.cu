@@ -365,8 +365,9 @@ __global__ void k_fill_pscene(Frame F) {
 //                    jitter pool (k_jitter_pool walks each pixel's stream)
 //   lens sample    = update p of pixel (pixel+17)%n (raygen.cu:100-106)
 //   light/path     = updates pL, pL+1, ... one per bounce (hybrid-pt.h:229-233),
-//                    handed out by a per-pixel stream cursor that advances by
-//                    L updates whenever a path of the pixel starts.
+//                    handed out by a per-pixel stream cursor that jumps by
+//                    L updates (3L generator steps, mrg_jump) whenever a path
+//                    of the pixel starts.
 // A launch starts paths from a contiguous range of at most nslots <= min_r
 // N_r paths, so it starts at most one path per pixel and never shares a
 // cursor; paths of a pixel start in sample order.
@@ -406,13 +407,14 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
     curandStateMRG32k3a* cur = (curandStateMRG32k3a*)F.cursor;
     curandStateMRG32k3a bs = cur[gpix];
     ((curandStateMRG32k3a*)F.rng)[slot] = bs;
-    for (int u = 0; u < R.L; ++u) (void)draw3(&bs);
+    mrg_jump(bs.s1, bs.s2, R.jump1, R.jump2);  // = L draw3 calls
     cur[gpix] = bs;
     v3 o, d;
     camera_ray(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w), j.x, j.y, lx, ly, &o, &d);
     F.ray_o[slot] = make_float4(o.x, o.y, o.z, FLT_MAX);
     F.ray_d[slot] = make_float4(d.x, d.y, d.z, 0.0f);
     F.tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    if (P.mode == MODE_FROZEN) F.tp0[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     F.accum[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     F.pix[slot] = gpix;
     F.ps[slot] = sc;
@@ -646,16 +648,16 @@ __global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
                     lr = mk(halton(pid, 2), hy, hy);
                 }
                 v3 so = mk(0.0f, 0.0f, 0.0f), sd = mk(0.0f, 0.0f, 0.0f), psc = mk(0.0f, 0.0f, 0.0f);
-                float smax = -1.0f;
+                float smax = -1.0f, scale = 0.0f;
                 if (S.n_lights > 0) {
                     int l = pick_light(S.lights, S.n_lights, S.overall_power, lr.z);
                     LightRec L = S.lights[l];
-                    rect_light_sample(L, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset, &so, &sd, &smax,
-                                      &psc);
+                    rect_light_sample(L, S.lights_eval[l].col, S.overall_power, Pp, Nr, lr.x, lr.y,
+                                      R.sp.shadow_offset, &so, &sd, &smax, &psc, &scale);
                 }
                 F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
                 F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-                F.psc[slot] = make_float4(psc.x, psc.y, psc.z, 0.0f);
+                F.psc[slot] = make_float4(psc.x, psc.y, psc.z, scale);
                 F.rnd[slot] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
                 F.hit_p[slot] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
                 F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, 0.0f);
@@ -698,9 +700,33 @@ __global__ void __launch_bounds__(kBlock) k_shadow(Frame F, RenderParams P) {
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
 }
 
+__device__ __forceinline__ MaterialRec load_material(const float* mats, uint32_t mi) {
+    float mf[kMaterialFloats];
+    const float4* mp = (const float4*)(mats + (size_t)kMaterialFloats * mi);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        float4 q = __ldg(mp + k);
+        mf[4 * k] = q.x; mf[4 * k + 1] = q.y; mf[4 * k + 2] = q.z; mf[4 * k + 3] = q.w;
+    }
+    return unpack_material(mf);
+}
+
+// Light the NEE of a hit picked (arealight-sampler-cpu.cpp:32-39 on the
+// light draw of k_extend).
+__device__ __forceinline__ int nee_light(const Frame& F, const SceneRec& R, uint32_t slot, v3 rnd) {
+    if (R.S.n_lights <= 0) return 0;
+    float lz = rnd.z;
+    if (R.rng_mode == 1) lz = halton((int)(F.pix[slot] - R.pixel_base) + 1, 3);
+    return pick_light(R.S.lights, R.S.n_lights, R.S.overall_power, lz);
+}
+
 // BRDF sample/eval, NEE accumulation and next ray for every shadow-queue
 // entry (compute_path_contribution_and_bounce for the hits); paths that end
-// go to the free queue.
+// go to the free queue.  MODE_FROZEN evaluates the BRDF with the scene's
+// eval records and carries the sampling throughput in tp0; MODE_ADJOINT
+// writes the vertex record of the path-replay adjoint.  Every path leaves
+// with pb's bounce field = the number of vertices it shaded.
+template <int MODE>
 __global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
@@ -720,35 +746,130 @@ __global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
             float4 sd = F.sh_d[slot];
             float4 hp = F.hit_p[slot], hn = F.hit_n[slot];
             uint32_t mi = __float_as_uint(hp.w);
-            float mf[kMaterialFloats];
-            const float4* mp = (const float4*)(R.S.mats + (size_t)kMaterialFloats * mi);
-#pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                float4 q = __ldg(mp + k);
-                mf[4 * k] = q.x; mf[4 * k + 1] = q.y; mf[4 * k + 2] = q.z; mf[4 * k + 3] = q.w;
-            }
-            MaterialRec m = unpack_material(mf);
+            MaterialRec m = load_material(R.S.mats, mi);
             uint32_t pbv = F.pb[slot];
             int bounce = (int)(pbv & 1023u);
             uint32_t path = pbv >> 10;
             float4 rd = F.ray_d[slot], tp4 = F.tp[slot], rn = F.rnd[slot], ps = F.psc[slot];
             float4 acc = F.accum[slot];
-            ShadeOut o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps),
-                                   R.sp, F.pix[slot] - R.pixel_base, path, bounce);
+            ShadeOut o;
+            if (MODE == MODE_FROZEN) {
+                MaterialRec me = load_material(R.S.mats_eval, mi);
+                v3 t0 = ld3(F.tp0[slot]);
+                o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps), R.sp,
+                              F.pix[slot] - R.pixel_base, path, bounce, &me, &t0);
+                F.tp0[slot] = make_float4(t0.x, t0.y, t0.z, 0.0f);
+            } else if (MODE == MODE_ADJOINT) {
+                ShadeTrace tr;
+                o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps), R.sp,
+                              F.pix[slot] - R.pixel_base, path, bounce, nullptr, nullptr, &tr);
+                int light = nee_light(F, R, slot, ld3(rn));
+                uint32_t info = (uint32_t)light | ((uint32_t)tr.lobe << 16) | (tr.clamp_mask << 20) |
+                                (tr.nee ? (1u << 23) : 0u);
+                float4* rec = F.adj + (size_t)bounce * kAdjPlanes * F.nslots + slot;
+                rec[0] = make_float4(tp4.x, tp4.y, tp4.z, tr.pdf);
+                rec[(size_t)F.nslots] = make_float4(tr.wo.x, tr.wo.y, tr.wo.z, tr.q);
+                rec[2 * (size_t)F.nslots] = make_float4(tr.wi.x, tr.wi.y, tr.wi.z, tr.nee ? ps.w : 0.0f);
+                rec[3 * (size_t)F.nslots] = make_float4(tr.N.x, tr.N.y, tr.N.z, __uint_as_float(mi));
+                rec[4 * (size_t)F.nslots] = make_float4(tr.ld.x, tr.ld.y, tr.ld.z, __uint_as_float(info));
+            } else {
+                o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps), R.sp,
+                              F.pix[slot] - R.pixel_base, path, bounce);
+            }
             acc = make_float4(acc.x + o.accum_add.x, acc.y + o.accum_add.y, acc.z + o.accum_add.z, 0.0f);
             cont = o.alive && bounce + 1 < R.L;
             ended = !cont;
             F.accum[slot] = acc;
+            F.pb[slot] = pbv + 1u;
             if (cont) {
                 F.tp[slot] = make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f);
                 F.ray_o[slot] = make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX);
                 F.ray_d[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, 0.0f);
-                F.pb[slot] = pbv + 1u;
             }
         }
         push(cont, slot, qout, cn);
         end_paths(F, ended, slot, cn);
     }
+}
+
+// Path-replay adjoint of every path that ended this iteration (free queue,
+// before k_regen reuses the slots).  The path's value is
+//   C = sum_k T_k * bl_k * col_l(k) * s_k,  T_{k+1} = clamp1(T_k * brdf_k / pdf_k) / q_k
+// with pdf, q, the clamp pattern and all directions held at their recorded
+// values; the reverse sweep k = K-1 .. 0 carries a = dLoss/dT_{k+1} and adds
+// the BRDF vector-Jacobian products and the emission gradient to this
+// block's gradient replica.  g = dLoss/dI(pixel) / spp.
+__global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
+    const int it = *F.iter;
+    uint32_t* cn = ctr_set(F, it + 1);
+    const uint32_t count = cn[4];
+    float* grad = F.grad + (size_t)(blockIdx.x % (uint32_t)F.grad_replicas) * (size_t)F.grad_stride;
+    const size_t ns = (size_t)F.nslots;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = F.q[3][i];
+        const int K = (int)(F.pb[slot] & 1023u);
+        const float4 g4 = F.dimg[F.pix[slot]];
+        if (K == 0 || (g4.x == 0.0f && g4.y == 0.0f && g4.z == 0.0f)) continue;
+        const SceneRec& R = F.scenes[F.ps[slot]];
+        const v3 g = ld3(g4);
+        float* gm_base = grad + R.grad_base;
+        float* gl_base = gm_base + (size_t)kMatGradFloats * (size_t)R.n_mats;
+        v3 an = mk(0.0f, 0.0f, 0.0f);  // dLoss / dT_{k+1}
+        for (int k = K - 1; k >= 0; --k) {
+            const float4* rec = F.adj + (size_t)k * kAdjPlanes * ns + slot;
+            const float4 r0 = rec[0], r1 = rec[ns], r2 = rec[2 * ns], r3 = rec[3 * ns], r4 = rec[4 * ns];
+            const v3 T = ld3(r0), wo = ld3(r1), wi = ld3(r2), N = ld3(r3), ld = ld3(r4);
+            const float pdf = r0.w, q = r1.w, sc = r2.w;
+            const uint32_t mi = __float_as_uint(r3.w), info = __float_as_uint(r4.w);
+            const int light = (int)(info & 0xffffu), lobe = (int)((info >> 16) & 15u);
+            const uint32_t cmask = (info >> 20) & 7u;
+            const bool nee = (info >> 23) & 1u;
+            const MaterialRec m = load_material(R.S.mats, mi);
+            MatGrad mg;
+            matgrad_zero(&mg);
+            v3 ak = mk(0.0f, 0.0f, 0.0f);
+            if (an.x != 0.0f || an.y != 0.0f || an.z != 0.0f) {
+                const v3 brdf = material_eval(m, lobe, wo, wi, N);
+                const float inv = 1.0f / (pdf * q);
+                const v3 c = mk((cmask & 1u) ? 0.0f : 1.0f, (cmask & 2u) ? 0.0f : 1.0f, (cmask & 4u) ? 0.0f : 1.0f);
+                material_eval_vjp(m, lobe, wo, wi, N, (c * T * an) * inv, &mg);
+                ak = (c * brdf * an) * inv;
+            }
+            if (nee) {
+                const v3 col = R.S.lights[light].col;
+                const v3 psc = col * sc;
+                const v3 bl = material_eval(m, lobe, wo, ld, N);
+                material_eval_vjp(m, lobe, wo, ld, N, g * T * psc, &mg);
+                const v3 acol = (g * T * bl) * sc;
+                float* gl = gl_base + 3 * light;
+                if (acol.x != 0.0f) atomicAdd(gl + 0, acol.x);
+                if (acol.y != 0.0f) atomicAdd(gl + 1, acol.y);
+                if (acol.z != 0.0f) atomicAdd(gl + 2, acol.z);
+                ak = ak + g * bl * psc;
+            }
+            float* gmat = gm_base + (size_t)kMatGradFloats * mi;
+            const float* mv = &mg.cdlin[0];
+#pragma unroll
+            for (int f = 0; f < kMatGradFloats; ++f)
+                if (mv[f] != 0.0f) atomicAdd(gmat + f, mv[f]);
+            an = ak;
+        }
+    }
+}
+
+__global__ void k_dimg_pack(const float* __restrict__ src, int n, float scale, float4* dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dst[i] = make_float4(src[3 * i] * scale, src[3 * i + 1] * scale, src[3 * i + 2] * scale, 0.0f);
+}
+
+// Sum of the gradient replicas, in double.
+__global__ void k_grad_reduce(const float* __restrict__ grad, int replicas, int stride, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= stride) return;
+    double acc = 0.0;
+    for (int r = 0; r < replicas; ++r) acc += (double)grad[(size_t)r * (size_t)stride + (size_t)i];
+    out[i] = acc;
 }
 
 // new_path's moving average (util-kernels.cu:17-25) over the chunk's paths
@@ -803,7 +924,8 @@ __global__ void k_nee_stage(DevScene S, int n, float shadow_offset, const float*
         v3 Pp = bary(h.y, h.z, ld3(sh[0]), ld3(sh[1]), ld3(sh[2]));
         v3 Nr = bary(h.y, h.z, ld3(sh[3]), ld3(sh[4]), ld3(sh[5]));
         v3 so, sd, ps; float sm;
-        rect_light_sample(S.lights[l], S.overall_power, Pp, Nr, r.x, r.y, shadow_offset, &so, &sd, &sm, &ps);
+        rect_light_sample(S.lights[l], S.lights[l].col, S.overall_power, Pp, Nr, r.x, r.y, shadow_offset, &so, &sd,
+                          &sm, &ps);
         ray_orig[3 * i] = so.x; ray_orig[3 * i + 1] = so.y; ray_orig[3 * i + 2] = so.z;
         ray_dir[3 * i] = sd.x; ray_dir[3 * i + 1] = sd.y; ray_dir[3 * i + 2] = sd.z;
         max_t[i] = sm;
@@ -949,9 +1071,38 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
     return cudaGetLastError();
 }
 
+template <int MODE>
+void launch_shade_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    static int g = persistent_blocks(k_shade<MODE>);
+    k_shade<MODE><<<g, kBlock, 0, st>>>(F, P);
+}
+
 cudaError_t k_launch_shade(const Frame& F, const RenderParams& P, cudaStream_t st) {
-    static int g0 = persistent_blocks(k_shade);
-    k_shade<<<g0, kBlock, 0, st>>>(F, P);
+    if (P.mode == MODE_FROZEN) launch_shade_t<MODE_FROZEN>(F, P, st);
+    else if (P.mode == MODE_ADJOINT) launch_shade_t<MODE_ADJOINT>(F, P, st);
+    else launch_shade_t<MODE_FORWARD>(F, P, st);
+    return cudaGetLastError();
+}
+
+int k_adjoint_grid() {
+    static int g = persistent_blocks(k_adjoint);
+    return g;
+}
+
+cudaError_t k_launch_adjoint(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    k_adjoint<<<k_adjoint_grid(), kBlock, 0, st>>>(F, P);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_dimg_pack<<<blocks_for(n), kBlock, 0, st>>>(src, n, scale, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, double* out, cudaStream_t st) {
+    if (stride <= 0) return cudaSuccess;
+    k_grad_reduce<<<blocks_for(stride), kBlock, 0, st>>>(grad, replicas, stride, out);
     return cudaGetLastError();
 }
 

@@ -19,6 +19,11 @@ struct DevScene {
     int n_lights;
     float overall_power;
     int n_nodes, n_tris;
+    // records the BRDF values and light emission are evaluated with: the same
+    // as mats / lights, except in a frozen-sampling replay (directions,
+    // lobes, pdfs and light picks still come from mats / lights)
+    const float* mats_eval;
+    const LightRec* lights_eval;
 };
 
 // Status bits written by the kernels (never a trap).
@@ -34,7 +39,15 @@ struct SceneRec {
     int spp, L, rng_mode;
     uint32_t pixel_base;  // first global pixel of the scene
     uint32_t seed;
+    uint32_t jump1[9], jump2[9];  // MRG32k3a jump by the 3 L draws of one path
+    int n_mats;
+    uint32_t grad_base;   // first record-gradient float of the scene (adjoint)
 };
+
+// Render modes of a chunk.
+enum { MODE_FORWARD = 0, MODE_FROZEN = 1, MODE_ADJOINT = 2 };
+constexpr int kAdjPlanes = 5;        // float4 planes of one adjoint vertex record
+constexpr int kMaxAdjBounces = 16;   // bounces the adjoint records per path
 
 constexpr int kMaxRounds = 64;  // path samples per chunk
 
@@ -74,6 +87,15 @@ struct Frame {
     int* iter;         // iteration index of the chunk's slot-pool loop
     unsigned long long* stats;  // 0 camera, 1 ext, 2 shadow rays; 3/4 closest, 5/6 shadow node visits / tri tests
     uint32_t* status;
+    // frozen-sampling replay: throughput of the path under the sampling records
+    float4* tp0;
+    // adjoint: vertex records [bounce][plane][slot], per-pixel loss gradient
+    // (already divided by spp), per-block gradient replicas of the record fields
+    float4* adj;
+    float4* dimg;
+    float* grad;
+    int grad_stride;   // floats per replica
+    int grad_replicas;
 };
 
 // Launch-wide parameters of one chunk.
@@ -81,6 +103,7 @@ struct RenderParams {
     int refill;        // refill a warp's lanes once this many are idle (1..32)
     int tri_mode;      // 0: all pending triangles then a node; 1/2: triangle postponing, one / all triangles
     int blocks_per_sm; // resident blocks per SM of the traversal kernels (0 = occupancy limit)
+    int mode;          // MODE_*
     int p0, rounds;    // path samples p0 .. p0+rounds-1
     uint32_t chunk_paths;  // paths of the chunk
     uint32_t round_start[kMaxRounds + 1];  // first path index of each round (prefix sums of N_p)
@@ -98,6 +121,10 @@ cudaError_t k_launch_step(const Frame& F, unsigned long long cond, bool has_cond
 cudaError_t k_launch_jitter_pool(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_combine(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t st);
+cudaError_t k_launch_adjoint(const Frame& F, const RenderParams& P, cudaStream_t st);
+int k_adjoint_grid();
+cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st);
+cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, double* out, cudaStream_t st);
 cudaError_t k_launch_mrg_pool(int npix, uint32_t seed, int first_update, int num_updates, float* out,
                               cudaStream_t st);
 cudaError_t k_launch_nee_stage(const DevScene& S, int n, float shadow_offset, const float* rnd, const float4* hits,

@@ -186,6 +186,43 @@ GB_HD float rr_uniform(uint32_t seed, uint32_t pixel, uint32_t path, uint32_t bo
     return float(h >> 8) * (1.0f / 16777216.0f);
 }
 
+// MRG32k3a jump-ahead (L'Ecuyer 1999, "Good parameters and implementations
+// for combined multiple recursive random number generators"; jumps by matrix
+// powers as in L'Ecuyer, Simard, Chen and Kelton 2002, "An object-oriented
+// random-number package with many long streams and substreams").  The two
+// component states are kept oldest value first, (x[n-3], x[n-2], x[n-1]);
+// one step maps them with
+//   A1 = [[0, 1, 0], [0, 0, 1], [-810728, 1403580, 0]]   mod m1 = 2^32 - 209
+//   A2 = [[0, 1, 0], [0, 0, 1], [-1370589, 0, 527612]]   mod m2 = 2^32 - 22853
+// and k steps with A1^k, A2^k (row-major, entries reduced mod m).
+constexpr uint32_t kMrgM1 = 4294967087u;
+constexpr uint32_t kMrgM2 = 4294944443u;
+
+// x mod m for m = 2^32 - c (x < 2^64): 2^32 = c (mod m) folds the high word
+// into the low word twice, then at most two subtractions remain.
+GB_HD uint32_t mrg_reduce(uint64_t x, uint32_t c, uint32_t m) {
+    x = (x >> 32) * c + (x & 0xffffffffull);
+    x = (x >> 32) * c + (x & 0xffffffffull);
+    while (x >= m) x -= m;
+    return (uint32_t)x;
+}
+
+GB_HD void mrg_apply(uint32_t s[3], const uint32_t* J, uint32_t c, uint32_t m) {
+    uint32_t r[3];
+    for (int i = 0; i < 3; ++i) {
+        uint64_t acc = 0;
+        for (int j = 0; j < 3; ++j) acc += mrg_reduce((uint64_t)J[3 * i + j] * s[j], c, m);
+        r[i] = mrg_reduce(acc, c, m);  // acc < 3 m
+    }
+    s[0] = r[0]; s[1] = r[1]; s[2] = r[2];
+}
+
+// Advances a state (s1, s2) by the steps J1 = A1^k, J2 = A2^k stand for.
+GB_HD void mrg_jump(uint32_t s1[3], uint32_t s2[3], const uint32_t* J1, const uint32_t* J2) {
+    mrg_apply(s1, J1, 209u, kMrgM1);
+    mrg_apply(s2, J2, 22853u, kMrgM2);
+}
+
 // ----------------------------------------------------------------- camera --
 // Per-frame constants of setup_jittered_dof_shirley (raygen.cu:61-118); the
 // host fills them once (W, U, V are the same for every ray).
@@ -254,9 +291,11 @@ GB_HD int pick_light(const LightRec* L, int n, float overall_power, float rnd_z)
 
 // Rectangular-light sample at a hit (arealight-sampler-cpu.cpp:65-86, 114-119).
 // P, N: interpolated hit point and (unnormalised) normal.  Outputs the
-// shadow ray and potential_sample_contribution.
-GB_HD void rect_light_sample(const LightRec& l, float overall_power, v3 P, v3 N, float rx, float ry,
-                             float shadow_offset, v3* so, v3* sd, float* smax, v3* psc) {
+// shadow ray and potential_sample_contribution = col * scale, where col is
+// the light's emission (l.col, or the emission being differentiated) and
+// scale the geometry term over the light's pick probability.
+GB_HD void rect_light_sample(const LightRec& l, v3 col, float overall_power, v3 P, v3 N, float rx, float ry,
+                             float shadow_offset, v3* so, v3* sd, float* smax, v3* psc, float* scale = nullptr) {
     float offx = (rx - 0.5f) * l.w;
     float offy = (ry - 0.5f) * l.h;
     v3 ls = (l.center + offx * l.right) + offy * l.up;
@@ -266,12 +305,14 @@ GB_HD void rect_light_sample(const LightRec& l, float overall_power, v3 P, v3 N,
     float ndotl = fmaxf(dot(N, dir), 0.0f);
     float light_cos = fmaxf(dot(l.dir, -dir), 0.0f);
     float factor = l.w * l.h * ndotl * light_cos / (len * len);
-    v3 contribution = l.col * factor;
+    v3 contribution = col * factor;
     dir = normalize_div(dir);
     *so = P + shadow_offset * dir;
     *sd = dir;
     *smax = len;
-    *psc = contribution * (overall_power / l.power);
+    float inv_pick = overall_power / l.power;
+    *psc = contribution * inv_pick;
+    if (scale) *scale = factor * inv_pick;
 }
 
 // -------------------------------------------------------------- materials --
@@ -469,6 +510,103 @@ GB_HD v3 material_eval(const MaterialRec& m, int lobe, v3 wo, v3 wi, v3 N) {
     return principled_diffuse(m, wo, N, wi);
 }
 
+// ---------------------------------------------------------------- adjoint --
+// Gradient of the differentiable fields of a material record.  Sampling
+// quantities (ax, ay, roughg2, lobe choice) are held fixed by the
+// path-replay adjoint, so roughness enters through the diffuse lobe only.
+struct MatGrad {
+    float cdlin[3], csheen[3], cspec0[3];
+    float metallic, roughness;
+    float diffuse[3];
+};
+static const int kMatGradFloats = 14;  // cdlin[3], csheen[3], cspec0[3], metallic, roughness, diffuse[3]
+
+GB_HD void matgrad_zero(MatGrad* g) {
+    for (int c = 0; c < 3; ++c) { g->cdlin[c] = 0.0f; g->csheen[c] = 0.0f; g->cspec0[c] = 0.0f; g->diffuse[c] = 0.0f; }
+    g->metallic = 0.0f;
+    g->roughness = 0.0f;
+}
+GB_HD float v3c(v3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
+
+// a^T d(principled_diffuse)/d(cdlin, csheen, metallic, roughness), added to g.
+GB_HD void principled_diffuse_vjp(const MaterialRec& m, v3 V, v3 N, v3 L, v3 a, MatGrad* g) {
+    float NdotL = dot(N, L);
+    float NdotV = dot(N, V);
+    if (NdotL < 0.0f || NdotV < 0.0f) return;
+    v3 H = normalize_rcp(L + V);
+    float LdotH = dot(L, H);
+    float FL = schlick(NdotL), FV = schlick(NdotV);
+    float l2 = LdotH * LdotH;
+    float Fd90 = 0.5f + 2.0f * l2 * m.roughness;
+    float Ad = mixf(1.0f, Fd90, FL), Bd = mixf(1.0f, Fd90, FV);
+    float Fd = Ad * Bd;
+    float FH = schlick(LdotH);
+    float Fss90 = l2 * m.roughness;
+    float As = mixf(1.0f, Fss90, FL), Bs = mixf(1.0f, Fss90, FV);
+    float Fss = As * Bs;
+    float css = 1.25f * (1.0f / (NdotL + NdotV) - 0.5f);  // d ss / d Fss
+    float ss = css * Fss + 0.625f;
+    float k = kInvPi * mixf(Fd, ss, m.subsurface);
+    float om = 1.0f - m.metallic;
+    float fsh = FH * m.sheen;
+    v3 ad = a * NdotL;  // adjoint of dcol
+    float ak = 0.0f, am = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+        float adc = v3c(ad, c);
+        g->cdlin[c] += adc * k * om;
+        g->csheen[c] += adc * fsh * om;
+        ak += adc * m.cdlin[c] * om;
+        am -= adc * (k * m.cdlin[c] + fsh * m.csheen[c]);
+    }
+    g->metallic += am;
+    float dFd = (FL * Bd + Ad * FV) * 2.0f * l2;
+    float dss = css * (FL * Bs + As * FV) * l2;
+    g->roughness += ak * kInvPi * ((1.0f - m.subsurface) * dFd + m.subsurface * dss);
+}
+
+// a^T d(principled_specular)/d(cspec0, metallic), added to g.
+GB_HD void principled_specular_vjp(const MaterialRec& m, v3 V, v3 N, v3 L, v3 a, MatGrad* g) {
+    float NdotL = dot(N, L);
+    float NdotV = dot(N, V);
+    if (NdotL < 0.0f || NdotV < 0.0f) return;
+    v3 H = normalize_rcp(L + V);
+    float NdotH = dot(N, H);
+    float LdotH = dot(L, H);
+    float FH = schlick(LdotH);
+    float cg = 0.0f;
+    if (m.clearcoat > 0.0f) {
+        float Dr;
+        if (m.cc_a >= 1.0f) Dr = kInvPi;
+        else {
+            float t = 1.0f + m.cc_a2m1 * NdotH * NdotH;
+            Dr = m.cc_a2m1 / (m.cc_pilog * t);
+        }
+        float Fr = mixf(0.04f, 1.0f, FH);
+        float Gr = smithG_GGX(NdotL, 0.25f) * smithG_GGX(NdotV, 0.25f);
+        cg = 0.25f * m.clearcoat * Gr * Fr * Dr;
+    }
+    float am = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+        float ac = v3c(a, c);
+        float Fs = (1.0f - FH) * m.cspec0[c] + FH;
+        g->cspec0[c] += ac * NdotL * m.metallic * (1.0f - FH);
+        am += ac * (Fs + cg) * NdotL;
+    }
+    g->metallic += am;
+}
+
+// a^T d(material_eval)/d(record fields), added to g.
+GB_HD void material_eval_vjp(const MaterialRec& m, int lobe, v3 wo, v3 wi, v3 N, v3 a, MatGrad* g) {
+    if (m.kind == MAT_LAMBERT) {
+        float f = kInvPi * fabsf(dot(wi, N));
+        g->diffuse[0] += a.x * f; g->diffuse[1] += a.y * f; g->diffuse[2] += a.z * f;
+        return;
+    }
+    if (lobe == LOBE_DISNEY_REFLECTION) { principled_specular_vjp(m, wo, N, wi, a, g); return; }
+    if (lobe == LOBE_SPECULAR_REFLECTION || lobe == LOBE_SPECULAR_TRANSMISSION) return;
+    principled_diffuse_vjp(m, wo, N, wi, a, g);
+}
+
 // ------------------------------------------------------------ shade/bounce --
 // Parameters of compute_path_contribution_and_bounce that the reference hard
 // codes (hybrid-pt.cpp:45, :52, :551; arealight-sampler-cpu.cpp:115).
@@ -517,14 +655,43 @@ GB_HD BsdfSample sample_bsdf(const MaterialRec& m, v3 Nraw, v3 ray_dir, v3 rnd) 
     return s;
 }
 
+// What the path-replay adjoint needs of one shaded vertex: the directions
+// and normal the BRDF was evaluated with, the sampling pdf and roulette
+// probability (both held fixed when differentiating), the lobe, which
+// throughput channels were clamped at 1, and whether the NEE term counted.
+struct ShadeTrace {
+    v3 wo, wi, N, ld;
+    float pdf, q;
+    int lobe;
+    uint32_t clamp_mask;  // bit c: channel c of the new throughput was clamped
+    bool nee;
+};
+
+GB_HD v3 clamp_one(v3 t, uint32_t* mask) {
+    uint32_t mk_ = 0;
+    if (t.x > 1.0f) { t.x = 1.0f; mk_ |= 1u; }
+    if (t.y > 1.0f) { t.y = 1.0f; mk_ |= 2u; }
+    if (t.z > 1.0f) { t.z = 1.0f; mk_ |= 4u; }
+    *mask = mk_;
+    return t;
+}
+GB_HD bool has_nan(v3 t) { return t.x != t.x || t.y != t.y || t.z != t.z; }
+
 // One pixel of compute_path_contribution_and_bounce (hybrid-pt.cpp:465-564)
 // for a valid hit.  P, Nraw: interpolated hit point / normal; ray_dir: the
 // ray direction; rnd: the path-stream draw; unoccluded: shadow result;
 // to_light, psc: the NEE outputs of this bounce.
+// Frozen-sampling replay (me, tp0 given): directions, lobes and pdfs come
+// from m, the BRDF values from me; tp0 carries the throughput under m, which
+// makes the roulette and path-end decisions, so the path's random choices
+// are those of m while its value is that of me.  trace (optional) receives
+// the vertex record of the adjoint.
 GB_HD ShadeOut shade_hit(const MaterialRec& m, v3 P, v3 Nraw, v3 ray_dir, v3 tp, v3 rnd,
                          bool unoccluded, v3 to_light, v3 psc, const ShadeParams& sp,
-                         uint32_t pixel, uint32_t path, int bounce) {
+                         uint32_t pixel, uint32_t path, int bounce, const MaterialRec* me = nullptr,
+                         v3* tp0 = nullptr, ShadeTrace* trace = nullptr) {
     ShadeOut o;
+    const MaterialRec& E = me ? *me : m;
     BsdfSample bs = sample_bsdf(m, Nraw, ray_dir, rnd);
     const v3 org_dir = bs.org_dir, inv_org_dir = bs.inv_org_dir, N = bs.N, wi = bs.wi;
     const float pdf = bs.pdf;
@@ -532,38 +699,51 @@ GB_HD ShadeOut shade_hit(const MaterialRec& m, v3 P, v3 Nraw, v3 ray_dir, v3 tp,
     const bool glass = bs.glass;
     // evaluate_material (hybrid-pt.cpp:351-371)
     o.accum_add = mk(0.0f, 0.0f, 0.0f);
+    bool nee = false;
+    v3 ld = mk(0.0f, 0.0f, 0.0f);
     if (!glass && unoccluded) {
         v3 currTP = tp * psc;
-        v3 ld = normalize_div(to_light);
-        v3 bl = material_eval(m, lobe, inv_org_dir, ld, N);
+        ld = normalize_div(to_light);
+        v3 bl = material_eval(E, lobe, inv_org_dir, ld, N);
         v3 add = bl * currTP;
-        if (add.x == add.x && add.y == add.y && add.z == add.z) o.accum_add = add;
+        if (!has_nan(add)) { o.accum_add = add; nee = true; }
     }
-    v3 brdf = material_eval(m, lobe, inv_org_dir, wi, N);
+    v3 brdf = material_eval(E, lobe, inv_org_dir, wi, N);
     // next ray (hybrid-pt.cpp:550-562)
     v3 Pn = glass ? P + sp.ray_offset * org_dir : P + sp.ray_offset * N;
     o.org = Pn;
     o.dir = wi;
-    v3 ntp = (tp * brdf) / pdf;
-    if (ntp.x > 1.0f) ntp.x = 1.0f;
-    if (ntp.y > 1.0f) ntp.y = 1.0f;
-    if (ntp.z > 1.0f) ntp.z = 1.0f;
+    uint32_t cmask = 0;
+    v3 ntp = clamp_one((tp * brdf) / pdf, &cmask);
+    v3 ntp0 = ntp;  // throughput that makes the decisions
+    if (tp0) {
+        uint32_t unused;
+        ntp0 = clamp_one((*tp0 * material_eval(m, lobe, inv_org_dir, wi, N)) / pdf, &unused);
+    }
     o.alive = true;
     // pdf == 0 or a NaN throughput would poison the pixel forever in the
     // reference; such paths end here.
-    if (!(pdf > 0.0f) || ntp.x != ntp.x || ntp.y != ntp.y || ntp.z != ntp.z) {
+    if (!(pdf > 0.0f) || has_nan(ntp0)) {
         o.alive = false;
+        ntp = ntp0 = mk(0.0f, 0.0f, 0.0f);
+    } else if (has_nan(ntp)) {
         ntp = mk(0.0f, 0.0f, 0.0f);
     }
     // Russian roulette (extension, off when rr_start < 0)
+    float q = 1.0f;
     if (o.alive && sp.rr_start >= 0 && bounce >= sp.rr_start) {
-        float q = fmaxf(fmaxf(ntp.x, ntp.y), ntp.z);
+        q = fmaxf(fmaxf(ntp0.x, ntp0.y), ntp0.z);
         q = clampf(q, 0.05f, 1.0f);
         float u = rr_uniform(sp.seed, pixel, path, (uint32_t)bounce);
-        if (u >= q) { o.alive = false; ntp = mk(0.0f, 0.0f, 0.0f); }
-        else ntp = ntp / q;
+        if (u >= q) { o.alive = false; ntp = ntp0 = mk(0.0f, 0.0f, 0.0f); }
+        else { ntp = ntp / q; ntp0 = ntp0 / q; }
     }
     o.tp = ntp;
+    if (tp0) *tp0 = ntp0;
+    if (trace) {
+        trace->wo = inv_org_dir; trace->wi = wi; trace->N = N; trace->ld = ld;
+        trace->pdf = pdf; trace->q = q; trace->lobe = lobe; trace->clamp_mask = cmask; trace->nee = nee;
+    }
     return o;
 }
 

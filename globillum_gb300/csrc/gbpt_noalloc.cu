@@ -151,6 +151,7 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
     R.rng_mode = d->rng_mode;
     R.pixel_base = 0;
     R.seed = d->seed;
+    mrg_jump_matrices(3ull * (uint64_t)R.L, R.jump1, R.jump2);
     RenderParams P{};
     P.refill = 16;
     P.tri_mode = 0;

@@ -72,6 +72,11 @@ class BatchItem(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("desc", RenderDesc), ("out_rgb", C.c_void_p)]
 
 
+class AdjointItem(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("desc", RenderDesc), ("dL_dimg", C.c_void_p),
+                ("dL_dparams", C.c_void_p)]
+
+
 class Hit(C.Structure):
     _fields_ = [("t", C.c_float), ("beta", C.c_float), ("gamma", C.c_float), ("ref", C.c_uint32)]
 
@@ -93,7 +98,8 @@ EXPORTS = [
     "gb_trace_closest", "gb_trace_any", "gb_generate_arealight_sample", "gb_compute_path_contribution_and_bounce",
     "gb_mrg_pool", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
     "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning", "gb_set_fault_injection", "gb_render_batch",
-    "gb_autotune",
+    "gb_autotune", "gb_scene_param_count", "gb_scene_get_params", "gb_scene_set_params", "gb_forward",
+    "gb_backward", "gb_backward_batch",
 ]
 
 _lib = None
@@ -140,6 +146,12 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_render_noalloc.argtypes = [vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp]
     lib.gb_render_batch.argtypes = [vp, ip, C.POINTER(BatchItem), ip, ip]
     lib.gb_autotune.argtypes = [vp, ip, C.POINTER(BatchItem), ip, ip, C.POINTER(Tuning), C.POINTER(C.c_double)]
+    lib.gb_scene_param_count.argtypes = [vp, C.POINTER(C.c_int)]
+    lib.gb_scene_get_params.argtypes = [vp, vp]
+    lib.gb_scene_set_params.argtypes = [vp, vp]
+    lib.gb_forward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp, ip]
+    lib.gb_backward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, ip, vp]
+    lib.gb_backward_batch.argtypes = [vp, ip, C.POINTER(AdjointItem), ip, ip]
     if path is None:
         _lib = lib
     return lib
@@ -271,6 +283,21 @@ class Context:
         g = -1 if graph is None else (1 if graph else 0)
         self.check(self.lib.gb_render_batch(self.h, len(jobs), items, 1, g))
 
+    def backward_batch(self, jobs: list, dimgs: list, graph: bool | None = None) -> list:
+        """gb_backward_batch over [(Scene, cam, rdesc), ...] with one image
+        gradient per job; returns one parameter gradient per job."""
+        items = (AdjointItem * max(1, len(jobs)))()
+        keep, outs = [], []
+        for i, ((sc, cam, rdesc), g) in enumerate(zip(jobs, dimgs)):
+            g = np.ascontiguousarray(g, np.float32)
+            o = np.empty(sc.param_count(), np.float32)
+            keep.append(g)
+            outs.append(o)
+            items[i] = AdjointItem(sc.h, make_camera(cam), make_render_desc(rdesc), _ptr(g), _ptr(o))
+        gflag = -1 if graph is None else (1 if graph else 0)
+        self.check(self.lib.gb_backward_batch(self.h, len(jobs), items, 0, gflag))
+        return outs
+
     def autotune(self, jobs: list, proxy_spp: int = 0, repeats: int = 2) -> tuple[dict, float]:
         """gb_autotune over the batch; returns (best tuning, its frame ms)
         and leaves that tuning set."""
@@ -320,6 +347,50 @@ class Scene:
         rd = make_render_desc(rdesc)
         self.ctx.check(self.ctx.lib.gb_render(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd),
                                               C.c_void_p(out_ptr), 1))
+
+    # ------------------------------------------------------ differentiation
+    def param_count(self) -> int:
+        n = C.c_int()
+        self.ctx.check(self.ctx.lib.gb_scene_param_count(self.h, C.byref(n)))
+        return n.value
+
+    def get_params(self) -> np.ndarray:
+        x = np.empty(self.param_count(), np.float32)
+        self.ctx.check(self.ctx.lib.gb_scene_get_params(self.h, _ptr(x)))
+        return x
+
+    def set_params(self, x) -> None:
+        x = np.ascontiguousarray(x, np.float32)
+        assert x.shape == (self.param_count(),)
+        self.ctx.check(self.ctx.lib.gb_scene_set_params(self.h, _ptr(x)))
+
+    def forward(self, cam: dict, rdesc: dict, eval_params=None) -> np.ndarray:
+        """gb_forward: the image, or with eval_params the frozen-sampling
+        replay evaluated at eval_params."""
+        rd = make_render_desc(rdesc)
+        out = np.empty((rd.height, rd.width, 3), dtype=np.float32)
+        ev = None if eval_params is None else np.ascontiguousarray(eval_params, np.float32)
+        self.ctx.check(self.ctx.lib.gb_forward(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd), _ptr(ev),
+                                               _ptr(out), 0))
+        return out
+
+    def backward(self, cam: dict, rdesc: dict, dimg) -> np.ndarray:
+        """gb_backward: dLoss/dparams for dLoss/dimage `dimg` (h, w, 3)."""
+        rd = make_render_desc(rdesc)
+        g = np.ascontiguousarray(dimg, np.float32)
+        assert g.shape == (rd.height, rd.width, 3)
+        out = np.empty(self.param_count(), np.float32)
+        self.ctx.check(self.ctx.lib.gb_backward(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd), _ptr(g),
+                                                0, _ptr(out)))
+        return out
+
+    def backward_device(self, cam: dict, rdesc: dict, dimg_ptr: int) -> np.ndarray:
+        """gb_backward with dLoss/dimage in device memory (h*w*3 floats)."""
+        rd = make_render_desc(rdesc)
+        out = np.empty(self.param_count(), np.float32)
+        self.ctx.check(self.ctx.lib.gb_backward(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd),
+                                                C.c_void_p(dimg_ptr), 1, _ptr(out)))
+        return out
 
     def trace_closest(self, orig: np.ndarray, dirs: np.ndarray, max_t: np.ndarray) -> np.ndarray:
         o = np.ascontiguousarray(orig, dtype=np.float32)

@@ -231,6 +231,21 @@ def icospheres(n_spheres: int = 800, level: int = 3, width: int = 1280, height: 
                      name=f"icospheres-{n_spheres}x{nf}+10tri")
 
 
+def param_vector(scene: SceneData) -> np.ndarray:
+    """The scene's differentiable parameters in gb_scene_param_count order:
+    per material base colour, roughness, metallic; per light emission."""
+    out = []
+    for m in scene.materials:
+        if m.get("principled", -1) >= 0:
+            p = scene.params[m["principled"]]
+            out += list(p.get("color", (0.0, 0.0, 0.0))) + [p.get("roughness", 0.0), p.get("metallic", 0.0)]
+        else:
+            out += list(m["diffuse"]) + [0.0, 0.0]
+    for l in scene.lights:
+        out += list(l["col"])
+    return np.array(out, np.float32)
+
+
 def mixed_set(n_scenes: int = 64, seed: int = 42, tri_range: tuple = (1_000, 500_000),
               resolutions: tuple = (64, 128, 256, 512), spp_choices: tuple = (4, 16, 64), max_bounces: int = 6,
               n_materials: int = 256, rr_start: int = 3) -> list:

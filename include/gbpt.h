@@ -181,6 +181,53 @@ typedef struct {
  * call has no counterpart there. */
 int gb_render_batch(gb_ctx* ctx, int n, const gb_batch_item* items, int out_is_device, int graph_capture);
 
+/* ------------------------------------------------------ differentiation */
+/* Differentiable parameters of a scene, as one float vector: per material
+ * (in gb_scene_desc order) base colour r, g, b, roughness, metallic (the
+ * principled set's color / roughness / metallic, or a Lambert material's
+ * diffuse colour with two unused entries), then per light emission r, g, b.
+ * The reference has no derivatives; these calls have no counterpart there. */
+int gb_scene_param_count(const gb_scene* scene, int* n);
+int gb_scene_get_params(const gb_scene* scene, float* params);
+/* Replaces the parameters (materials and light emission; a light described
+ * with power < 0 gets its power recomputed by the add-rectlight rule). */
+int gb_scene_set_params(gb_scene* scene, const float* params);
+
+/* Forward pass of the path-replay adjoint.  eval_params = NULL renders
+ * exactly as gb_render.  Otherwise the frame is replayed with every random
+ * choice (camera jitter, light pick and point, BRDF lobe and direction,
+ * roulette) made with the scene's current parameters while the BRDF values
+ * and emission are evaluated with eval_params: the function whose
+ * derivative gb_backward returns, so finite differences of it at common
+ * random numbers check the adjoint. */
+int gb_forward(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+               const float* eval_params, float* out_rgb, int out_is_device);
+
+/* Backward pass: gradient of a loss with respect to the scene's parameters,
+ * given dL_dimg = dLoss/d(image) (w*h*3 floats, host or device).  The frame
+ * is replayed from its random-number streams (no path is stored between the
+ * passes); each path slot records its vertices (80 bytes per bounce, at
+ * most 16 bounces) and, when the path ends, a reverse sweep adds
+ * hand-written vector-Jacobian products of the BRDF evaluations and the
+ * emission to per-block gradient copies, which are summed in double.  Pdfs,
+ * lobe choices and roulette probabilities are held at their sampled values
+ * (the derivative of gb_forward(eval_params) at eval_params = current).
+ * dL_dparams receives gb_scene_param_count floats. */
+int gb_backward(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+                const float* dL_dimg, int dimg_is_device, float* dL_dparams);
+
+typedef struct {
+    gb_scene* scene;
+    gb_camera camera;
+    gb_render_desc desc;
+    const float* dL_dimg;   /* width*height*3 */
+    float* dL_dparams;      /* gb_scene_param_count of the scene (host) */
+} gb_adjoint_item;
+
+/* gb_backward for several scenes in one wavefront frame (as gb_render_batch;
+ * graph_capture 1 / 0 / -1 as there). */
+int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg_is_device, int graph_capture);
+
 /* -------------------------------------------------------------- tracing */
 /* triangle_intersection (t, beta, gamma, ref): ref = canonical triangle id,
  * 0xffffffff and t = FLT_MAX for a miss. */

@@ -63,6 +63,10 @@ struct OScene {
     bool use_bvh = true;
     std::vector<ONode> nodes;
     std::vector<int> idx;
+    // descriptions the differentiable parameters come from
+    std::vector<gb_material> mats_in;
+    std::vector<gb_principled_params> params_in;
+    std::vector<gb_light> lights_in;
 };
 
 void box_grow(OBox& b, const float* p) {
@@ -263,7 +267,7 @@ void nee_pixel(const OScene& s, int id, const gb_hit& h, v3 rnd, float shadow_of
         int l = pick_light(s.lights.data(), (int)s.lights.size(), s.overall, rnd.z);
         v3 P = tri_interp(s.pos, (int)h.ref, h.beta, h.gamma);
         v3 N = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
-        rect_light_sample(s.lights[l], s.overall, P, N, rnd.x, rnd.y, shadow_offset, so, sd, smax, psc);
+        rect_light_sample(s.lights[l], s.lights[l].col, s.overall, P, N, rnd.x, rnd.y, shadow_offset, so, sd, smax, psc);
     } else {
         *so = mk(FLT_MAX, FLT_MAX, FLT_MAX);
         *sd = mk(0.0f, 0.0f, 0.0f);
@@ -272,6 +276,128 @@ void nee_pixel(const OScene& s, int id, const gb_hit& h, v3 rnd, float shadow_of
     }
     (void)id;
 }
+
+// ---------------------------------------------------- FP64 adjoint reference --
+// Forward-mode dual numbers in double: value and derivative with respect to
+// one parameter.
+struct Dd {
+    double v, d;
+};
+inline Dd cst(double x) { return Dd{x, 0.0}; }
+inline Dd operator+(Dd a, Dd b) { return Dd{a.v + b.v, a.d + b.d}; }
+inline Dd operator-(Dd a, Dd b) { return Dd{a.v - b.v, a.d - b.d}; }
+inline Dd operator*(Dd a, Dd b) { return Dd{a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dd operator/(Dd a, Dd b) { return Dd{a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline Dd powc(Dd a, double e) {  // a^e for a >= 0
+    if (a.v <= 0.0) return Dd{0.0, 0.0};
+    return Dd{std::pow(a.v, e), e * std::pow(a.v, e - 1.0) * a.d};
+}
+inline Dd mixd(Dd x, Dd y, Dd t) { return (cst(1.0) - t) * x + t * y; }
+
+struct MatD {
+    int kind;
+    Dd diffuse[3], metallic, subsurface, roughness, sheen, clearcoat;
+    Dd cdlin[3], csheen[3], cspec0[3];
+    double cc_a, cc_a2m1, cc_pilog;
+};
+
+// make_material (principledMaterial.h:178-252 constants) in dual numbers;
+// `seed` = 0..4 marks colour r, g, b, roughness or metallic as the variable.
+MatD make_material_d(const gb_material& m, const gb_principled_params* params, int seed) {
+    MatD r{};
+    if (m.principled < 0) {
+        r.kind = MAT_LAMBERT;
+        for (int c = 0; c < 3; ++c) r.diffuse[c] = Dd{m.diffuse[c], seed == c ? 1.0 : 0.0};
+        return r;
+    }
+    const gb_principled_params& p = params[m.principled];
+    r.kind = MAT_PRINCIPLED;
+    Dd col[3];
+    for (int c = 0; c < 3; ++c) col[c] = Dd{p.color[c], seed == c ? 1.0 : 0.0};
+    r.roughness = Dd{p.roughness, seed == 3 ? 1.0 : 0.0};
+    r.metallic = Dd{p.metallic, seed == 4 ? 1.0 : 0.0};
+    r.subsurface = cst(p.subsurface);
+    r.sheen = cst(p.sheen);
+    r.clearcoat = cst(p.clearcoat);
+    Dd cd[3];
+    for (int c = 0; c < 3; ++c) cd[c] = powc(col[c], 2.2);
+    Dd lum = cst(.3) * cd[0] + cst(.6) * cd[1] + cst(.1) * cd[2];
+    for (int c = 0; c < 3; ++c) {
+        Dd ct = lum.v > 0.0 ? cd[c] / lum : cst(1.0);
+        r.cdlin[c] = cd[c];
+        r.csheen[c] = cst(1.0 - p.sheen_tint) + cst(p.sheen_tint) * ct;
+        Dd st = cst(1.0 - p.specular_tint) + cst(p.specular_tint) * ct;
+        r.cspec0[c] = (cst(1.0) - r.metallic) * cst(p.specular * .08) * st + r.metallic * cd[c];
+    }
+    double a = (1.0 - p.clearcoat_gloss) * 0.1 + p.clearcoat_gloss * 0.001;
+    r.cc_a = a;
+    r.cc_a2m1 = a * a - 1.0;
+    r.cc_pilog = M_PI * std::log(a * a);
+    return r;
+}
+
+struct V3d {
+    double x, y, z;
+};
+inline V3d vd(v3 a) { return V3d{a.x, a.y, a.z}; }
+inline double dotd(V3d a, V3d b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double schlickd(double u) {
+    double m = std::min(1.0, std::max(0.0, 1.0 - u));
+    return m * m * m * m * m;
+}
+inline double smithd(double ndv, double ag) {
+    double a = ag * ag, b = ndv * ndv;
+    return 1.0 / (ndv + std::sqrt(a + b - a * b));
+}
+
+// material_eval (principledMaterial.h:210-301, simpleMaterial.h:82-113) in double.
+void eval_d(const MatD& m, int lobe, V3d V, V3d L, V3d N, Dd out[3]) {
+    for (int c = 0; c < 3; ++c) out[c] = cst(0.0);
+    if (m.kind == MAT_LAMBERT) {
+        double f = std::fabs(dotd(L, N)) / M_PI;
+        for (int c = 0; c < 3; ++c) out[c] = m.diffuse[c] * cst(f);
+        return;
+    }
+    if (lobe == LOBE_SPECULAR_REFLECTION) { for (int c = 0; c < 3; ++c) out[c] = cst(1.0); return; }
+    if (lobe == LOBE_SPECULAR_TRANSMISSION) {
+        for (int c = 0; c < 3; ++c) out[c] = cst(1.0 / std::fabs(dotd(L, N)));
+        return;
+    }
+    double NdotL = dotd(N, L), NdotV = dotd(N, V);
+    if (NdotL < 0.0 || NdotV < 0.0) return;
+    V3d H{L.x + V.x, L.y + V.y, L.z + V.z};
+    double hl = std::sqrt(dotd(H, H));
+    H = V3d{H.x / hl, H.y / hl, H.z / hl};
+    double LdotH = dotd(L, H), FH = schlickd(LdotH);
+    if (lobe == LOBE_DISNEY_REFLECTION) {
+        double NdotH = dotd(N, H), cg = 0.0;
+        if (m.clearcoat.v > 0.0) {
+            double Dr = m.cc_a >= 1.0 ? 1.0 / M_PI : m.cc_a2m1 / (m.cc_pilog * (1.0 + m.cc_a2m1 * NdotH * NdotH));
+            double Fr = (1.0 - FH) * 0.04 + FH;
+            cg = 0.25 * m.clearcoat.v * smithd(NdotL, 0.25) * smithd(NdotV, 0.25) * Fr * Dr;
+        }
+        for (int c = 0; c < 3; ++c)
+            out[c] = (cst(1.0 - FH) * m.cspec0[c] + cst(FH + cg)) * cst(NdotL) * m.metallic;
+        return;
+    }
+    double FL = schlickd(NdotL), FV = schlickd(NdotV);
+    Dd Fd90 = cst(0.5) + cst(2.0 * LdotH * LdotH) * m.roughness;
+    Dd Fd = mixd(cst(1.0), Fd90, cst(FL)) * mixd(cst(1.0), Fd90, cst(FV));
+    Dd Fss90 = cst(LdotH * LdotH) * m.roughness;
+    Dd Fss = mixd(cst(1.0), Fss90, cst(FL)) * mixd(cst(1.0), Fss90, cst(FV));
+    Dd ss = cst(1.25) * (Fss * cst(1.0 / (NdotL + NdotV) - 0.5) + cst(0.5));
+    Dd k = cst(1.0 / M_PI) * mixd(Fd, ss, m.subsurface);
+    for (int c = 0; c < 3; ++c)
+        out[c] = (k * m.cdlin[c] + cst(FH) * m.sheen * m.csheen[c]) * (cst(1.0) - m.metallic) * cst(NdotL);
+}
+
+// One shaded vertex of a replayed path.
+struct AdjVertex {
+    int mi, light, lobe;
+    bool nee;
+    float pdf, q, scale;
+    v3 wo, wi, N, ld;
+};
 
 }  // namespace
 
@@ -302,6 +428,9 @@ void* orc_scene_create(int n, const float* pos, const float* nrm, const int* mat
     }
     for (int l = 0; l < nl; ++l) s->lights.push_back(make_light(lights[l]));
     s->overall = overall_power(s->lights.data(), (int)s->lights.size());
+    s->mats_in.assign(mats, mats + nmat);
+    if (nparams > 0 && params) s->params_in.assign(params, params + nparams);
+    if (nl > 0) s->lights_in.assign(lights, lights + nl);
     s->use_bvh = use_bvh != 0;
     if (s->use_bvh) build_bvh(*s);
     return s;
@@ -496,6 +625,125 @@ int orc_render(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0
     return 0;
 }
 
+// FP64 reference gradient of sum(dimg * image) over rows [row0, row1) with
+// respect to the parameters `sel` (gb_scene_param_count layout: 5 per
+// material, then 3 per light): every path is replayed in float exactly as
+// orc_render traces and shades it (same pools), its vertices are recorded,
+// and the path value C = sum_k T_k bl_k col s_k with
+// T_{k+1} = clamp1(T_k brdf_k / pdf_k) / q_k is differentiated in double by
+// forward-mode dual numbers, one parameter at a time, through
+// make_material and the BRDF formulas (directions, pdfs and roulette held
+// at their sampled values).  dimg: rows' pixels x 3 (not divided by spp).
+int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0, int row1, const float* pool,
+                    int pool_updates, const float* dimg, int n_sel, const int* sel, double* out) {
+    const OScene& s = *(const OScene*)sp;
+    const int W = d->width, H = d->height, L = d->max_bounces;
+    if (row0 < 0 || row1 > H || row0 >= row1) return 1;
+    if (pool_updates < d->spp * L) return 2;
+    if (cam->aperture != 0.0f && (row0 != 0 || row1 != H)) return 3;
+    const int n = W * (row1 - row0), base = row0 * W;
+    const int nm = (int)s.mats_in.size();
+    CameraRec C = make_camera(*cam, W, H);
+    ShadeParams par = make_shade_params(*d);
+    for (int j = 0; j < n_sel; ++j) out[j] = 0.0;
+    const gb_principled_params* prm = s.params_in.empty() ? nullptr : s.params_in.data();
+#pragma omp parallel
+    {
+        std::vector<double> acc(n_sel, 0.0);
+        std::vector<AdjVertex> vs;
+#pragma omp for schedule(dynamic, 16)
+        for (int i = 0; i < n; ++i) {
+            const int id = base + i, x = id % W, y = id / W;
+            const v3 g = mk(dimg[3 * i], dimg[3 * i + 1], dimg[3 * i + 2]);
+            if (g.x == 0.0f && g.y == 0.0f && g.z == 0.0f) continue;
+            for (int p = 0; p < d->spp; ++p) {
+                const float* jp = pool + (size_t)p * n * 3;
+                float lx = 0.0f, ly = 0.0f;
+                if (C.aperture != 0.0f) {
+                    int o = (id + 17) % (W * H);
+                    lx = jp[3 * o + 2] - 0.5f;
+                    ly = jp[3 * o + 1] - 0.5f;
+                }
+                v3 o, dd;
+                camera_ray(C, x, y, jp[3 * i], jp[3 * i + 1], lx, ly, &o, &dd);
+                float tmax = FLT_MAX;
+                v3 tp = mk(1.0f, 1.0f, 1.0f);
+                vs.clear();
+                for (int b = 0; b < L; ++b) {
+                    gb_hit h = trace_closest(s, o, dd, tmax, nullptr, nullptr);
+                    if (h.ref == 0xffffffffu) break;
+                    const float* up = pool + ((size_t)p * L + b) * n * 3;
+                    v3 rnd = mk(up[3 * i], up[3 * i + 1], up[3 * i + 2]);
+                    v3 lr = rnd;
+                    if (d->rng_mode == GB_RNG_HALTON_LIGHT) {
+                        float hy = halton(id + 1, 3);
+                        lr = mk(halton(id + 1, 2), hy, hy);
+                    }
+                    v3 P = tri_interp(s.pos, (int)h.ref, h.beta, h.gamma);
+                    v3 Nr = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
+                    v3 so = mk(0.0f, 0.0f, 0.0f), sd = so, psc = so;
+                    float smax = -1.0f, scale = 0.0f;
+                    int light = 0;
+                    if (!s.lights.empty()) {
+                        light = pick_light(s.lights.data(), (int)s.lights.size(), s.overall, lr.z);
+                        rect_light_sample(s.lights[light], s.lights[light].col, s.overall, P, Nr, lr.x, lr.y,
+                                          d->shadow_offset, &so, &sd, &smax, &psc, &scale);
+                    }
+                    bool occl = smax < 0.0f || trace_any(s, so, sd, smax);
+                    const int mi = s.mat[h.ref];
+                    ShadeTrace tr;
+                    ShadeOut so2 = shade_hit(s.mats[mi], P, Nr, dd, tp, rnd, !occl, sd, psc, par, (uint32_t)id,
+                                             (uint32_t)p, b, nullptr, nullptr, &tr);
+                    vs.push_back(AdjVertex{mi, light, tr.lobe, tr.nee, tr.pdf, tr.q, scale, tr.wo, tr.wi, tr.N, tr.ld});
+                    if (!so2.alive || b + 1 >= L) break;
+                    tp = so2.tp;
+                    o = so2.org;
+                    dd = so2.dir;
+                    tmax = FLT_MAX;
+                }
+                const int K = (int)vs.size();
+                for (int j = 0; j < n_sel; ++j) {
+                    const int pi = sel[j];
+                    int pm = -1, pk = -1, pl = -1, pc = -1;
+                    if (pi < 5 * nm) { pm = pi / 5; pk = pi % 5; }
+                    else { pl = (pi - 5 * nm) / 3; pc = (pi - 5 * nm) % 3; }
+                    bool touched = false;
+                    for (const AdjVertex& v : vs)
+                        if ((pm >= 0 && v.mi == pm) || (pl >= 0 && v.nee && v.light == pl)) touched = true;
+                    if (!touched) continue;
+                    Dd T[3] = {cst(1.0), cst(1.0), cst(1.0)}, Cc[3] = {cst(0.0), cst(0.0), cst(0.0)};
+                    for (int k = 0; k < K; ++k) {
+                        const AdjVertex& v = vs[k];
+                        MatD m = make_material_d(s.mats_in[v.mi], prm, v.mi == pm ? pk : -1);
+                        if (v.nee) {
+                            Dd bl[3];
+                            eval_d(m, v.lobe, vd(v.wo), vd(v.ld), vd(v.N), bl);
+                            const gb_light& li = s.lights_in[v.light];
+                            for (int c = 0; c < 3; ++c) {
+                                Dd col{li.col[c], (v.light == pl && c == pc) ? 1.0 : 0.0};
+                                Cc[c] = Cc[c] + T[c] * bl[c] * col * cst(v.scale);
+                            }
+                        }
+                        if (k + 1 < K) {
+                            Dd br[3];
+                            eval_d(m, v.lobe, vd(v.wo), vd(v.wi), vd(v.N), br);
+                            for (int c = 0; c < 3; ++c) {
+                                Dd t = T[c] * br[c] / cst(v.pdf);
+                                if (t.v > 1.0) t = cst(1.0);
+                                T[c] = t / cst(v.q);
+                            }
+                        }
+                    }
+                    acc[j] += ((double)g.x * Cc[0].d + (double)g.y * Cc[1].d + (double)g.z * Cc[2].d) / d->spp;
+                }
+            }
+        }
+#pragma omp critical
+        for (int j = 0; j < n_sel; ++j) out[j] += acc[j];
+    }
+    return 0;
+}
+
 // Halton pool of util.cpp:38-51 for pixels [0, n): (h2(i+1), h3(i+1)).
 int orc_halton_pool(int n, float* out) {
     for (int i = 0; i < n; ++i) { out[2 * i] = halton(i + 1, 2); out[2 * i + 1] = halton(i + 1, 3); }
@@ -546,6 +794,15 @@ int orc_shade_eval(const gb_material* mat, const gb_principled_params* params, c
 
 int orc_sincos_2pi(int n, const float* u, float* s, float* c) {
     for (int i = 0; i < n; ++i) sincos_2pi(u[i], &s[i], &c[i]);
+    return 0;
+}
+
+// MRG32k3a jump of `steps` generator steps (mrg_jump_matrices + mrg_jump of
+// the library's shared headers) applied to s1[3], s2[3] in place.
+int orc_mrg_jump(unsigned long long steps, uint32_t* s1, uint32_t* s2) {
+    uint32_t J1[9], J2[9];
+    mrg_jump_matrices(steps, J1, J2);
+    mrg_jump(s1, s2, J1, J2);
     return 0;
 }
 

@@ -37,10 +37,12 @@ def load() -> C.CDLL:
         lib.orc_compute_path_contribution_and_bounce.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                                                  vp, vp, ip, ip, ip]
         lib.orc_render.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp]
+        lib.orc_adjoint_f64.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp, vp]
         lib.orc_halton_pool.argtypes = [ip, vp]
         lib.orc_material_sample_eval.argtypes = [vp] * 12
         lib.orc_sincos_2pi.argtypes = [ip, vp, vp, vp]
         lib.orc_shade_eval.argtypes = [vp] * 7
+        lib.orc_mrg_jump.argtypes = [C.c_ulonglong, vp, vp]
         lib.orc_threads.restype = ip
         lib.orc_set_threads.argtypes = [ip]
         lib.orc_set_threads.restype = None
@@ -107,6 +109,25 @@ class OracleScene:
         if rc != 0:
             raise ValueError(f"orc_render failed ({rc})")
         return (out, st) if with_stats else out
+
+    def adjoint_f64(self, cam: dict, rdesc: dict, pool: np.ndarray, dimg: np.ndarray, sel, row0: int = 0,
+                    row1: int | None = None) -> np.ndarray:
+        """FP64 reference gradient of sum(dimg * image[rows]) with respect to
+        the parameters `sel` (gb_scene_param_count layout)."""
+        rd = _gbpt.make_render_desc(rdesc)
+        cm = _gbpt.make_camera(cam)
+        row1 = rd.height if row1 is None else row1
+        pool = np.ascontiguousarray(pool, np.float32)
+        n = (row1 - row0) * rd.width
+        assert pool.shape[1] == n and pool.shape[2] == 3
+        g = np.ascontiguousarray(dimg, np.float32).reshape(n, 3)
+        sel = np.ascontiguousarray(sel, np.int32)
+        out = np.zeros(sel.shape[0], np.float64)
+        rc = self.lib.orc_adjoint_f64(self.h, C.byref(cm), C.byref(rd), row0, row1, _p(pool), pool.shape[0], _p(g),
+                                      sel.shape[0], _p(sel), _p(out))
+        if rc != 0:
+            raise ValueError(f"orc_adjoint_f64 failed ({rc})")
+        return out
 
     def generate_arealight_sample(self, w, h, shadow_offset, rnd, hits, ray_dir, serial=False):
         n = w * h
@@ -178,6 +199,14 @@ def shade_eval(diffuse, principled: bool, params18, n_raw, ray_dir, rnd, to_ligh
     out = np.zeros(11, np.float32)
     lib.orc_shade_eval(C.byref(m), C.byref(pp), _p(f(n_raw)), _p(f(ray_dir)), _p(f(rnd)), _p(f(to_light)), _p(out))
     return out
+
+
+def mrg_jump(steps: int, s1, s2):
+    """Library jump-ahead of an MRG32k3a state by `steps` generator steps."""
+    a = np.ascontiguousarray(s1, np.uint32).copy()
+    b = np.ascontiguousarray(s2, np.uint32).copy()
+    load().orc_mrg_jump(int(steps), _p(a), _p(b))
+    return a, b
 
 
 def threads() -> int:
