@@ -66,7 +66,7 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     LIBDIR.mkdir(parents=True, exist_ok=True)
     cu = [CSRC / "gbpt_kernels.cu", CSRC / "gbpt_noalloc.cu"]
-    cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp"]
+    cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp", CSRC / "gbpt_ingest.cpp"]
     deps = cu + cpp + _sources()
     if not force and not _stale(LIB, deps):
         return LIB

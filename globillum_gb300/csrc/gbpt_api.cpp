@@ -175,7 +175,7 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nsc
         float4** bufs[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
         for (float4** b : bufs)
             if ((e = dalloc(ctx->slot_allocs, (void**)b, v4)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->slot_allocs, &F.rng, 48 * (size_t)nslots)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.rng, sizeof(MrgState) * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.pix, 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.pb, 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.ps, 4 * (size_t)nslots)) != cudaSuccess) return e;
@@ -193,9 +193,9 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nsc
         ctx->pristine_key.clear();
         if ((e = dalloc(ctx->pixel_allocs, (void**)&F.out, sizeof(float4) * (size_t)n)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->pixel_allocs, (void**)&F.pscene, 4 * (size_t)n)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->pixel_allocs, &F.pristine, 48 * (size_t)n)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->pixel_allocs, &F.cursor, 48 * (size_t)n)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->pixel_allocs, &F.jcursor, 48 * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, (void**)&F.pristine, sizeof(MrgState) * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, (void**)&F.cursor, sizeof(MrgState) * (size_t)n)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->pixel_allocs, (void**)&F.jcursor, sizeof(MrgState) * (size_t)n)) != cudaSuccess) return e;
         ctx->pixel_cap = (size_t)n;
     }
     if ((size_t)nscenes > ctx->scenes_cap) {
@@ -571,8 +571,8 @@ int begin_frame(gb_ctx* ctx, std::vector<BatchScene>& items) {
         ctx->pristine_key = key;
     }
     // both streams of every pixel restart at curand_init(seed, pixel, 0)
-    CK(cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(F.jcursor, F.pristine, sizeof(MrgState) * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->active = true;
     return GB_OK;
 }
@@ -606,7 +606,7 @@ int run_chunk_loop(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters
         CK(stage_mark(ctx, 4, true));
         if (P.mode == MODE_ADJOINT) CK(k_launch_adjoint(F, P, ctx->stream));
         CK(k_launch_regen(F, P, ctx->stream));
-        CK(k_launch_step(F, 0, false, max_iters, ctx->stream));
+        CK(k_launch_step(F, P, 0, false, max_iters, ctx->stream));
         CK(stage_mark(ctx, 4, false));
         if (it % kEvery == kEvery - 1) {
             int k = head % kSnaps;
@@ -699,7 +699,7 @@ int build_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_it
             if (e == cudaSuccess) e = k_launch_shade(F, P, a);
             if (e == cudaSuccess && P.mode == MODE_ADJOINT) e = k_launch_adjoint(F, P, a);
             if (e == cudaSuccess) e = k_launch_regen(F, P, a);
-            if (e == cudaSuccess) e = k_launch_step(F, (unsigned long long)h, true, max_iters, a);
+            if (e == cudaSuccess) e = k_launch_step(F, P, (unsigned long long)h, true, max_iters, a);
             cudaGraph_t body_out = nullptr;
             e2 = cudaStreamEndCapture(a, &body_out);
             if (e == cudaSuccess) e = e2;

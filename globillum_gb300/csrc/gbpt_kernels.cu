@@ -329,6 +329,43 @@ __device__ __forceinline__ v3 draw3(curandStateMRG32k3a* s) {
     return mk(x, y, z);
 }
 
+// MrgState <-> curandStateMRG32k3a (the Box-Muller caches are unused by
+// uniform draws and start cleared, as after curand_init).
+__device__ __forceinline__ curandStateMRG32k3a mrg_expand(const MrgState& m) {
+    curandStateMRG32k3a st;
+    for (int k = 0; k < 3; ++k) { st.s1[k] = m.s1[k]; st.s2[k] = m.s2[k]; }
+    st.boxmuller_flag = 0;
+    st.boxmuller_flag_double = 0;
+    st.boxmuller_extra = 0.0f;
+    st.boxmuller_extra_double = 0.0;
+    return st;
+}
+__device__ __forceinline__ MrgState mrg_pack(const curandStateMRG32k3a& st) {
+    MrgState m;
+    for (int k = 0; k < 3; ++k) { m.s1[k] = st.s1[k]; m.s2[k] = st.s2[k]; }
+    return m;
+}
+// 24-byte states as three 8-byte accesses.
+__device__ __forceinline__ MrgState ld_mrg(const MrgState* base, size_t i) {
+    const uint2* q = reinterpret_cast<const uint2*>(base + i);
+    uint2 a = q[0], b = q[1], c = q[2];
+    MrgState m;
+    m.s1[0] = a.x; m.s1[1] = a.y; m.s1[2] = b.x; m.s2[0] = b.y; m.s2[1] = c.x; m.s2[2] = c.y;
+    return m;
+}
+__device__ __forceinline__ void st_mrg(MrgState* base, size_t i, const MrgState& m) {
+    uint2* q = reinterpret_cast<uint2*>(base + i);
+    q[0] = make_uint2(m.s1[0], m.s1[1]);
+    q[1] = make_uint2(m.s1[2], m.s2[0]);
+    q[2] = make_uint2(m.s2[1], m.s2[2]);
+}
+__device__ __forceinline__ v3 draw3(MrgState* m) {
+    curandStateMRG32k3a st = mrg_expand(*m);
+    v3 r = draw3(&st);
+    *m = mrg_pack(st);
+    return r;
+}
+
 // curand states right after curand_init(seed, pixel, 0) (util-kernels.cu:277-285)
 // for every pixel of every scene of the frame (pixel = index within its scene).
 __global__ void k_rng_init_frame(Frame F) {
@@ -337,7 +374,7 @@ __global__ void k_rng_init_frame(Frame F) {
     const SceneRec& R = F.scenes[F.pscene[g]];
     curandStateMRG32k3a s;
     curand_init((unsigned long long)R.seed, (unsigned long long)(g - (int)R.pixel_base), 0ull, &s);
-    ((curandStateMRG32k3a*)F.pristine)[g] = s;
+    st_mrg(F.pristine, (size_t)g, mrg_pack(s));
 }
 
 // Scene of every global pixel.
@@ -375,14 +412,13 @@ __global__ void k_jitter_pool(Frame F, RenderParams P) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= F.ntot) return;
     const int spp = F.scenes[F.pscene[g]].spp;
-    curandStateMRG32k3a* jc = (curandStateMRG32k3a*)F.jcursor;
-    curandStateMRG32k3a s = jc[g];
+    MrgState s = ld_mrg(F.jcursor, (size_t)g);
     const int pe = min(P.p0 + P.rounds, spp);
     for (int p = P.p0; p < pe; ++p) {
         v3 j = draw3(&s);
         F.jpool[P.round_start[p - P.p0] + (uint32_t)g] = make_float4(j.x, j.y, j.z, 0.0f);
     }
-    jc[g] = s;
+    st_mrg(F.jcursor, (size_t)g, s);
 }
 
 __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t l) {
@@ -404,11 +440,10 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
         lx = lj.z - 0.5f;
         ly = lj.y - 0.5f;
     }
-    curandStateMRG32k3a* cur = (curandStateMRG32k3a*)F.cursor;
-    curandStateMRG32k3a bs = cur[gpix];
-    ((curandStateMRG32k3a*)F.rng)[slot] = bs;
+    MrgState bs = ld_mrg(F.cursor, gpix);
+    st_mrg(F.rng, slot, bs);
     mrg_jump(bs.s1, bs.s2, R.jump1, R.jump2);  // = L draw3 calls
-    cur[gpix] = bs;
+    st_mrg(F.cursor, gpix, bs);
     v3 o, d;
     camera_ray(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w), j.x, j.y, lx, ly, &o, &d);
     F.ray_o[slot] = make_float4(o.x, o.y, o.z, FLT_MAX);
@@ -438,34 +473,23 @@ __device__ __forceinline__ void end_paths(const Frame& F, bool ended, uint32_t s
 // appending them to the next extension queue.
 __global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P) {
     const int it = *F.iter;
-    uint32_t* cn = ctr_set(F, it + 1);
-    const uint32_t count = cn[4];
+    const uint32_t* cn = ctr_set(F, it + 1);
+    const uint32_t count = cn[4];   // ended paths of this iteration (free queue)
+    const uint32_t next0 = cn[0];   // paths already queued for the next iteration
+    const uint32_t l0 = *F.path_ctr;
+    const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
     uint32_t* qout = F.q[(it + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < count; i0 += stride) {
-        uint32_t qi = i0 + lane_id();
-        bool ended = qi < count;
-        uint32_t slot = 0;
-        if (ended) {
-            slot = F.q[3][qi];
-            uint32_t p = F.pb[slot] >> 10;
-            F.samples[P.round_start[p - (uint32_t)P.p0] + F.pix[slot]] = F.accum[slot];
+    // free-queue entry qi takes path l0 + qi and next-queue entry next0 + qi:
+    // no counter round trip; k_step advances both counters afterwards
+    for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < count; qi += stride) {
+        const uint32_t slot = F.q[3][qi];
+        const uint32_t p = F.pb[slot] >> 10;
+        F.samples[P.round_start[p - (uint32_t)P.p0] + F.pix[slot]] = F.accum[slot];
+        if (qi < avail) {
+            start_path(F, P, slot, l0 + qi);
+            qout[next0 + qi] = slot;
         }
-        uint32_t m = __ballot_sync(0xffffffffu, ended);
-        uint32_t leader = (uint32_t)__ffs(m) - 1u;
-        uint32_t base = 0;
-        if (lane_id() == leader) base = atomicAdd(F.path_ctr, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, (int)leader);
-        bool started = false;
-        if (ended) {
-            uint32_t l = base + (uint32_t)__popc(m & ((1u << lane_id()) - 1u));
-            if (l < P.chunk_paths) {
-                start_path(F, P, slot, l);
-                started = true;
-            }
-        }
-        add_stats(&F.stats[0], started ? 1u : 0u);
-        push(started, slot, qout, cn);
     }
 }
 
@@ -479,14 +503,23 @@ __global__ void __launch_bounds__(kBlock) k_start(Frame F, RenderParams P, int n
     push(go, s, F.q[0], F.ctr + 0);  // queue of iteration 0
 }
 
-// End of an iteration: clears the counter set two iterations ahead, moves
-// the iteration index, counts the iteration (stats[7]) and tells the graph's loop (when there is one)
-// whether the next extension queue has work.
-__global__ void k_step(Frame F, unsigned long long cond, int has_cond, int max_iters) {
+// End of an iteration: accounts the paths k_regen started (path counter,
+// next queue count, camera rays), clears the counter set two iterations
+// ahead, moves the iteration index, counts the iteration (stats[7]) and
+// tells the graph's loop (when there is one) whether the next extension
+// queue has work.
+__global__ void k_step(Frame F, RenderParams P, unsigned long long cond, int has_cond, int max_iters) {
     const int it = *F.iter;
+    uint32_t* cn = ctr_set(F, it + 1);
+    const uint32_t l0 = *F.path_ctr;
+    const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
+    const uint32_t started = min(cn[4], avail);
+    *F.path_ctr = l0 + started;
+    cn[0] += started;
+    F.stats[0] += (unsigned long long)started;
     uint32_t* c2 = ctr_set(F, it + 2);
     for (int k = 0; k < 8; ++k) c2[k] = 0u;
-    const uint32_t next = ctr_set(F, it + 1)[0];
+    const uint32_t next = cn[0];
     *F.iter = it + 1;
     F.stats[7] += 1ull;
     if (next != 0u && it + 1 >= max_iters) atomicOr(F.status, (uint32_t)ST_ITER_LIMIT);
@@ -606,7 +639,6 @@ __global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
     const uint32_t* qin = F.q[it & 1];
     uint32_t* qsh = F.q[2];
     uint32_t nvis = 0, ntri = 0;
-    curandStateMRG32k3a* rs = (curandStateMRG32k3a*)F.rng;
     auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris) {
         uint32_t slot = qin[q];
         float4 ro = F.ray_o[slot], rd = F.ray_d[slot];
@@ -638,9 +670,9 @@ __global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
                 float4 na = __ldg(sh + 3), nb = __ldg(sh + 4), nc = __ldg(sh + 5);
                 v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
                 v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
-                curandStateMRG32k3a st = rs[slot];
+                MrgState st = ld_mrg(F.rng, slot);
                 v3 rnd = draw3(&st);
-                rs[slot] = st;
+                st_mrg(F.rng, slot, st);
                 v3 lr = rnd;
                 if (R.rng_mode == 1) {
                     int pid = (int)(F.pix[slot] - R.pixel_base) + 1;
@@ -750,7 +782,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
             uint32_t pbv = F.pb[slot];
             int bounce = (int)(pbv & 1023u);
             uint32_t path = pbv >> 10;
-            float4 rd = F.ray_d[slot], tp4 = F.tp[slot], rn = F.rnd[slot], ps = F.psc[slot];
+            float4 rd = F.ray_d[slot], tp4 = F.tp[slot], rn = F.rnd[slot],
+                   ps = F.psc[slot];
             float4 acc = F.accum[slot];
             ShadeOut o;
             if (MODE == MODE_FROZEN) {
@@ -1112,8 +1145,9 @@ cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_step(const Frame& F, unsigned long long cond, bool has_cond, int max_iters, cudaStream_t st) {
-    k_step<<<1, 1, 0, st>>>(F, cond, has_cond ? 1 : 0, max_iters);
+cudaError_t k_launch_step(const Frame& F, const RenderParams& P, unsigned long long cond, bool has_cond,
+                          int max_iters, cudaStream_t st) {
+    k_step<<<1, 1, 0, st>>>(F, P, cond, has_cond ? 1 : 0, max_iters);
     return cudaGetLastError();
 }
 

@@ -26,6 +26,12 @@ struct DevScene {
     const LightRec* lights_eval;
 };
 
+// The six 32-bit component words of a curandStateMRG32k3a (s1[3], s2[3]):
+// all a uniform draw reads and writes, stored in 24 bytes instead of 48.
+struct MrgState {
+    uint32_t s1[3], s2[3];
+};
+
 // Status bits written by the kernels (never a trap).
 enum { ST_STACK_OVERFLOW = 1u, ST_ITER_LIMIT = 2u };
 
@@ -68,16 +74,16 @@ struct Frame {
     float4* rnd;       // path draw of this bounce
     float4* hit_p;     // hit point xyz | material index bits
     float4* hit_n;     // interpolated (unnormalised) normal
-    void* rng;         // curandStateMRG32k3a: light/path stream of the slot's path
+    MrgState* rng;     // light/path stream of the slot's path
     uint32_t* pix;     // global pixel of the slot's path
     uint32_t* ps;      // scene of the slot's path
     uint32_t* pb;      // path index << 10 | bounce
     uint32_t* q[4];    // queues: extension (ping/pong), shadow, ended paths; nslots entries each
     // per global pixel
     float4* out;       // output_color (moving average)
-    void* pristine;    // curandStateMRG32k3a after curand_init(seed, pixel, 0)
-    void* cursor;      // curandStateMRG32k3a: light/path stream at the pixel's next path
-    void* jcursor;     // curandStateMRG32k3a: camera-jitter stream at the pixel's next path
+    MrgState* pristine;  // stream after curand_init(seed, pixel, 0)
+    MrgState* cursor;    // light/path stream at the pixel's next path
+    MrgState* jcursor;   // camera-jitter stream at the pixel's next path
     uint32_t* pscene;  // scene of each pixel
     float4* samples;   // sample of path l of the chunk (l = round_start[r] + pixel)
     float4* jpool;     // camera jitter of path l of the chunk
@@ -117,7 +123,8 @@ cudaError_t k_launch_extend(const Frame& F, const RenderParams& P, bool instrume
 cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrument, cudaStream_t st);
 cudaError_t k_launch_shade(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st);
-cudaError_t k_launch_step(const Frame& F, unsigned long long cond, bool has_cond, int max_iters, cudaStream_t st);
+cudaError_t k_launch_step(const Frame& F, const RenderParams& P, unsigned long long cond, bool has_cond,
+                          int max_iters, cudaStream_t st);
 cudaError_t k_launch_jitter_pool(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_combine(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t st);

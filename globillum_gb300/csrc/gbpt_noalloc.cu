@@ -45,7 +45,7 @@ constexpr size_t kAlign = 256;
 
 constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 constexpr size_t kV4 = align_up(sizeof(float4) * (size_t)kNoAllocMaxPixels);  // one float4 per slot / pixel
-constexpr size_t kRng = align_up(48 * (size_t)kNoAllocMaxPixels);             // curandStateMRG32k3a per slot / pixel
+constexpr size_t kRng = align_up(sizeof(MrgState) * (size_t)kNoAllocMaxPixels);  // MRG32k3a words per slot / pixel
 constexpr size_t kU32 = align_up(4 * (size_t)kNoAllocMaxPixels);              // one 32-bit word per slot
 constexpr size_t kCtr = align_up(4 * 32);
 constexpr size_t kStats = align_up(8 * 8);
@@ -85,15 +85,15 @@ Frame carve(unsigned char* base, int n, SceneRec** rec) {
     size_t off = 0;
     float4** planes[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
     for (float4** p : planes) { *p = (float4*)(base + off); off += kV4; }
-    F.rng = base + off; off += kRng;
+    F.rng = (MrgState*)(base + off); off += kRng;
     F.pix = (uint32_t*)(base + off); off += kU32;
     F.pb = (uint32_t*)(base + off); off += kU32;
     F.ps = (uint32_t*)(base + off); off += kU32;
     for (int k = 0; k < 4; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
     F.out = (float4*)(base + off); off += kV4;
-    F.pristine = base + off; off += kRng;
-    F.cursor = base + off; off += kRng;
-    F.jcursor = base + off; off += kRng;
+    F.pristine = (MrgState*)(base + off); off += kRng;
+    F.cursor = (MrgState*)(base + off); off += kRng;
+    F.jcursor = (MrgState*)(base + off); off += kRng;
     F.pscene = (uint32_t*)(base + off); off += kU32;
     F.samples = (float4*)(base + off); off += kV4;
     F.jpool = (float4*)(base + off); off += kV4;
@@ -164,8 +164,8 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
     if (e == cudaSuccess) e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(F.status, 0, 4, st);
     if (e == cudaSuccess) e = k_launch_frame_init(F, true, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(F.jcursor, F.pristine, 48 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F.jcursor, F.pristine, sizeof(MrgState) * (size_t)n, cudaMemcpyDeviceToDevice, st);
     // one path sample of every pixel per pass; the host checks the queue
     // count every 8 iterations (a path has at most max_bounces segments)
     const int max_iters = n * (d->max_bounces + 1) + 8;
@@ -180,7 +180,7 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
             if (e == cudaSuccess) e = k_launch_shadow(F, P, false, st);
             if (e == cudaSuccess) e = k_launch_shade(F, P, st);
             if (e == cudaSuccess) e = k_launch_regen(F, P, st);
-            if (e == cudaSuccess) e = k_launch_step(F, 0, false, max_iters, st);
+            if (e == cudaSuccess) e = k_launch_step(F, P, 0, false, max_iters, st);
             if (e == cudaSuccess && (it % 8 == 7 || it == d->max_bounces)) {
                 e = cudaMemcpyAsync(&left, F.ctr + 8 * ((it + 1) % 3), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -99,7 +99,9 @@ EXPORTS = [
     "gb_mrg_pool", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
     "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning", "gb_set_fault_injection", "gb_render_batch",
     "gb_autotune", "gb_scene_param_count", "gb_scene_get_params", "gb_scene_set_params", "gb_forward",
-    "gb_backward", "gb_backward_batch",
+    "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
+    "gb_asset_add_obj", "gb_asset_add_lights", "gb_asset_add_light", "gb_asset_get_desc", "gb_asset_material_name",
+    "gb_read_pbrdf",
 ]
 
 _lib = None
@@ -152,6 +154,17 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_forward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp, ip]
     lib.gb_backward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, ip, vp]
     lib.gb_backward_batch.argtypes = [vp, ip, C.POINTER(AdjointItem), ip, ip]
+    lib.gb_asset_create.argtypes = [C.POINTER(vp)]
+    lib.gb_asset_destroy.argtypes = [vp]
+    lib.gb_asset_destroy.restype = None
+    lib.gb_asset_last_error.argtypes = [vp]
+    lib.gb_asset_last_error.restype = C.c_char_p
+    lib.gb_asset_add_obj.argtypes = [vp, C.c_char_p, C.c_char_p, vp]
+    lib.gb_asset_add_lights.argtypes = [vp, C.c_char_p, C.POINTER(C.c_int)]
+    lib.gb_asset_add_light.argtypes = [vp, C.POINTER(Light)]
+    lib.gb_asset_get_desc.argtypes = [vp, C.POINTER(SceneDesc)]
+    lib.gb_asset_material_name.argtypes = [vp, ip, C.POINTER(C.c_char_p)]
+    lib.gb_read_pbrdf.argtypes = [C.c_char_p, C.POINTER(PrincipledParams)]
     if path is None:
         _lib = lib
     return lib
@@ -409,3 +422,89 @@ class Scene:
         occ = np.empty(n, dtype=np.uint8)
         self.ctx.check(self.ctx.lib.gb_trace_any(self.ctx.h, self.h, n, _ptr(o), _ptr(d), _ptr(t), _ptr(occ), 0))
         return occ
+
+
+_PRINCIPLED_FIELDS = ("metallic", "subsurface", "specular", "roughness", "specular_tint", "anisotropic", "sheen",
+                      "sheen_tint", "clearcoat", "clearcoat_gloss", "opacity", "transmiss")
+
+
+def read_pbrdf(path) -> dict:
+    """gb_read_pbrdf: one .pbrdf file as a params dict."""
+    lib = load_library()
+    p = PrincipledParams()
+    rc = lib.gb_read_pbrdf(str(path).encode(), C.byref(p))
+    if rc != GB_OK:
+        raise GBError(rc, f"cannot read {path}")
+    d = {k: float(getattr(p, k)) for k in _PRINCIPLED_FIELDS}
+    d["color"] = tuple(float(x) for x in p.color)
+    d["tangent"] = tuple(float(x) for x in p.tangent)
+    return d
+
+
+class Asset:
+    """gb_asset: OBJ/MTL geometry, .pbrdf materials and light scripts
+    gathered into one scene description (host only; no GPU needed)."""
+
+    def __init__(self):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        if self.lib.gb_asset_create(C.byref(self.h)) != GB_OK:
+            raise GBError(GB_ERR_OOM, "gb_asset_create failed")
+
+    def _check(self, rc):
+        if rc != GB_OK:
+            raise GBError(rc, self.lib.gb_asset_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.gb_asset_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def add_obj(self, path, material_dir=None, trafo=None):
+        t = None if trafo is None else np.ascontiguousarray(trafo, np.float32).reshape(16)
+        self._check(self.lib.gb_asset_add_obj(self.h, str(path).encode(),
+                                              None if material_dir is None else str(material_dir).encode(), _ptr(t)))
+
+    def add_lights(self, script_path) -> int:
+        """Adds the script's rect lights; returns how many other lights it skipped."""
+        n = C.c_int()
+        self._check(self.lib.gb_asset_add_lights(self.h, str(script_path).encode(), C.byref(n)))
+        return n.value
+
+    def material_names(self) -> list:
+        d = SceneDesc()
+        self._check(self.lib.gb_asset_get_desc(self.h, C.byref(d)))
+        out = []
+        for i in range(d.num_materials):
+            nm = C.c_char_p()
+            self._check(self.lib.gb_asset_material_name(self.h, i, C.byref(nm)))
+            out.append(nm.value.decode())
+        return out
+
+    def scene_data(self, camera: dict | None = None, render: dict | None = None, name: str = "asset"):
+        """The gathered scene as a globillum_gb300.scenes.SceneData (copies)."""
+        from .scenes import SceneData
+        d = SceneDesc()
+        self._check(self.lib.gb_asset_get_desc(self.h, C.byref(d)))
+        n = d.num_triangles
+        fp = C.POINTER(C.c_float)
+        pos = np.ctypeslib.as_array(C.cast(d.positions, fp), shape=(n, 9)).copy() if n else np.zeros((0, 9), np.float32)
+        nrm = np.ctypeslib.as_array(C.cast(d.normals, fp), shape=(n, 9)).copy() if n else np.zeros((0, 9), np.float32)
+        mid = np.ctypeslib.as_array(C.cast(d.material_index, C.POINTER(C.c_int)), shape=(n,)).copy() if n else \
+            np.zeros(0, np.int32)
+        mats = [{"diffuse": tuple(float(x) for x in d.materials[i].diffuse), "principled": int(d.materials[i].principled)}
+                for i in range(d.num_materials)]
+        params = []
+        for i in range(d.num_params):
+            p = d.params[i]
+            q = {k: float(getattr(p, k)) for k in _PRINCIPLED_FIELDS}
+            q["color"] = tuple(float(x) for x in p.color)
+            q["tangent"] = tuple(float(x) for x in p.tangent)
+            params.append(q)
+        lights = []
+        for i in range(d.num_lights):
+            l = d.lights[i]
+            lights.append({"type": int(l.type), "power": float(l.power), "center": tuple(l.center), "dir": tuple(l.dir),
+                           "up": tuple(l.up), "col": tuple(l.col), "wh": tuple(l.wh)})
+        return SceneData(pos.astype(np.float32), nrm.astype(np.float32), mid.astype(np.int32), mats, params, lights,
+                         dict(camera or {}), dict(render or {}), name=name)

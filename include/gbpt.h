@@ -228,6 +228,40 @@ typedef struct {
  * graph_capture 1 / 0 / -1 as there). */
 int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg_is_device, int graph_capture);
 
+/* ---------------------------------------------------------------- ingest */
+/* Scene assets gathered on the host into one gb_scene_desc, as the
+ * reference's loader does (add_objfile_to_flat_tri_list, hl-main.cpp:277-354;
+ * convert_and_upload_materials, material-conversion.cpp:59-148; the light /
+ * add-rectlight forms, lights.scm:4-9 and lights.cpp:84-96).  Textures and
+ * sky lights are not modelled (texture maps are ignored, sky forms skipped). */
+typedef struct gb_asset gb_asset;
+int gb_asset_create(gb_asset** out);
+void gb_asset_destroy(gb_asset* asset);
+const char* gb_asset_last_error(const gb_asset* asset);
+/* Appends the triangles of a Wavefront OBJ file (polygons fanned into
+ * triangles; per-corner normals, or the face normal where a corner has none)
+ * transformed by `trafo` (16 floats, row-major, NULL = identity; normals by
+ * its inverse transpose).  Materials follow the OBJ's MTL library: a name
+ * becomes a principled material when material_dir/<name>.pbrdf exists
+ * (material_dir may be NULL), else Lambert with the MTL's Kd; faces without a
+ * known material use the fallback material 0 (Lambert (1, 0, 0), created with
+ * the first OBJ). */
+int gb_asset_add_obj(gb_asset* asset, const char* obj_path, const char* material_dir, const float* trafo);
+/* Appends the rectangular lights of a scene script: every (light "name"
+ * :type :rect :color (list r g b) :pos (list ...) :dir (list ...) :up (list ...)
+ * :dim (list w h)) form, with add-rectlight's power rule.  Other light types
+ * are counted in *skipped_lights (may be NULL). */
+int gb_asset_add_lights(gb_asset* asset, const char* script_path, int* skipped_lights);
+int gb_asset_add_light(gb_asset* asset, const gb_light* light);
+/* A description of everything gathered so far; its pointers stay valid
+ * until the asset is changed or destroyed. */
+int gb_asset_get_desc(const gb_asset* asset, gb_scene_desc* desc);
+int gb_asset_material_name(const gb_asset* asset, int index, const char** name);
+/* One .pbrdf parameter file (principledParameters.h:64-125): "key value"
+ * pairs; keys absent from the file take the defaults of
+ * principledParameters.h:23-24 (0, opacity 1, transmission 1). */
+int gb_read_pbrdf(const char* path, gb_principled_params* out);
+
 /* -------------------------------------------------------------- tracing */
 /* triangle_intersection (t, beta, gamma, ref): ref = canonical triangle id,
  * 0xffffffff and t = FLT_MAX for a miss. */
@@ -342,7 +376,7 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
  * The scene is created beforehand (gb_scene_create allocates); this call
  * renders the same frame as gb_render into the caller's device buffer
  * `out_rgb` (w*h*3 floats) on `stream` (NULL = legacy default stream), with
- * its wavefront state in one fixed file-scope device array (about 24 MB,
+ * its wavefront state in one fixed file-scope device array (about 22 MB,
  * held by every GPU that loads the library until exit) instead of cudaMalloc.
  * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID.
  * The first call on a device looks the array up (cudaGetSymbolAddress) with

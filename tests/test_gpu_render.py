@@ -113,3 +113,33 @@ def test_mrg_pool_streams(gpu_ctx):
     assert np.array_equal(a[4:], b)
     assert (a > 0).all() and (a <= 1).all()
     assert not np.array_equal(a[0, 0], a[0, 1])
+
+
+def test_ingested_obj_scene_frame(gpu_ctx):
+    """A scene gathered by gb_asset (OBJ + MTL + .pbrdf + light script),
+    created straight from gb_asset_get_desc's description, renders the
+    oracle's frame."""
+    import ctypes as C
+    from pathlib import Path
+    assets = Path(__file__).resolve().parent / "golden" / "assets"
+    a = gbpt.Asset()
+    a.add_obj(assets / "room.obj", assets / "materials")
+    a.add_lights(assets / "room.lights.scm")
+    cam = {"pos": (2.0, 1.5, -3.0), "dir": (0.0, -0.1, 1.0), "up": (0.0, 1.0, 0.0), "fovy_deg": 50.0}
+    rd = {"width": 48, "height": 40, "spp": 3, "max_bounces": 4, "rng_mode": gbpt.GB_RNG_MRG32K3A_POOL, "seed": 0,
+          "ray_offset": 1e-3, "shadow_offset": 1e-3, "rr_start": -1}
+    desc = gbpt.SceneDesc()
+    assert gpu_ctx.lib.gb_asset_get_desc(a.h, C.byref(desc)) == gbpt.GB_OK
+    h = C.c_void_p()
+    gpu_ctx.check(gpu_ctx.lib.gb_scene_create(gpu_ctx.h, C.byref(desc), C.byref(h)))
+    img = np.empty((40, 48, 3), np.float32)
+    gpu_ctx.check(gpu_ctx.lib.gb_render(gpu_ctx.h, h, C.byref(gbpt.make_camera(cam)), C.byref(gbpt.make_render_desc(rd)),
+                                        img.ctypes.data_as(C.c_void_p), 0))
+    gpu_ctx.lib.gb_scene_destroy(h)
+    sd = a.scene_data(cam, rd)
+    a.close()
+    from oracle import oracle
+    pool = gpu_ctx.mrg_pool(48 * 40, rd["spp"] * rd["max_bounces"])
+    ref = oracle.OracleScene(sd, use_bvh=False).render(cam, rd, pool)
+    _compare(img, ref)
+    assert img.mean() > 1e-3
