@@ -68,6 +68,11 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     cu = [CSRC / "gbpt_kernels.cu", CSRC / "gbpt_noalloc.cu"]
     cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp", CSRC / "gbpt_ingest.cpp"]
     deps = cu + cpp + _sources()
+    # the library records the build-time defines it was made with
+    flags = f"GB_TRAV_MIN_BLOCKS={os.environ.get('GBPT_TRAV_MIN_BLOCKS', '')}"
+    stamp = LIB.with_suffix(".flags")
+    if not stamp.exists() or stamp.read_text() != flags:
+        force = True
     if not force and not _stale(LIB, deps):
         return LIB
     nvcc = _nvcc()
@@ -77,6 +82,11 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
         objs.append(o)
         c = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
              "-Xcompiler", "-ffp-contract=off", "-c", str(s), "-o", str(o)]
+        # GBPT_TRAV_MIN_BLOCKS: resident 128-thread blocks per SM the traversal
+        # kernels are compiled for (register budget); 1 = the compiler's choice
+        mb = os.environ.get("GBPT_TRAV_MIN_BLOCKS")
+        if mb:
+            c.insert(1, f"-DGB_TRAV_MIN_BLOCKS={int(mb)}")
         if verbose_ptxas:
             c.insert(1, "-Xptxas=-v")
         cmds.append(c)
@@ -89,6 +99,7 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     tmp = LIB.with_suffix(".so.tmp")
     _run_parallel([[nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]])
     os.replace(tmp, LIB)
+    stamp.write_text(flags)
     return LIB
 
 

@@ -359,9 +359,23 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
         if (p >= 0 && (p >= d->num_params || !d->params)) return fail(ctx, GB_ERR_INVALID, "parameter index out of range");
     }
     std::vector<LightRec> lights;
+    SkyTables sky_tab;
+    int sky_light = -1;
     for (int l = 0; l < d->num_lights; ++l) {
-        if (d->lights[l].type != GB_LIGHT_RECT) return fail(ctx, GB_ERR_UNSUPPORTED, "only rectangular lights are supported");
-        lights.push_back(make_light(d->lights[l]));
+        const gb_light& gl = d->lights[l];
+        if (gl.type == GB_LIGHT_SKY) {
+            if (sky_light >= 0) return fail(ctx, GB_ERR_UNSUPPORTED, "at most one sky light per scene");
+            if (!gl.sky_rgb || gl.sky_w <= 0 || gl.sky_h <= 0 || (long long)gl.sky_w * gl.sky_h > (1ll << 26))
+                return fail(ctx, GB_ERR_INVALID, "sky light without a valid map");
+            for (long long i = 0; i < 3ll * gl.sky_w * gl.sky_h; ++i)
+                if (!std::isfinite(gl.sky_rgb[i]) || gl.sky_rgb[i] < 0.0f)
+                    return fail(ctx, GB_ERR_INVALID, "sky map values must be finite and non-negative");
+            make_sky_tables(gl.sky_rgb, gl.sky_w, gl.sky_h, &sky_tab);
+            sky_light = l;
+        } else if (gl.type != GB_LIGHT_RECT) {
+            return fail(ctx, GB_ERR_UNSUPPORTED, "unknown light type");
+        }
+        lights.push_back(make_light(gl));
         if (!(lights.back().power > 0.0f)) return fail(ctx, GB_ERR_INVALID, "light power must be positive");
     }
     CwBvh bvh;
@@ -410,6 +424,29 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     if (e == cudaSuccess) e = cudaMemcpy(pm, mats.data(), bm, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !lights.empty())
         e = cudaMemcpy(pl, lights.data(), sizeof(LightRec) * lights.size(), cudaMemcpyHostToDevice);
+    sc->S.sky = SkyRec{};
+    sc->S.sky.light = -1;
+    if (e == cudaSuccess && sky_light >= 0) {
+        const std::vector<float>* src[5] = {&sky_tab.texel, &sky_tab.row_cdf, &sky_tab.row_pdf, &sky_tab.col_cdf,
+                                            &sky_tab.col_pdf};
+        const float* dst[5] = {};
+        for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+            void* p = nullptr;
+            e = dalloc(sc->allocs, &p, sizeof(float) * src[k]->size());
+            if (e == cudaSuccess) e = cudaMemcpy(p, src[k]->data(), sizeof(float) * src[k]->size(), cudaMemcpyHostToDevice);
+            dst[k] = (const float*)p;
+            bs += sizeof(float) * src[k]->size();
+        }
+        sc->S.sky.texel = dst[0];
+        sc->S.sky.row_cdf = dst[1];
+        sc->S.sky.row_pdf = dst[2];
+        sc->S.sky.col_cdf = dst[3];
+        sc->S.sky.col_pdf = dst[4];
+        sc->S.sky.w = sky_tab.w;
+        sc->S.sky.h = sky_tab.h;
+        sc->S.sky.scale = lights[sky_light].scale;
+        sc->S.sky.light = sky_light;
+    }
     if (e != cudaSuccess) {
         free_all(sc->allocs);
         delete sc;
@@ -429,6 +466,7 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     sc->mats.assign(d->materials, d->materials + d->num_materials);
     if (d->num_params > 0) sc->params.assign(d->params, d->params + d->num_params);
     if (d->num_lights > 0) sc->lights.assign(d->lights, d->lights + d->num_lights);
+    for (gb_light& l : sc->lights) l.sky_rgb = nullptr;  // the map was copied; the caller owns its memory
     sc->info.num_triangles = n;
     sc->info.num_nodes = bvh.n_nodes;
     sc->info.depth = bvh.depth;
@@ -1080,6 +1118,8 @@ int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg
             return fail(ctx, GB_ERR_INVALID, "null scene, image gradient or parameter gradient");
         if (items[i].desc.max_bounces > kMaxAdjBounces)
             return fail(ctx, GB_ERR_INVALID, "the adjoint records at most 16 bounces per path");
+        if (items[i].scene->S.sky.light >= 0)
+            return fail(ctx, GB_ERR_UNSUPPORTED, "the adjoint covers scenes with rectangular lights only");
         v[i].scene = items[i].scene;
         v[i].cam = items[i].camera;
         v[i].desc = items[i].desc;

@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "../../include/gbpt.h"
 #include "gbpt_math.h"
@@ -116,9 +117,19 @@ static inline void pack_material(const MaterialRec& r, float* f) {
     f[22] = r.cc_a; f[23] = r.cc_a2m1; f[24] = r.cc_pilog;
 }
 
-// gi::light rect light with its fixed basis (arealight-sampler-cpu.cpp:70-73).
+// gi::light: a rect light with its fixed basis (arealight-sampler-cpu.cpp:70-73),
+// or a sky light with add-skylight's power rule scale * 4 pi (d / 2)^2
+// (lights.cpp:98-104).
 static inline LightRec make_light(const gb_light& l) {
     LightRec r;
+    std::memset(&r, 0, sizeof(r));
+    r.type = l.type == GB_LIGHT_SKY ? 1 : 0;
+    if (r.type == 1) {
+        r.scale = l.sky_scale;
+        float d = l.sky_diameter;
+        r.power = l.power >= 0.0f ? l.power : l.sky_scale * 4.0f * (float)M_PI * (d * 0.5f) * (d * 0.5f);
+        return r;
+    }
     r.center = mk(l.center[0], l.center[1], l.center[2]);
     r.dir = mk(l.dir[0], l.dir[1], l.dir[2]);
     r.col = mk(l.col[0], l.col[1], l.col[2]);
@@ -127,6 +138,54 @@ static inline LightRec make_light(const gb_light& l) {
     r.up = make_tangential(mk(0.0f, 1.0f, 0.0f), r.dir);
     r.power = l.power >= 0.0f ? l.power : rect_light_power(r.w, r.h, r.col);
     return r;
+}
+
+// Host copy of a sky map and its sampling tables (SkyRec's arrays).
+struct SkyTables {
+    std::vector<float> texel;    // 4 floats per texel (rgb, 0)
+    std::vector<float> row_cdf, row_pdf, col_cdf, col_pdf;
+    int w = 0, h = 0;
+};
+
+// Distribution1D::init (lights.h:28-45) in float: PDF = data / sum (0 when
+// the sum is 0), CDF[0] = 0, CDF[i] = CDF[i-1] + PDF[i-1], CDF[n] = 1.
+static inline float dist1d_init(const float* data, int n, float* pdf, float* cdf) {
+    float sum = 0.0f;
+    for (int i = 0; i < n; ++i) sum += data[i];
+    float scale = sum > 0.0f ? 1.0f / sum : 0.0f;
+    cdf[0] = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        pdf[i] = data[i] * scale;
+        if (i > 0) cdf[i] = cdf[i - 1] + pdf[i - 1];
+    }
+    cdf[n] = 1.0f;
+    return sum;
+}
+
+// sky_light::initSkylight (lights.h:100-110): importance of texel (x, y) =
+// sin(pi (y + 0.5) / h) * (r + g + b), one row distribution per row and a
+// distribution over the row sums (Distribution2D, lights.h:62-72).
+static inline void make_sky_tables(const float* rgb, int w, int h, SkyTables* t) {
+    t->w = w;
+    t->h = h;
+    t->texel.assign(4 * (size_t)w * h, 0.0f);
+    std::vector<float> imp((size_t)w * h);
+    for (int y = 0; y < h; ++y) {
+        float sy = std::sin((float)(M_PI * (y + 0.5f) / h));
+        for (int x = 0; x < w; ++x) {
+            const float* c = rgb + 3 * ((size_t)y * w + x);
+            for (int k = 0; k < 3; ++k) t->texel[4 * ((size_t)y * w + x) + k] = c[k];
+            imp[(size_t)y * w + x] = sy * ((c[0] + c[1]) + c[2]);
+        }
+    }
+    t->col_pdf.assign((size_t)w * h, 0.0f);
+    t->col_cdf.assign((size_t)(w + 1) * h, 0.0f);
+    std::vector<float> rows(h);
+    for (int y = 0; y < h; ++y)
+        rows[y] = dist1d_init(&imp[(size_t)y * w], w, &t->col_pdf[(size_t)y * w], &t->col_cdf[(size_t)y * (w + 1)]);
+    t->row_pdf.assign(h, 0.0f);
+    t->row_cdf.assign(h + 1, 0.0f);
+    dist1d_init(rows.data(), h, t->row_pdf.data(), t->row_cdf.data());
 }
 
 // hybrid-pt.cpp:74-78

@@ -33,6 +33,9 @@ namespace gb {
 namespace {
 
 constexpr int kBlock = 128;
+#ifndef GB_TRAV_MIN_BLOCKS
+#define GB_TRAV_MIN_BLOCKS 1  // resident blocks per SM the traversal kernels are compiled for
+#endif
 constexpr int kStack = 32;
 constexpr int kIterLimit = 1 << 22;
 
@@ -631,7 +634,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
 // contribution and end their path; hits draw the bounce's uniforms and emit
 // the area-light shadow ray (arealight-sampler-cpu.cpp:25-143).
 template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
+__global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     uint32_t* cn = ctr_set(F, it + 1);
@@ -660,7 +663,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
             if (!hit) {
                 float4 tp4 = F.tp[slot];
                 float4 acc = F.accum[slot];
-                v3 add = miss_contribution(ld3(tp4), R.sp);
+                v3 add = miss_contribution(ld3(tp4), ld3(F.ray_d[slot]), R.sp, &R.S.sky);
                 F.accum[slot] = make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f);
                 ended = true;
             } else {
@@ -684,8 +687,12 @@ __global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
                 if (S.n_lights > 0) {
                     int l = pick_light(S.lights, S.n_lights, S.overall_power, lr.z);
                     LightRec L = S.lights[l];
-                    rect_light_sample(L, S.lights_eval[l].col, S.overall_power, Pp, Nr, lr.x, lr.y,
-                                      R.sp.shadow_offset, &so, &sd, &smax, &psc, &scale);
+                    if (L.type == 1)
+                        sky_light_sample(S.sky, L.power, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset,
+                                         &so, &sd, &smax, &psc);
+                    else
+                        rect_light_sample(L, S.lights_eval[l].col, S.overall_power, Pp, Nr, lr.x, lr.y,
+                                          R.sp.shadow_offset, &so, &sd, &smax, &psc, &scale);
                 }
                 F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
                 F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
@@ -704,7 +711,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(Frame F, RenderParams P) {
 
 // Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
 template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock) k_shadow(Frame F, RenderParams P) {
+__global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     const uint32_t count = cs[2];
@@ -957,18 +964,25 @@ __global__ void k_nee_stage(DevScene S, int n, float shadow_offset, const float*
         v3 Pp = bary(h.y, h.z, ld3(sh[0]), ld3(sh[1]), ld3(sh[2]));
         v3 Nr = bary(h.y, h.z, ld3(sh[3]), ld3(sh[4]), ld3(sh[5]));
         v3 so, sd, ps; float sm;
-        rect_light_sample(S.lights[l], S.lights[l].col, S.overall_power, Pp, Nr, r.x, r.y, shadow_offset, &so, &sd,
-                          &sm, &ps);
+        if (S.lights[l].type == 1)
+            sky_light_sample(S.sky, S.lights[l].power, S.overall_power, Pp, Nr, r.x, r.y, shadow_offset, &so, &sd,
+                             &sm, &ps);
+        else
+            rect_light_sample(S.lights[l], S.lights[l].col, S.overall_power, Pp, Nr, r.x, r.y, shadow_offset, &so,
+                              &sd, &sm, &ps);
         ray_orig[3 * i] = so.x; ray_orig[3 * i + 1] = so.y; ray_orig[3 * i + 2] = so.z;
         ray_dir[3 * i] = sd.x; ray_dir[3 * i + 1] = sd.y; ray_dir[3 * i + 2] = sd.z;
         max_t[i] = sm;
         psc[3 * i] = ps.x; psc[3 * i + 1] = ps.y; psc[3 * i + 2] = ps.z;
     } else {
-        // arealight-sampler-cpu.cpp:121-142 without a sky light
+        // arealight-sampler-cpu.cpp:121-142: the ray is killed and psc is the
+        // (scaled) sky texel of the direction the buffer held, 0 without a sky
+        v3 d = mk(ray_dir[3 * i], ray_dir[3 * i + 1], ray_dir[3 * i + 2]);
+        v3 le = S.sky.light >= 0 ? S.sky.scale * sky_eval(S.sky, d) : mk(0.0f, 0.0f, 0.0f);
         ray_orig[3 * i] = FLT_MAX; ray_orig[3 * i + 1] = FLT_MAX; ray_orig[3 * i + 2] = FLT_MAX;
         ray_dir[3 * i] = 0.0f; ray_dir[3 * i + 1] = 0.0f; ray_dir[3 * i + 2] = 0.0f;
         max_t[i] = -1.0f;
-        psc[3 * i] = 0.0f; psc[3 * i + 1] = 0.0f; psc[3 * i + 2] = 0.0f;
+        psc[3 * i] = le.x; psc[3 * i + 1] = le.y; psc[3 * i + 2] = le.z;
     }
 }
 
@@ -1008,7 +1022,8 @@ __global__ void k_shade_stage(DevScene S, int n, ShadeParams sp, float* ray_orig
         }
     } else {
         // handle_no_hit (hybrid-pt.cpp:196-206); dead rays (max_t == -1) add 0
-        if (max_t[i] != -1.0f) ac = ac + miss_contribution(t, sp);
+        if (max_t[i] != -1.0f)
+            ac = ac + miss_contribution(t, mk(ray_dir[3 * i], ray_dir[3 * i + 1], ray_dir[3 * i + 2]), sp, &S.sky);
         ray_orig[3 * i] = FLT_MAX; ray_orig[3 * i + 1] = FLT_MAX; ray_orig[3 * i + 2] = FLT_MAX;
         ray_dir[3 * i] = 0.0f; ray_dir[3 * i + 1] = 0.0f; ray_dir[3 * i + 2] = 0.0f;
         max_t[i] = -1.0f;

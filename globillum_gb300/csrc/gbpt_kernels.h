@@ -24,6 +24,7 @@ struct DevScene {
     // lobes, pdfs and light picks still come from mats / lights)
     const float* mats_eval;
     const LightRec* lights_eval;
+    SkyRec sky;  // the scene's sky light (sky.light = -1 when it has none)
 };
 
 // The six 32-bit component words of a curandStateMRG32k3a (s1[3], s2[3]):

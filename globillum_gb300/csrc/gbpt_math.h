@@ -268,7 +268,132 @@ GB_HD void camera_ray(const CameraRec& c, int x, int y, float jx_r, float jy_r, 
 struct LightRec {
     v3 center, dir, col, right, up;
     float w, h, power;
+    int type;        // 0 rect, 1 sky (gi::light::type_t, lights.h:147-149)
+    float scale;     // sky: radiance scale (sky_light::scale)
 };
+
+// --------------------------------------------------------------- sky light --
+// atan / atan2 / acos from IEEE-exact operations: the Taylor series
+// atan(z) = z - z^3/3 + z^5/5 - ... (terms to z^17) on |z| <= tan(pi/12),
+// the addition formula atan(z) = pi/6 + atan((sqrt(3) z - 1) / (z + sqrt(3)))
+// above it, and atan(z) = pi/2 - atan(1/z) for z > 1.  Used only to find the
+// texel of a direction in a sky map.
+GB_HD float atan_pos(float z) {  // z >= 0
+    bool inv = z > 1.0f;
+    if (inv) z = 1.0f / z;
+    bool shift = z > 0.267949192f;  // tan(pi/12)
+    if (shift) z = (1.73205081f * z - 1.0f) / (z + 1.73205081f);
+    float z2 = z * z;
+    // q = -1/3 + z^2/5 - z^4/7 + ... + z^14/17, atan(z) = z (1 + z^2 q)
+    float q = 1.0f / 17.0f;
+    q = q * z2 - 1.0f / 15.0f;
+    q = q * z2 + 1.0f / 13.0f;
+    q = q * z2 - 1.0f / 11.0f;
+    q = q * z2 + 1.0f / 9.0f;
+    q = q * z2 - 1.0f / 7.0f;
+    q = q * z2 + 1.0f / 5.0f;
+    q = q * z2 - 1.0f / 3.0f;
+    float a = z + z * (z2 * q);
+    if (shift) a = a + 0.523598776f;  // pi/6
+    if (inv) a = 1.57079633f - a;     // pi/2
+    return a;
+}
+GB_HD float atan2_ex(float y, float x) {
+    if (x == 0.0f && y == 0.0f) return 0.0f;
+    float ax = fabsf(x), ay = fabsf(y);
+    float a = ax >= ay ? atan_pos(ay / ax) : 1.57079633f - atan_pos(ax / ay);
+    if (x < 0.0f) a = 3.14159265f - a;
+    return y < 0.0f ? -a : a;
+}
+GB_HD float acos_ex(float x) {
+    x = fminf(1.0f, fmaxf(-1.0f, x));
+    return atan2_ex(sqrtf((1.0f - x) * (1.0f + x)), x);
+}
+
+// A lat-long radiance map (rows theta = 0 .. pi, columns phi = 0 .. 2 pi)
+// with the two-level sampling tables of Distribution2D (lights.h:18-90):
+// a row CDF/PDF over the summed row importance and one column CDF/PDF per
+// row, built on the host (gbpt_host.h, make_sky_tables).
+struct SkyRec {
+    const float* texel;    // w*h radiance, 4 floats per texel (rgb, 0)
+    const float* row_cdf;  // h + 1
+    const float* row_pdf;  // h
+    const float* col_cdf;  // h * (w + 1)
+    const float* col_pdf;  // h * w
+    int w, h;
+    float scale;
+    int light;             // index of the sky light, -1 = none
+};
+
+// Distribution1D::sample (lights.h:49-56): index with CDF[i] <= u < CDF[i+1]
+// (upper_bound - 1, clamped), then x = (1 - t) i + t (i + 1) with
+// t = (CDF[i+1] - u) / (CDF[i+1] - CDF[i]) as written there.
+GB_HD void dist1d_sample(const float* cdf, const float* pdf, int n, float u, float* x, float* p) {
+    int lo = 0, hi = n;
+    while (lo < hi) {  // upper_bound over cdf[0 .. n-1]
+        int mid = (lo + hi) >> 1;
+        if (cdf[mid] <= u) lo = mid + 1;
+        else hi = mid;
+    }
+    int idx = lo - 1;
+    idx = idx < 0 ? 0 : (idx > n - 1 ? n - 1 : idx);
+    float t = (cdf[idx + 1] - u) / (cdf[idx + 1] - cdf[idx]);
+    *x = (1.0f - t) * float(idx) + t * float(idx + 1);
+    *p = pdf[idx];
+}
+
+// sky_light::sample (lights.h:107-126) with Distribution2D::sample
+// (lights.h:73-79): (u, v) from the tables, direction
+// (sin t cos p, sin t sin p, cos t) for t = u pi / h, p = v 2 pi / w, pdf
+// (pdf_row pdf_col w h) / (2 pi^2 sin t), radiance of texel (int u, int v).
+GB_HD v3 sky_sample(const SkyRec& s, float ru, float rv, float* pdf_out, v3* dir) {
+    float u, v, pu, pv;
+    dist1d_sample(s.row_cdf, s.row_pdf, s.h, ru, &u, &pu);
+    int yi = (int)u;
+    yi = yi < 0 ? 0 : (yi > s.h - 1 ? s.h - 1 : yi);
+    dist1d_sample(s.col_cdf + (size_t)yi * (s.w + 1), s.col_pdf + (size_t)yi * s.w, s.w, rv, &v, &pv);
+    float st, ct, sp, cp;
+    sincos_2pi(u * (0.5f / float(s.h)), &st, &ct);
+    sincos_2pi(v / float(s.w), &sp, &cp);
+    *dir = mk(st * cp, st * sp, ct);
+    *pdf_out = (pu * pv * float(s.w * s.h)) / (19.7392088f * st);  // 2 pi^2
+    int xi = (int)v;
+    xi = xi < 0 ? 0 : (xi > s.w - 1 ? s.w - 1 : xi);
+    const float* t = s.texel + 4 * ((size_t)yi * s.w + xi);
+    return mk(t[0], t[1], t[2]);
+}
+
+// evaluateSkyLight (hybrid-pt.cpp:175-189): the texel of a direction,
+// theta = acos(d.y), phi = atan2(d.z, d.x) in [0, 2 pi); no scale applied.
+GB_HD v3 sky_eval(const SkyRec& s, v3 d) {
+    float theta = acos_ex(d.y);
+    float phi = atan2_ex(d.z, d.x);
+    if (phi < 0.0f) phi += 6.28318531f;
+    float su = phi / 6.28318531f, tv = theta / 3.14159265f;
+    long long idx = (long long)(int)(tv * float(s.h)) * s.w + (int)(su * float(s.w));
+    if (idx < 0 || idx >= (long long)s.h * s.w) return mk(0.0f, 0.0f, 0.0f);
+    const float* t = s.texel + 4 * idx;
+    return mk(t[0], t[1], t[2]);
+}
+
+// Sky branch of pixel_generate_arealight_sample_cpu with USE_SKY_SAMPLING
+// (arealight-sampler-cpu.cpp:87-96, 113-119): the sampled direction is
+// mapped around the (unnormalised) normal with make_tangential, weighted by
+// scale / pdf * |dir . N|; the shadow ray is unbounded.
+GB_HD void sky_light_sample(const SkyRec& s, float power, float overall_power, v3 P, v3 N, float rx, float ry,
+                            float shadow_offset, v3* so, v3* sd, float* smax, v3* psc) {
+    float pdf;
+    v3 dir;
+    v3 L = sky_sample(s, rx, ry, &pdf, &dir);
+    dir = make_tangential(dir, N);
+    float a = 1.0f / pdf;
+    v3 contribution = (s.scale * L) * (a * fabsf(dot(dir, N)));
+    dir = normalize_div(dir);
+    *so = P + shadow_offset * dir;
+    *sd = dir;
+    *smax = FLT_MAX;
+    *psc = contribution * (overall_power / power);
+}
 
 // lights.cpp:92: power = w*h*(r+g+b)*.333
 GB_HD float rect_light_power(float w, float h, v3 col) {
@@ -748,10 +873,13 @@ GB_HD ShadeOut shade_hit(const MaterialRec& m, v3 P, v3 Nraw, v3 ray_dir, v3 tp,
 }
 
 // handle_no_hit (hybrid-pt.cpp:196-206, :567-575): primary misses are
-// recognised by throughput == (1,1,1); no sky light is modelled, so other
-// misses add throughput * 0.
-GB_HD v3 miss_contribution(v3 tp, const ShadeParams& sp) {
+// recognised by throughput == (1,1,1) and add the background; other misses
+// add throughput * the sky texel of the normalised ray direction
+// (evaluateSkyLight, hybrid-pt.cpp:175-189, unscaled), or nothing when the
+// scene has no sky light.
+GB_HD v3 miss_contribution(v3 tp, v3 ray_dir, const ShadeParams& sp, const SkyRec* sky = nullptr) {
     if (tp.x == 1.0f && tp.y == 1.0f && tp.z == 1.0f) return tp * sp.background;
+    if (sky && sky->light >= 0) return tp * sky_eval(*sky, normalize_div(ray_dir));
     return tp * mk(0.0f, 0.0f, 0.0f);
 }
 

@@ -37,7 +37,8 @@ class Material(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("type", C.c_int), ("power", C.c_float), ("center", F3), ("dir", F3), ("up", F3), ("col", F3),
-                ("wh", C.c_float * 2)]
+                ("wh", C.c_float * 2), ("sky_rgb", C.c_void_p), ("sky_w", C.c_int), ("sky_h", C.c_int),
+                ("sky_scale", C.c_float), ("sky_diameter", C.c_float)]
 
 
 class SceneDesc(C.Structure):
@@ -212,13 +213,22 @@ def make_scene_desc(scene) -> tuple[SceneDesc, list]:
             ("anisotropic", 0), ("sheen", 0), ("sheen_tint", 0), ("clearcoat", 0), ("clearcoat_gloss", 0),
             ("opacity", 1), ("transmiss", 1))], _f3(p.get("color", (0, 0, 0))), _f3(p.get("tangent", (0, 0, 0))))
     lights = (Light * max(1, len(scene.lights)))()
+    maps = []
     for i, l in enumerate(scene.lights):
-        lights[i] = Light(int(l.get("type", GB_LIGHT_RECT)), float(l.get("power", -1.0)), _f3(l["center"]),
-                          _f3(l["dir"]), _f3(l.get("up", (0, 0, 1))), _f3(l["col"]),
-                          (C.c_float * 2)(*[float(x) for x in l["wh"]]))
+        t = int(l.get("type", GB_LIGHT_RECT))
+        if t == GB_LIGHT_SKY:
+            # sky: {"type": 1, "map": (h, w, 3) float32 radiance, "scale": s, "diameter": d, "power": -1}
+            m = None if l.get("map") is None else np.ascontiguousarray(l["map"], np.float32)
+            maps.append(m)
+            lights[i] = Light(t, float(l.get("power", -1.0)), F3(), F3(), F3(), F3(), (C.c_float * 2)(),
+                              _ptr(m), 0 if m is None else int(m.shape[1]), 0 if m is None else int(m.shape[0]),
+                              float(l.get("scale", 1.0)), float(l.get("diameter", 1.0)))
+        else:
+            lights[i] = Light(t, float(l.get("power", -1.0)), _f3(l["center"]), _f3(l["dir"]),
+                              _f3(l.get("up", (0, 0, 1))), _f3(l["col"]), (C.c_float * 2)(*[float(x) for x in l["wh"]]))
     d = SceneDesc(int(pos.shape[0]), _ptr(pos), _ptr(nrm), _ptr(mid), len(scene.materials), mats,
                   len(scene.params), params, len(scene.lights), lights)
-    return d, [pos, nrm, mid, mats, params, lights]
+    return d, [pos, nrm, mid, mats, params, lights, maps]
 
 
 class Context:

@@ -231,6 +231,26 @@ def icospheres(n_spheres: int = 800, level: int = 3, width: int = 1280, height: 
                      name=f"icospheres-{n_spheres}x{nf}+10tri")
 
 
+def procedural_sky(width: int = 64, height: int = 32, sun=(0.35, 0.2), seed: int = 0) -> np.ndarray:
+    """A lat-long sky radiance map (height rows theta 0..pi, width columns
+    phi 0..2 pi, float RGB): a blue-to-white gradient over the upper
+    hemisphere, a dim ground, a small bright sun at (theta, phi) / pi,
+    2 pi = `sun`, and seeded low-amplitude texel noise.  Stands in for the
+    HDR maps add-skylight loads."""
+    rng = np.random.default_rng(seed)
+    th = (np.arange(height) + 0.5) / height * np.pi
+    ph = (np.arange(width) + 0.5) / width * 2 * np.pi
+    T, Ph = np.meshgrid(th, ph, indexing="ij")
+    up = np.clip(np.cos(T), 0.0, 1.0)[..., None]
+    sky = up * np.array([0.3, 0.5, 1.0]) + (1 - up) * np.array([0.9, 0.9, 0.95])
+    sky = np.where((T < np.pi / 2)[..., None], sky, np.array([0.15, 0.12, 0.1]))
+    st, sp = sun[0] * np.pi, sun[1] * 2 * np.pi
+    d2 = (T - st) ** 2 + (np.angle(np.exp(1j * (Ph - sp)))) ** 2
+    sky = sky + (np.exp(-d2 / (2 * 0.08 ** 2)) * 40.0)[..., None] * np.array([1.0, 0.9, 0.7])
+    sky = sky * (1.0 + 0.05 * rng.standard_normal(sky.shape))
+    return np.clip(sky, 0.0, None).astype(np.float32)
+
+
 def param_vector(scene: SceneData) -> np.ndarray:
     """The scene's differentiable parameters in gb_scene_param_count order:
     per material base colour, roughness, metallic; per light emission."""
@@ -242,7 +262,7 @@ def param_vector(scene: SceneData) -> np.ndarray:
         else:
             out += list(m["diffuse"]) + [0.0, 0.0]
     for l in scene.lights:
-        out += list(l["col"])
+        out += list(l.get("col", (0.0, 0.0, 0.0)))
     return np.array(out, np.float32)
 
 

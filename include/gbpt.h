@@ -77,13 +77,22 @@ typedef struct {
 } gb_material;
 
 enum { GB_LIGHT_RECT = 0, GB_LIGHT_SKY = 1 };
-/* gi::light / rect_light (lights.h:94-154).  power < 0 means "compute it
- * with the add-rectlight rule" w*h*(r+g+b)*.333 (lights.cpp:92). */
+/* gi::light with rect_light / sky_light (lights.h:94-154).
+ * Rect: center, dir, up, col, wh; power < 0 means "compute it with the
+ * add-rectlight rule" w*h*(r+g+b)*.333 (lights.cpp:92).
+ * Sky: sky_rgb is a lat-long radiance map of sky_h rows (theta 0 .. pi) by
+ * sky_w columns (phi 0 .. 2 pi), float RGB, copied at scene creation (the
+ * texture add-skylight loads, lights.cpp:98-111); sky_scale scales the
+ * light samples; power < 0 means scale * 4 pi (sky_diameter / 2)^2
+ * (lights.cpp:104).  At most one sky light per scene. */
 typedef struct {
     int type;
     float power;
     float center[3], dir[3], up[3], col[3];
     float wh[2];
+    const float* sky_rgb;
+    int sky_w, sky_h;
+    float sky_scale, sky_diameter;
 } gb_light;
 
 typedef struct {

@@ -63,6 +63,9 @@ struct OScene {
     bool use_bvh = true;
     std::vector<ONode> nodes;
     std::vector<int> idx;
+    // sky light tables (sky.light = -1 without one)
+    SkyTables sky_tab;
+    SkyRec sky{};
     // descriptions the differentiable parameters come from
     std::vector<gb_material> mats_in;
     std::vector<gb_principled_params> params_in;
@@ -259,20 +262,26 @@ inline v3 tri_interp(const std::vector<float>& a, int t, float beta, float gamma
     return bary(beta, gamma, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]));
 }
 
-// pixel_generate_arealight_sample_cpu (arealight-sampler-cpu.cpp:25-143)
-// without a sky light.
+// pixel_generate_arealight_sample_cpu (arealight-sampler-cpu.cpp:25-143).
+// *sd holds the buffer's direction on entry (read by the miss branch).
 void nee_pixel(const OScene& s, int id, const gb_hit& h, v3 rnd, float shadow_offset, v3* so, v3* sd, float* smax,
                v3* psc) {
     if (h.ref != 0xffffffffu && !s.lights.empty()) {
         int l = pick_light(s.lights.data(), (int)s.lights.size(), s.overall, rnd.z);
         v3 P = tri_interp(s.pos, (int)h.ref, h.beta, h.gamma);
         v3 N = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
-        rect_light_sample(s.lights[l], s.lights[l].col, s.overall, P, N, rnd.x, rnd.y, shadow_offset, so, sd, smax, psc);
+        if (s.lights[l].type == 1)
+            sky_light_sample(s.sky, s.lights[l].power, s.overall, P, N, rnd.x, rnd.y, shadow_offset, so, sd, smax,
+                             psc);
+        else
+            rect_light_sample(s.lights[l], s.lights[l].col, s.overall, P, N, rnd.x, rnd.y, shadow_offset, so, sd,
+                              smax, psc);
     } else {
+        v3 d = *sd;
         *so = mk(FLT_MAX, FLT_MAX, FLT_MAX);
         *sd = mk(0.0f, 0.0f, 0.0f);
         *smax = -1.0f;
-        *psc = mk(0.0f, 0.0f, 0.0f);
+        *psc = s.sky.light >= 0 ? s.sky.scale * sky_eval(s.sky, d) : mk(0.0f, 0.0f, 0.0f);
     }
     (void)id;
 }
@@ -426,7 +435,25 @@ void* orc_scene_create(int n, const float* pos, const float* nrm, const int* mat
         pack_material(make_material(mats[m], params), f);
         s->mats.push_back(unpack_material(f));
     }
-    for (int l = 0; l < nl; ++l) s->lights.push_back(make_light(lights[l]));
+    s->sky.light = -1;
+    for (int l = 0; l < nl; ++l) {
+        s->lights.push_back(make_light(lights[l]));
+        if (lights[l].type == GB_LIGHT_SKY && lights[l].sky_rgb && lights[l].sky_w > 0 && lights[l].sky_h > 0) {
+            make_sky_tables(lights[l].sky_rgb, lights[l].sky_w, lights[l].sky_h, &s->sky_tab);
+            s->sky.light = l;
+        }
+    }
+    if (s->sky.light >= 0) {
+        SkyTables& t = s->sky_tab;
+        s->sky.texel = t.texel.data();
+        s->sky.row_cdf = t.row_cdf.data();
+        s->sky.row_pdf = t.row_pdf.data();
+        s->sky.col_cdf = t.col_cdf.data();
+        s->sky.col_pdf = t.col_pdf.data();
+        s->sky.w = t.w;
+        s->sky.h = t.h;
+        s->sky.scale = s->lights[s->sky.light].scale;
+    }
     s->overall = overall_power(s->lights.data(), (int)s->lights.size());
     s->mats_in.assign(mats, mats + nmat);
     if (nparams > 0 && params) s->params_in.assign(params, params + nparams);
@@ -472,7 +499,8 @@ int orc_generate_arealight_sample(void* sp, int w, int h, float shadow_offset, c
     for (int y = 0; y < h; ++y)
         for (int x = 0; x < w; ++x) {
             int id = y * w + x;
-            v3 so, sd, ps; float sm;
+            v3 so, ps; float sm;
+            v3 sd = mk(ray_dir[3 * id], ray_dir[3 * id + 1], ray_dir[3 * id + 2]);
             nee_pixel(s, id, hits[id], mk(rnd[3 * id], rnd[3 * id + 1], rnd[3 * id + 2]), shadow_offset, &so, &sd, &sm, &ps);
             ray_orig[3 * id] = so.x; ray_orig[3 * id + 1] = so.y; ray_orig[3 * id + 2] = so.z;
             ray_dir[3 * id] = sd.x; ray_dir[3 * id + 1] = sd.y; ray_dir[3 * id + 2] = sd.z;
@@ -516,7 +544,9 @@ int orc_compute_path_contribution_and_bounce(void* sp, int w, int h, const gb_re
                     max_t[id] = FLT_MAX;
                 }
             } else {
-                if (max_t[id] != -1.0f) ac = ac + miss_contribution(t, par);
+                if (max_t[id] != -1.0f)
+                    ac = ac + miss_contribution(t, mk(ray_dir[3 * id], ray_dir[3 * id + 1], ray_dir[3 * id + 2]), par,
+                                                &s.sky);
                 t = mk(0.0f, 0.0f, 0.0f);
             }
             if (!alive) {
@@ -641,6 +671,7 @@ int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int
     if (row0 < 0 || row1 > H || row0 >= row1) return 1;
     if (pool_updates < d->spp * L) return 2;
     if (cam->aperture != 0.0f && (row0 != 0 || row1 != H)) return 3;
+    if (s.sky.light >= 0) return 4;  // the adjoint covers rect lights only
     const int n = W * (row1 - row0), base = row0 * W;
     const int nm = (int)s.mats_in.size();
     CameraRec C = make_camera(*cam, W, H);
@@ -803,6 +834,23 @@ int orc_mrg_jump(unsigned long long steps, uint32_t* s1, uint32_t* s2) {
     uint32_t J1[9], J2[9];
     mrg_jump_matrices(steps, J1, J2);
     mrg_jump(s1, s2, J1, J2);
+    return 0;
+}
+
+// The shared atan2 / acos (sky texel lookup) for accuracy tests.
+int orc_atan2_acos(int n, const float* y, const float* x, float* atan2_out, float* acos_out) {
+    for (int i = 0; i < n; ++i) {
+        atan2_out[i] = atan2_ex(y[i], x[i]);
+        acos_out[i] = acos_ex(x[i]);
+    }
+    return 0;
+}
+
+// Distribution1D::init + sample on the host tables (sky sampling tests).
+int orc_dist1d(int n, const float* data, int m, const float* u, float* x, float* p) {
+    std::vector<float> pdf(n), cdf(n + 1);
+    dist1d_init(data, n, pdf.data(), cdf.data());
+    for (int i = 0; i < m; ++i) dist1d_sample(cdf.data(), pdf.data(), n, u[i], &x[i], &p[i]);
     return 0;
 }
 

@@ -43,6 +43,8 @@ def load() -> C.CDLL:
         lib.orc_sincos_2pi.argtypes = [ip, vp, vp, vp]
         lib.orc_shade_eval.argtypes = [vp] * 7
         lib.orc_mrg_jump.argtypes = [C.c_ulonglong, vp, vp]
+        lib.orc_atan2_acos.argtypes = [ip, vp, vp, vp, vp]
+        lib.orc_dist1d.argtypes = [ip, vp, ip, vp, vp, vp]
         lib.orc_threads.restype = ip
         lib.orc_set_threads.argtypes = [ip]
         lib.orc_set_threads.restype = None
@@ -207,6 +209,26 @@ def mrg_jump(steps: int, s1, s2):
     b = np.ascontiguousarray(s2, np.uint32).copy()
     load().orc_mrg_jump(int(steps), _p(a), _p(b))
     return a, b
+
+
+def atan2_acos(y, x):
+    """The shared atan2_ex(y, x) and acos_ex(x)."""
+    y = np.ascontiguousarray(y, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    a = np.empty_like(x)
+    c = np.empty_like(x)
+    load().orc_atan2_acos(x.shape[0], _p(y), _p(x), _p(a), _p(c))
+    return a, c
+
+
+def dist1d(data, u):
+    """Distribution1D init on `data` and samples at `u`: (x, pdf)."""
+    d = np.ascontiguousarray(data, np.float32)
+    u = np.ascontiguousarray(u, np.float32)
+    x = np.empty_like(u)
+    p = np.empty_like(u)
+    load().orc_dist1d(d.shape[0], _p(d), u.shape[0], _p(u), _p(x), _p(p))
+    return x, p
 
 
 def threads() -> int:

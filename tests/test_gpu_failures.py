@@ -37,9 +37,12 @@ def test_bad_scenes_are_rejected(gpu_ctx):
     rc, _, _ = _create(gpu_ctx, bad)
     _expect(gpu_ctx, rc, gbpt.GB_ERR_INVALID, "material index")
     bad = scenes.cornell()
-    bad.lights = [dict(bad.lights[0], type=gbpt.GB_LIGHT_SKY)]
+    bad.lights = [dict(bad.lights[0], type=gbpt.GB_LIGHT_SKY)]  # a sky light without a map
     rc, _, _ = _create(gpu_ctx, bad)
-    _expect(gpu_ctx, rc, gbpt.GB_ERR_UNSUPPORTED)
+    _expect(gpu_ctx, rc, gbpt.GB_ERR_INVALID, "valid map")
+    bad.lights = [dict(bad.lights[0], type=7)]
+    rc, _, _ = _create(gpu_ctx, bad)
+    _expect(gpu_ctx, rc, gbpt.GB_ERR_UNSUPPORTED, "light type")
     # the context still renders
     scene = gpu_ctx.scene(sc)
     img = scene.render(sc.camera, sc.render)

@@ -143,3 +143,38 @@ def test_ingested_obj_scene_frame(gpu_ctx):
     ref = oracle.OracleScene(sd, use_bvh=False).render(cam, rd, pool)
     _compare(img, ref)
     assert img.mean() > 1e-3
+
+
+def test_sky_light_frame(gpu_ctx):
+    """A rect light plus a sky light: sky NEE samples (importance-sampled
+    lat-long map) and sky lookups of secondary misses, against the oracle."""
+    sc = scenes.icospheres(n_spheres=20, level=2, box=12.0, width=48, height=32, spp=3, max_bounces=4, n_lights=1,
+                           rr_start=-1)
+    sc.lights.append({"type": gbpt.GB_LIGHT_SKY, "map": scenes.procedural_sky(64, 32), "scale": 0.5,
+                      "diameter": 30.0, "power": -1.0})
+    for mode in (gbpt.GB_RNG_MRG32K3A_POOL, gbpt.GB_RNG_HALTON_LIGHT):
+        rd = dict(sc.render, rng_mode=mode)
+        img, ref = _render_pair(gpu_ctx, sc, rd)
+        _compare(img, ref)
+        assert img.mean() > 1e-3
+
+
+def test_sky_light_errors(gpu_ctx):
+    sc = scenes.icospheres(n_spheres=4, level=1, box=6.0, width=16, height=16, spp=1, max_bounces=2, n_lights=1)
+    sky = {"type": gbpt.GB_LIGHT_SKY, "map": scenes.procedural_sky(16, 8), "scale": 1.0, "diameter": 10.0,
+           "power": -1.0}
+    two = scenes.SceneData(sc.positions, sc.normals, sc.material_index, sc.materials, sc.params,
+                           sc.lights + [sky, dict(sky)], sc.camera, sc.render)
+    with pytest.raises(gbpt.GBError, match="one sky"):
+        gpu_ctx.scene(two)
+    bad = dict(sky, map=np.full((8, 16, 3), np.nan, np.float32))
+    nan = scenes.SceneData(sc.positions, sc.normals, sc.material_index, sc.materials, sc.params,
+                           sc.lights + [bad], sc.camera, sc.render)
+    with pytest.raises(gbpt.GBError, match="finite"):
+        gpu_ctx.scene(nan)
+    ok = scenes.SceneData(sc.positions, sc.normals, sc.material_index, sc.materials, sc.params,
+                          sc.lights + [sky], sc.camera, sc.render)
+    s = gpu_ctx.scene(ok)
+    with pytest.raises(gbpt.GBError, match="rectangular"):
+        s.backward(sc.camera, sc.render, np.zeros((16, 16, 3), np.float32))
+    s.close()
