@@ -567,6 +567,10 @@ def run_gbpt(args, rank, world):
             "mrays_per_s": mrays,
             "rays_per_frame": {"camera": ist["camera_rays"], "extension": ist["extension_rays"],
                                "shadow": ist["shadow_rays"]},
+            "traversal_per_ray": {"closest_node_visits": ist["closest_node_visits"] / max(1, ext_rays),
+                                  "closest_tri_tests": ist["closest_tri_tests"] / max(1, ext_rays),
+                                  "shadow_node_visits": ist["shadow_node_visits"] / max(1, ist["shadow_rays"]),
+                                  "shadow_tri_tests": ist["shadow_tri_tests"] / max(1, ist["shadow_rays"])},
             "stage_ms_per_frame": {"path_start": stage_ms[0], "closest_hit+light_sample": ext_ms,
                                    "any_hit": stage_ms[2], "shade": stage_ms[3], "path_end+restart": stage_ms[4],
                                    "moving_average": stage_ms[5], "frame_ms_with_stage_events": stage_frame_ms},

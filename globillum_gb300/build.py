@@ -69,7 +69,8 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp", CSRC / "gbpt_ingest.cpp"]
     deps = cu + cpp + _sources()
     # the library records the build-time defines it was made with
-    flags = f"GB_TRAV_MIN_BLOCKS={os.environ.get('GBPT_TRAV_MIN_BLOCKS', '')}"
+    flags = (f"GB_TRAV_MIN_BLOCKS={os.environ.get('GBPT_TRAV_MIN_BLOCKS', '')} "
+             f"GB_WIDE_STREAM_GRIDS={os.environ.get('GBPT_WIDE_STREAM_GRIDS', '')}")
     stamp = LIB.with_suffix(".flags")
     if not stamp.exists() or stamp.read_text() != flags:
         force = True
@@ -83,10 +84,13 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
         c = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
              "-Xcompiler", "-ffp-contract=off", "-c", str(s), "-o", str(o)]
         # GBPT_TRAV_MIN_BLOCKS: resident 128-thread blocks per SM the traversal
-        # kernels are compiled for (register budget); 1 = the compiler's choice
+        # kernels are compiled for (register budget; default 7)
         mb = os.environ.get("GBPT_TRAV_MIN_BLOCKS")
         if mb:
             c.insert(1, f"-DGB_TRAV_MIN_BLOCKS={int(mb)}")
+        # GBPT_WIDE_STREAM_GRIDS=1: one thread per slot for k_shade / k_regen
+        if os.environ.get("GBPT_WIDE_STREAM_GRIDS"):
+            c.insert(1, f"-DGB_WIDE_STREAM_GRIDS={int(os.environ['GBPT_WIDE_STREAM_GRIDS'])}")
         if verbose_ptxas:
             c.insert(1, "-Xptxas=-v")
         cmds.append(c)

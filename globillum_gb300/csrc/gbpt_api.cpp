@@ -1251,7 +1251,7 @@ int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, i
         {&gb_tuning::graph, {1, 2}},
         {&gb_tuning::slots, {1 << 18, 1 << 19, 1 << 20, 1 << 21}},
         {&gb_tuning::refill, {8, 16, 24, 32}},
-        {&gb_tuning::tri_mode, {1, 2, 3}},
+        {&gb_tuning::tri_mode, {1, 2, 3, 4}},
         {&gb_tuning::blocks_per_sm, {1, 3, 4, 5, 6}},
     };
     for (int pass = 0; pass < 2; ++pass) {
@@ -1286,6 +1286,36 @@ int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, i
     return GB_OK;
 }
 
+int gb_render_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* d,
+                     int light_samples, float* out_rgb, int out_is_device) {
+    if (!ctx || !scene) return fail(ctx, GB_ERR_INVALID, "null context or scene");
+    int rc = check_render_desc(ctx, cam, d);
+    if (rc != GB_OK) return rc;
+    if (light_samples <= 0 || light_samples > (1 << 20)) return fail(ctx, GB_ERR_INVALID, "bad light sample count");
+    if (!out_rgb) return fail(ctx, GB_ERR_INVALID, "null output");
+    CK(cudaSetDevice(ctx->device));
+    const int n = d->width * d->height;
+    const size_t bytes = sizeof(float) * 3 * (size_t)n;
+    float* dst = out_rgb;
+    if (!out_is_device) {
+        CK(ensure_scratch(ctx, 0, bytes));
+        dst = (float*)ctx->scratch[0].p;
+    }
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    CK(k_launch_direct(scene->S, make_camera(*cam, d->width, d->height), d->width, d->height, light_samples, d->seed,
+                       d->shadow_offset, mk(d->background[0], d->background[1], d->background[2]), dst,
+                       ctx->d_status, ctx->stream));
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (!out_is_device) CK(cudaMemcpyAsync(out_rgb, dst, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->stats.render_ms = ms;
+    ctx->stats.kernel_launches = 1;
+    cudaGetLastError();
+    return check_status(ctx);
+}
+
 int gb_get_stats(const gb_ctx* ctx, gb_stats* stats) {
     if (!ctx || !stats) return GB_ERR_INVALID;
     *stats = ctx->stats;
@@ -1301,7 +1331,7 @@ int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* t) {
     if (!ctx || !t) return fail(ctx, GB_ERR_INVALID, "null argument");
     if (t->refill < 0 || t->refill > 32) return fail(ctx, GB_ERR_INVALID, "refill must be in 1..32");
     if (t->slots < 0 || t->sample_mb < 0) return fail(ctx, GB_ERR_INVALID, "negative tuning value");
-    if (t->tri_mode < 0 || t->tri_mode > 3) return fail(ctx, GB_ERR_INVALID, "tri_mode must be 1..3 (0 keeps)");
+    if (t->tri_mode < 0 || t->tri_mode > 4) return fail(ctx, GB_ERR_INVALID, "tri_mode must be 1..4 (0 keeps)");
     if (t->graph < 0 || t->graph > 2) return fail(ctx, GB_ERR_INVALID, "graph must be 1 or 2 (0 keeps)");
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 65)
         return fail(ctx, GB_ERR_INVALID, "blocks_per_sm must be 1..65 (0 keeps)");

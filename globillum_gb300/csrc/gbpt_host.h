@@ -18,6 +18,7 @@ namespace gb {
 static inline MaterialRec make_material(const gb_material& m, const gb_principled_params* params) {
     MaterialRec r;
     std::memset(&r, 0, sizeof(r));
+    for (int k = 0; k < 3; ++k) r.kd[k] = m.diffuse[k];
     if (m.principled < 0) {
         r.kind = MAT_LAMBERT;
         for (int k = 0; k < 3; ++k) r.diffuse[k] = m.diffuse[k];
@@ -115,6 +116,7 @@ static inline void pack_material(const MaterialRec& r, float* f) {
     f[8] = r.clearcoat; f[9] = r.opacity; f[10] = r.ax; f[11] = r.ay; f[12] = r.roughg2;
     for (int k = 0; k < 3; ++k) { f[13 + k] = r.cdlin[k]; f[16 + k] = r.csheen[k]; f[19 + k] = r.cspec0[k]; }
     f[22] = r.cc_a; f[23] = r.cc_a2m1; f[24] = r.cc_pilog;
+    f[25] = r.kd[0]; f[26] = r.kd[1]; f[27] = r.kd[2];
 }
 
 // gi::light: a rect light with its fixed basis (arealight-sampler-cpu.cpp:70-73),

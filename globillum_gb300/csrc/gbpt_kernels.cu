@@ -33,8 +33,12 @@ namespace gb {
 namespace {
 
 constexpr int kBlock = 128;
+// Resident 128-thread blocks per SM the traversal kernels are compiled for:
+// 7 (72 registers, 28 warps per SM) measured fastest on the 1 M-triangle
+// frame (8 blocks spill more; the compiler's own choice of 80 registers
+// gives 6 blocks).
 #ifndef GB_TRAV_MIN_BLOCKS
-#define GB_TRAV_MIN_BLOCKS 1  // resident blocks per SM the traversal kernels are compiled for
+#define GB_TRAV_MIN_BLOCKS 7
 #endif
 constexpr int kStack = 32;
 constexpr int kIterLimit = 1 << 22;
@@ -529,6 +533,91 @@ __global__ void k_step(Frame F, RenderParams P, unsigned long long cond, int has
     if (has_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, (next != 0u && it + 1 < max_iters) ? 1u : 0u);
 }
 
+// (t, canonical id) as one 64-bit key whose unsigned order is the
+// lexicographic closest-hit order: t > 0, so its bits order like its value.
+__device__ __forceinline__ unsigned long long hit_key(float t, uint32_t id) {
+    return ((unsigned long long)__float_as_uint(t) << 32) | id;
+}
+
+// Warp-cooperative triangle phase (triangle policy 3): the pending triangles
+// of all active lanes are tested by the whole warp, 32 at a time.  A warp
+// scan of the per-lane counts numbers the (lane, triangle) pairs; tester
+// lane g finds its owner (the last lane whose exclusive count is <= g), the
+// owner's k-th pending triangle, and the owner's ray through shuffles.  Hits
+// resolve per owner by an atomicMin of hit_key in shared memory, so the
+// result is the same lexicographic minimum as testing sequentially.  A new
+// closest hit's barycentrics are recomputed by its owner from the shading
+// record with the same (v0, v1 - v0, v2 - v0) arithmetic as the triangle
+// layout, so they are bit-identical too.  All 32 lanes must call this.
+template <bool ANY, bool INSTR>
+__device__ __forceinline__ bool coop_triangles(bool act, const float4* tris, const float4* shade, const RayInv& r,
+                                               float tmax, Trav& s, unsigned long long* skey, uint32_t* ntri) {
+    const uint32_t lane = lane_id();
+    const uint32_t cnt = act ? (uint32_t)__popc(s.tg.y) : 0u;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0u) return false;
+    const uint32_t excl = incl - cnt;
+    const unsigned long long mine = act ? hit_key(s.best_t, s.best_id) : ~0ull;
+    skey[lane] = mine;
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t g = base + lane;
+        uint32_t o = 0;
+#pragma unroll
+        for (uint32_t step = 16; step >= 1; step >>= 1) {
+            uint32_t c = o + step;
+            if (__shfl_sync(0xffffffffu, excl, (int)c) <= g) o = c;
+        }
+        const uint32_t om = __shfl_sync(0xffffffffu, s.tg.y, (int)o);
+        const uint32_t ob = __shfl_sync(0xffffffffu, s.tg.x, (int)o);
+        const uint32_t oe = __shfl_sync(0xffffffffu, excl, (int)o);
+        const v3 ro = mk(__shfl_sync(0xffffffffu, r.o.x, (int)o), __shfl_sync(0xffffffffu, r.o.y, (int)o),
+                         __shfl_sync(0xffffffffu, r.o.z, (int)o));
+        const v3 rd = mk(__shfl_sync(0xffffffffu, r.d.x, (int)o), __shfl_sync(0xffffffffu, r.d.y, (int)o),
+                         __shfl_sync(0xffffffffu, r.d.z, (int)o));
+        const float otmax = __shfl_sync(0xffffffffu, tmax, (int)o);
+        const float4* otris = (const float4*)__shfl_sync(0xffffffffu, (unsigned long long)tris, (int)o);
+        if (g < total) {
+            const uint32_t bit = __fns(om, 0u, (int)(g - oe) + 1);
+            if (bit < 32u && ((om >> bit) & 1u)) {
+                const float4* tp = otris + 3 * (size_t)(ob + bit);
+                float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
+                if (INSTR) ++*ntri;
+                float t, u, v;
+                if (intersect_tri(ro, rd, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= otmax)
+                    atomicMin(skey + o, hit_key(t, __float_as_uint(a0.w)));
+            }
+        }
+    }
+    __syncwarp();
+    bool found = false;
+    if (act) {
+        const unsigned long long k = skey[lane];
+        s.tg.y = 0u;
+        if (k != mine) {
+            const float t = __uint_as_float((uint32_t)(k >> 32));
+            const uint32_t id = (uint32_t)k;
+            s.best_t = t;
+            s.best_id = id;
+            found = true;
+            if (!ANY) {
+                const float4* sh = shade + 6 * (size_t)id;
+                const v3 a = ld3(__ldg(sh + 0)), b = ld3(__ldg(sh + 1)), c = ld3(__ldg(sh + 2));
+                float tt, u, v;
+                if (intersect_tri(r.o, r.d, a, b - a, c - a, &tt, &u, &v)) { s.bb = u; s.bg = v; }
+            }
+        }
+    }
+    __syncwarp();
+    return found;
+}
+
 // Persistent-warp ray loop shared by the traversal kernels: lanes whose ray
 // has finished run `finish` together, idle lanes are refilled from the queue
 // as soon as `refill` lanes are idle (all lanes once the queue is
@@ -552,6 +641,9 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
     uint2 stack[kStack];
     const float4* nodes = nullptr;
     const float4* tris = nullptr;
+    const float4* shade = nullptr;
+    __shared__ unsigned long long s_key[MODE == 3 ? kBlock : 1];
+    unsigned long long* skey = s_key + (MODE == 3 ? (threadIdx.x & ~31u) : 0u);
     while (true) {
         finish(fin, qi, s);
         fin = false;
@@ -575,7 +667,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
                 if (q < count) {
                     qi = q;
                     v3 o, d;
-                    if (fetch(q, &o, &d, &tmax, &nodes, &tris)) {
+                    if (fetch(q, &o, &d, &tmax, &nodes, &tris, &shade)) {
                         r = make_ray(o, d);
                         trav_init(s, r);
                         iters = 0;
@@ -589,7 +681,17 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
         }
         if (!__any_sync(0xffffffffu, act || fin)) break;
         while (true) {
-            if (MODE == 0) {
+            if (MODE == 3) {
+                // the warp tests every lane's pending triangles together, then
+                // each lane visits one node
+                bool hit = coop_triangles<ANY, INSTR>(act, tris, shade, r, tmax, s, skey, ntri);
+                if (ANY && act && hit) { act = false; fin = true; }
+                if (act) {
+                    bool done = node_step<INSTR>(nodes, r, tmax, s, stack, status, nvis);
+                    if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
+                    if (done) { act = false; fin = true; }
+                }
+            } else if (MODE == 0) {
                 // every pending triangle, then one node
                 if (act) {
                     bool done = trav_step<ANY, INSTR>(nodes, tris, r, tmax, s, stack, status, nvis, ntri);
@@ -642,12 +744,14 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
     const uint32_t* qin = F.q[it & 1];
     uint32_t* qsh = F.q[2];
     uint32_t nvis = 0, ntri = 0;
-    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris) {
+    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
+                     const float4** shade) {
         uint32_t slot = qin[q];
         float4 ro = F.ray_o[slot], rd = F.ray_d[slot];
         const SceneRec& R = F.scenes[F.ps[slot]];
         *nodes = R.S.nodes;
         *tris = R.S.tris;
+        *shade = R.S.shade;
         *o = ld3(ro); *d = ld3(rd); *tmax = ro.w;
         return true;
     };
@@ -718,12 +822,14 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
     const uint32_t* qsh = F.q[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&F.stats[2], (unsigned long long)count);
     uint32_t nvis = 0, ntri = 0;
-    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris) {
+    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
+                     const float4** shade) {
         uint32_t slot = qsh[q];
         float4 so = F.sh_o[slot], sd = F.sh_d[slot];
         const SceneRec& R = F.scenes[F.ps[slot]];
         *nodes = R.S.nodes;
         *tris = R.S.tris;
+        *shade = R.S.shade;
         *o = ld3(so); *d = ld3(sd); *tmax = so.w;
         return so.w >= 0.0f;
     };
@@ -895,6 +1001,69 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
             an = ak;
         }
     }
+}
+
+// Direct lighting as the reference's gpu_area_lights integrator
+// (direct-lighting.cpp:29-104, arealight-sampler.cu:156-260, :340-364), one
+// pixel per thread: the pixel-centre camera ray's first hit gives the
+// material colour (material_t::diffuse_color; the background for a miss,
+// evaluate_material), then `samples` area-light samples of the GPU sampler
+// (shadow offset as given, 0.01 there) are averaged: each adds psc * colour
+// when its shadow ray is unoccluded.  Sample k uses pool update max(0, k-1)
+// of the pixel's MRG32k3a stream, as the reference's update order gives
+// (the pool advances after the second sample is set up).  A missed pixel's
+// psc is the scaled sky texel of the direction its ray buffer holds: the
+// camera ray's for the first sample, (0, 0, 0) afterwards.
+__global__ void __launch_bounds__(kBlock) k_direct(DevScene S, CameraRec cam, int w, int h, int samples,
+                                                   uint32_t seed, float shadow_offset, v3 background, float* out,
+                                                   uint32_t* status) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= w * h) return;
+    v3 o, d;
+    camera_ray(cam, g % w, g / w, 0.5f, 0.5f, 0.0f, 0.0f, &o, &d);
+    TraceOut hit;
+    const bool is_hit = traverse<false>(S, make_ray(o, d), FLT_MAX, &hit, status);
+    v3 P = mk(0.0f, 0.0f, 0.0f), N = P, mcol = background;
+    if (is_hit) {
+        const float4* sh = S.shade + 6 * (size_t)hit.id;
+        const float4 a = sh[0];
+        P = bary(hit.beta, hit.gamma, ld3(a), ld3(sh[1]), ld3(sh[2]));
+        N = bary(hit.beta, hit.gamma, ld3(sh[3]), ld3(sh[4]), ld3(sh[5]));
+        const float* mf = S.mats + (size_t)kMaterialFloats * __float_as_uint(a.w);
+        mcol = mk(mf[25], mf[26], mf[27]);
+    }
+    curandStateMRG32k3a st;
+    curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &st);
+    v3 rnd = draw3(&st);
+    v3 buf_dir = d;
+    v3 acc = mk(0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < samples; ++k) {
+        if (k >= 2) rnd = draw3(&st);
+        v3 weight = mk(0.0f, 0.0f, 0.0f);
+        bool occluded = false;
+        if (is_hit && S.n_lights > 0) {
+            const int l = pick_light(S.lights, S.n_lights, S.overall_power, rnd.z);
+            const LightRec L = S.lights[l];
+            v3 so, sd;
+            float smax;
+            if (L.type == 1)
+                sky_light_sample_uniform(S.sky, L.power, S.overall_power, P, N, rnd.x, rnd.y, shadow_offset, &so,
+                                         &sd, &smax, &weight);
+            else
+                rect_light_sample(L, L.col, S.overall_power, P, N, rnd.x, rnd.y, shadow_offset, &so, &sd, &smax,
+                                  &weight, nullptr, false);
+            buf_dir = sd;
+            occluded = smax >= 0.0f && traverse<true>(S, make_ray(so, sd), smax, nullptr, status);
+        } else {
+            if (S.sky.light >= 0) weight = S.sky.scale * sky_eval(S.sky, buf_dir);
+            buf_dir = mk(0.0f, 0.0f, 0.0f);
+        }
+        const v3 mat = occluded ? mk(0.0f, 0.0f, 0.0f) : mcol;
+        acc = (float(k) * acc + weight * mat) / (float(k) + 1.0f);
+    }
+    out[3 * g] = acc.x;
+    out[3 * g + 1] = acc.y;
+    out[3 * g + 2] = acc.z;
 }
 
 __global__ void k_dimg_pack(const float* __restrict__ src, int n, float scale, float4* dst) {
@@ -1102,7 +1271,9 @@ cudaError_t k_launch_extend(const Frame& F, const RenderParams& P, bool instrume
         case 2: launch_extend_t<false, 1>(F, P, st); break;
         case 3: launch_extend_t<true, 1>(F, P, st); break;
         case 4: launch_extend_t<false, 2>(F, P, st); break;
-        default: launch_extend_t<true, 2>(F, P, st); break;
+        case 5: launch_extend_t<true, 2>(F, P, st); break;
+        case 6: launch_extend_t<false, 3>(F, P, st); break;
+        default: launch_extend_t<true, 3>(F, P, st); break;
     }
     return cudaGetLastError();
 }
@@ -1114,15 +1285,28 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
         case 2: launch_shadow_t<false, 1>(F, P, st); break;
         case 3: launch_shadow_t<true, 1>(F, P, st); break;
         case 4: launch_shadow_t<false, 2>(F, P, st); break;
-        default: launch_shadow_t<true, 2>(F, P, st); break;
+        case 5: launch_shadow_t<true, 2>(F, P, st); break;
+        case 6: launch_shadow_t<false, 3>(F, P, st); break;
+        default: launch_shadow_t<true, 3>(F, P, st); break;
     }
     return cudaGetLastError();
+}
+
+// Grid of the streaming per-path kernels (k_shade, k_regen), whose entry
+// counts are known only on the device: with GB_WIDE_STREAM_GRIDS one thread
+// per possible entry (the slot count), so every entry's dependent loads are
+// in flight at once; otherwise a persistent grid looping over the entries.
+#ifndef GB_WIDE_STREAM_GRIDS
+#define GB_WIDE_STREAM_GRIDS 0
+#endif
+inline int stream_grid(int persistent, int nslots) {
+    return GB_WIDE_STREAM_GRIDS ? std::max(1, blocks_for(nslots)) : persistent;
 }
 
 template <int MODE>
 void launch_shade_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g = persistent_blocks(k_shade<MODE>);
-    k_shade<MODE><<<g, kBlock, 0, st>>>(F, P);
+    k_shade<MODE><<<stream_grid(g, F.nslots), kBlock, 0, st>>>(F, P);
 }
 
 cudaError_t k_launch_shade(const Frame& F, const RenderParams& P, cudaStream_t st) {
@@ -1142,6 +1326,13 @@ cudaError_t k_launch_adjoint(const Frame& F, const RenderParams& P, cudaStream_t
     return cudaGetLastError();
 }
 
+cudaError_t k_launch_direct(const DevScene& S, const CameraRec& cam, int w, int h, int samples, uint32_t seed,
+                            float shadow_offset, v3 background, float* out, uint32_t* status, cudaStream_t st) {
+    if (w * h <= 0) return cudaSuccess;
+    k_direct<<<blocks_for(w * h), kBlock, 0, st>>>(S, cam, w, h, samples, seed, shadow_offset, background, out, status);
+    return cudaGetLastError();
+}
+
 cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     k_dimg_pack<<<blocks_for(n), kBlock, 0, st>>>(src, n, scale, dst);
@@ -1156,7 +1347,7 @@ cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, do
 
 cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g0 = persistent_blocks(k_regen);
-    k_regen<<<g0, kBlock, 0, st>>>(F, P);
+    k_regen<<<stream_grid(g0, F.nslots), kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
 }
 

@@ -108,7 +108,8 @@ struct Frame {
 // Launch-wide parameters of one chunk.
 struct RenderParams {
     int refill;        // refill a warp's lanes once this many are idle (1..32)
-    int tri_mode;      // 0: all pending triangles then a node; 1/2: triangle postponing, one / all triangles
+    int tri_mode;      // 0: all pending triangles then a node; 1/2: triangle postponing, one / all triangles;
+                       // 3: warp-cooperative triangle tests, then a node
     int blocks_per_sm; // resident blocks per SM of the traversal kernels (0 = occupancy limit)
     int mode;          // MODE_*
     int p0, rounds;    // path samples p0 .. p0+rounds-1
@@ -130,6 +131,8 @@ cudaError_t k_launch_jitter_pool(const Frame& F, const RenderParams& P, cudaStre
 cudaError_t k_launch_combine(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t st);
 cudaError_t k_launch_adjoint(const Frame& F, const RenderParams& P, cudaStream_t st);
+cudaError_t k_launch_direct(const DevScene& S, const CameraRec& cam, int w, int h, int samples, uint32_t seed,
+                            float shadow_offset, v3 background, float* out, uint32_t* status, cudaStream_t st);
 int k_adjoint_grid();
 cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st);
 cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, double* out, cudaStream_t st);

@@ -376,6 +376,31 @@ GB_HD v3 sky_eval(const SkyRec& s, v3 d) {
     return mk(t[0], t[1], t[2]);
 }
 
+// Sky branch of the GPU sampler k::pixel_generate_arealight_sample
+// (arealight-sampler.cu:213-229): a uniform hemisphere direction
+// (sqrt(1 - x^2) cos 2 pi y, sqrt(1 - x^2) sin 2 pi y, x) mapped around the
+// (unnormalised) normal, weighted by scale * texel(dir) * (dir . N); the
+// direction is not renormalised there and the shadow ray is unbounded.
+GB_HD void sky_light_sample_uniform(const SkyRec& s, float power, float overall_power, v3 P, v3 N, float rx,
+                                    float ry, float shadow_offset, v3* so, v3* sd, float* smax, v3* psc) {
+    float sq = sqrtf(1.0f - rx * rx);
+    float sn, cs;
+    sincos_2pi(ry, &sn, &cs);
+    v3 dir = make_tangential(mk(sq * cs, sq * sn, rx), N);
+    float theta = acos_ex(dir.y);
+    float phi = atan2_ex(dir.z, dir.x);
+    if (phi < 0.0f) phi += 6.28318531f;
+    float su = phi / 6.28318531f, tv = theta / 3.14159265f;
+    long long idx = (long long)(int)(tv * float(s.h)) * s.w + (int)(su * float(s.w));
+    v3 L = mk(0.0f, 0.0f, 0.0f);
+    if (idx >= 0 && idx < (long long)s.h * s.w) L = mk(s.texel[4 * idx], s.texel[4 * idx + 1], s.texel[4 * idx + 2]);
+    v3 contribution = (s.scale * L) * dot(dir, N);
+    *so = P + shadow_offset * dir;
+    *sd = dir;
+    *smax = FLT_MAX;
+    *psc = contribution * (overall_power / power);
+}
+
 // Sky branch of pixel_generate_arealight_sample_cpu with USE_SKY_SAMPLING
 // (arealight-sampler-cpu.cpp:87-96, 113-119): the sampled direction is
 // mapped around the (unnormalised) normal with make_tangential, weighted by
@@ -420,7 +445,8 @@ GB_HD int pick_light(const LightRec* L, int n, float overall_power, float rnd_z)
 // the light's emission (l.col, or the emission being differentiated) and
 // scale the geometry term over the light's pick probability.
 GB_HD void rect_light_sample(const LightRec& l, v3 col, float overall_power, v3 P, v3 N, float rx, float ry,
-                             float shadow_offset, v3* so, v3* sd, float* smax, v3* psc, float* scale = nullptr) {
+                             float shadow_offset, v3* so, v3* sd, float* smax, v3* psc, float* scale = nullptr,
+                             bool renormalize = true) {
     float offx = (rx - 0.5f) * l.w;
     float offy = (ry - 0.5f) * l.h;
     v3 ls = (l.center + offx * l.right) + offy * l.up;
@@ -431,7 +457,7 @@ GB_HD void rect_light_sample(const LightRec& l, v3 col, float overall_power, v3 
     float light_cos = fmaxf(dot(l.dir, -dir), 0.0f);
     float factor = l.w * l.h * ndotl * light_cos / (len * len);
     v3 contribution = col * factor;
-    dir = normalize_div(dir);
+    if (renormalize) dir = normalize_div(dir);  // the CPU sampler normalises again (:113)
     *so = P + shadow_offset * dir;
     *sd = dir;
     *smax = len;
@@ -454,6 +480,7 @@ struct MaterialRec {
     float csheen[3];           // mix(1, Ctint, sheenTint) :276
     float cspec0[3];           // :231
     float cc_a, cc_a2m1, cc_pilog;  // GTR1 constants        :186-192, :241
+    float kd[3];               // material_t::diffuse_color (evaluate_material, material-cpu.cpp:20-80)
 };
 static const int kMaterialFloats = 32;  // padded device record size
 
@@ -466,6 +493,7 @@ GB_HD MaterialRec unpack_material(const float* f) {
     r.clearcoat = f[8]; r.opacity = f[9]; r.ax = f[10]; r.ay = f[11]; r.roughg2 = f[12];
     for (int k = 0; k < 3; ++k) { r.cdlin[k] = f[13 + k]; r.csheen[k] = f[16 + k]; r.cspec0[k] = f[19 + k]; }
     r.cc_a = f[22]; r.cc_a2m1 = f[23]; r.cc_pilog = f[24];
+    r.kd[0] = f[25]; r.kd[1] = f[26]; r.kd[2] = f[27];
     return r;
 }
 

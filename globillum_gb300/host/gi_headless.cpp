@@ -4,10 +4,11 @@
 // then update while in_progress, and write the result image.
 //
 //   gi_headless <scene.bin> <out.pfm> [-r WxH] [-s spp] [-l path_length]
-//               [--offsets ray shadow] [--halton] [--rr bounce] [--save-every]
+//               [--offsets ray shadow] [--halton] [--rr bounce]
+//               [--algo hybrid_pt|gpu_area_lights] [--light-samples n]
 //
 // scene.bin (written by globillum_gb300.scenes.write_scene_bin): magic
-// "GBSC", version, counts, then positions, normals, material indices,
+// "GBSC", version 2, counts, then positions, normals, material indices,
 // materials, principled parameters, lights and the camera, little endian.
 // The image is written like save_image (util.cpp:111-150): pixel (x, y) to
 // (w-1-x, h-1-y), here as a float PFM.
@@ -37,12 +38,21 @@ template <typename T> bool rd(std::ifstream& f, T* p, size_t n) {
     return (bool)f;
 }
 
+// Scene files carry rect lights only: a stored sky map pointer means nothing.
+bool no_sky_maps(SceneFile* s) {
+    for (gb_light& l : s->lights) {
+        if (l.type == GB_LIGHT_SKY) return false;
+        l.sky_rgb = nullptr;
+    }
+    return true;
+}
+
 bool load_scene(const char* path, SceneFile* s) {
     std::ifstream f(path, std::ios::binary);
     if (!f) return false;
     char magic[4];
     int32_t hdr[5];  // version, triangles, materials, params, lights
-    if (!rd(f, magic, 4) || std::memcmp(magic, "GBSC", 4) != 0 || !rd(f, hdr, 5) || hdr[0] != 1) return false;
+    if (!rd(f, magic, 4) || std::memcmp(magic, "GBSC", 4) != 0 || !rd(f, hdr, 5) || hdr[0] != 2) return false;
     int nt = hdr[1], nm = hdr[2], np = hdr[3], nl = hdr[4];
     if (nt <= 0 || nm <= 0 || np < 0 || nl < 0) return false;
     s->pos.resize(9 * (size_t)nt);
@@ -54,7 +64,7 @@ bool load_scene(const char* path, SceneFile* s) {
     return rd(f, s->pos.data(), s->pos.size()) && rd(f, s->nrm.data(), s->nrm.size()) &&
            rd(f, s->mat.data(), s->mat.size()) && rd(f, s->mats.data(), s->mats.size()) &&
            (np == 0 || rd(f, s->params.data(), s->params.size())) &&
-           (nl == 0 || rd(f, s->lights.data(), s->lights.size())) && rd(f, &s->cam, 1);
+           (nl == 0 || rd(f, s->lights.data(), s->lights.size())) && rd(f, &s->cam, 1) && no_sky_maps(s);
 }
 
 bool write_pfm(const char* path, int w, int h, const std::vector<float>& rgb) {
@@ -77,13 +87,17 @@ bool write_pfm(const char* path, int w, int h, const std::vector<float>& rgb) {
 
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s scene.bin out.pfm [-r WxH] [-s spp] [-l len] [--offsets r s] [--halton] [--rr b]\n",
+        std::fprintf(stderr,
+                     "usage: %s scene.bin out.pfm [-r WxH] [-s spp] [-l len] [--offsets r s] [--halton] [--rr b]"
+                     " [--algo hybrid_pt|gpu_area_lights] [--light-samples n]\n",
                      argv[0]);
         return 2;
     }
     int w = 256, h = 256, spp = gb::init_path_samples(), len = gb::init_path_length(), rr = -1;
     float ro = 0.3f, so = 0.9f;
     bool halton = false;
+    std::string algo_name = "hybrid_pt";
+    int light_samples = 32;
     for (int i = 3; i < argc; ++i) {
         std::string a = argv[i];
         if (a == "-r" && i + 1 < argc) std::sscanf(argv[++i], "%dx%d", &w, &h);
@@ -92,6 +106,8 @@ int main(int argc, char** argv) {
         else if (a == "--offsets" && i + 2 < argc) { ro = (float)std::atof(argv[++i]); so = (float)std::atof(argv[++i]); }
         else if (a == "--halton") halton = true;
         else if (a == "--rr" && i + 1 < argc) rr = std::atoi(argv[++i]);
+        else if (a == "--algo" && i + 1 < argc) algo_name = argv[++i];
+        else if (a == "--light-samples" && i + 1 < argc) light_samples = std::atoi(argv[++i]);
         else { std::fprintf(stderr, "unknown argument %s\n", a.c_str()); return 2; }
     }
     SceneFile sf;
@@ -114,19 +130,25 @@ int main(int argc, char** argv) {
     try {
         gb::init_path_samples() = spp;
         gb::init_path_length() = len;
+        // both algorithms register, one is selected (hl-main.cpp:617-628)
         gb::hybrid_pt algo(w, h);
+        gb::gpu_area_lights direct(w, h);
         algo.render_desc().ray_offset = ro;
         algo.render_desc().shadow_offset = so;
         algo.render_desc().rng_mode = halton ? GB_RNG_HALTON_LIGHT : GB_RNG_MRG32K3A_POOL;
         algo.render_desc().rr_start = rr;
         gb::gi_algorithm::original_rt_set() = &set;
-        gb::gi_algorithm::select("hybrid_pt");
+        gb::gi_algorithm::select(algo_name);
         gb::gi_algorithm* a = gb::gi_algorithm::selected();
+        if (a == &direct) a->light_samples(light_samples);
         a->compute();
         while (a->in_progress()) a->update();
-        std::vector<float> img = algo.result();
+        std::vector<float> img = a == &algo ? algo.result() : direct.result();
         if (!write_pfm(argv[2], w, h, img)) { std::fprintf(stderr, "cannot write %s\n", argv[2]); return 1; }
-        std::printf("rendered %dx%d, %d paths of length %d per pixel\n", w, h, algo.paths_done(), len);
+        if (a == &algo)
+            std::printf("rendered %dx%d, %d paths of length %d per pixel\n", w, h, algo.paths_done(), len);
+        else
+            std::printf("rendered %dx%d, %d direct light samples per pixel\n", w, h, light_samples);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "error: %s\n", e.what());
         return 1;

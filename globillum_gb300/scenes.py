@@ -309,8 +309,9 @@ def random_rays(scene: SceneData, n: int, seed: int = 0, spread: float = 0.2):
 
 def write_scene_bin(scene: SceneData, path) -> None:
     """Binary scene file read by the headless front-end (host/gi_headless.cpp):
-    magic "GBSC", int32 version 1, triangles, materials, params, lights, then
-    the gb_scene_desc arrays and the gb_camera, little endian."""
+    magic "GBSC", int32 version 2 (gb_light with its sky fields; rect lights
+    only), triangles, materials, params, lights, then the gb_scene_desc arrays
+    and the gb_camera, little endian."""
     import ctypes as C
     from . import gbpt
     desc, keep = gbpt.make_scene_desc(scene)
@@ -319,7 +320,7 @@ def write_scene_bin(scene: SceneData, path) -> None:
     mid = np.ascontiguousarray(scene.material_index, np.int32)
     with open(path, "wb") as f:
         f.write(b"GBSC")
-        f.write(np.array([1, pos.shape[0], len(scene.materials), len(scene.params), len(scene.lights)],
+        f.write(np.array([2, pos.shape[0], len(scene.materials), len(scene.params), len(scene.lights)],
                          np.int32).tobytes())
         f.write(pos.tobytes())
         f.write(nrm.tobytes())

@@ -169,6 +169,18 @@ int gb_render_step(gb_ctx* ctx, int paths);
 int gb_render_paths_done(const gb_ctx* ctx, int* done);
 int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device);
 
+/* ------------------------------------------------------- direct lighting */
+/* The reference's GPU direct-lighting integrator gpu_area_lights
+ * (direct-lighting.cpp:29-104; samples as in arealight-sampler.cu:156-260,
+ * :340-364): per pixel the material colour of the pixel-centre camera ray's
+ * first hit (the MTL diffuse colour; desc->background for a miss) times
+ * the moving average of `light_samples` area-light samples that reach their
+ * light.  Uses width, height, seed, shadow_offset (0.01 in the reference)
+ * and background of desc; light sample k draws update max(0, k-1) of the
+ * pixel's MRG32k3a stream, as the reference's pool updates fall. */
+int gb_render_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+                     int light_samples, float* out_rgb, int out_is_device);
+
 /* ------------------------------------------------------------ batching */
 /* One scene of a batch: its own camera, resolution, spp, bounces, RNG mode
  * and seed; out_rgb receives width*height*3 floats as in gb_render. */
@@ -348,7 +360,9 @@ typedef struct {
     int sample_mb;
     int tri_mode;   /* traversal triangle policy + 1: 1 = every pending triangle then a
                        node; 2 / 3 = postpone triangle groups when fewer than a fifth of a
-                       warp's active lanes have any, else test one (2) / all (3) */
+                       warp's active lanes have any, else test one (2) / all (3);
+                       4 = the warp tests all lanes' pending triangles together
+                       (32 at a time), then every lane visits one node */
     int graph;      /* 1 = the host drives the slot-pool loop of single renders; 2 = each
                        chunk runs as one CUDA graph with a conditional while loop */
     int blocks_per_sm; /* resident 128-thread blocks per SM of the persistent traversal

@@ -775,6 +775,64 @@ int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int
     return 0;
 }
 
+// gpu_area_lights (direct-lighting.cpp:29-104): pixel-centre camera rays,
+// first-hit material colour (MTL diffuse colour, background for a miss),
+// `samples` GPU-sampler light samples averaged; sample k uses pool update
+// max(0, k - 1).  pool: [update][pixel][3], at least max(1, samples - 1)
+// updates.  out_rgb: w*h*3.
+int orc_render_direct(void* sp, const gb_camera* cam, const gb_render_desc* d, int samples, const float* pool,
+                      int pool_updates, float* out_rgb) {
+    const OScene& s = *(const OScene*)sp;
+    const int W = d->width, H = d->height, n = W * H;
+    if (samples <= 0 || pool_updates < std::max(1, samples - 1)) return 1;
+    CameraRec C = make_camera(*cam, W, H);
+    const v3 bg = mk(d->background[0], d->background[1], d->background[2]);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int g = 0; g < n; ++g) {
+        v3 o, dd;
+        camera_ray(C, g % W, g / W, 0.5f, 0.5f, 0.0f, 0.0f, &o, &dd);
+        gb_hit h = trace_closest(s, o, dd, FLT_MAX, nullptr, nullptr);
+        const bool hit = h.ref != 0xffffffffu;
+        v3 P = mk(0.0f, 0.0f, 0.0f), N = P, mcol = bg;
+        if (hit) {
+            P = tri_interp(s.pos, (int)h.ref, h.beta, h.gamma);
+            N = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
+            const MaterialRec& m = s.mats[s.mat[h.ref]];
+            mcol = mk(m.kd[0], m.kd[1], m.kd[2]);
+        }
+        v3 buf_dir = dd, acc = mk(0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < samples; ++k) {
+            const float* up = pool + ((size_t)std::max(0, k - 1) * n + g) * 3;
+            const v3 rnd = mk(up[0], up[1], up[2]);
+            v3 weight = mk(0.0f, 0.0f, 0.0f);
+            bool occluded = false;
+            if (hit && !s.lights.empty()) {
+                const int l = pick_light(s.lights.data(), (int)s.lights.size(), s.overall, rnd.z);
+                const LightRec& L = s.lights[l];
+                v3 so, sd;
+                float smax;
+                if (L.type == 1)
+                    sky_light_sample_uniform(s.sky, L.power, s.overall, P, N, rnd.x, rnd.y, d->shadow_offset, &so, &sd,
+                                             &smax, &weight);
+                else
+                    rect_light_sample(L, L.col, s.overall, P, N, rnd.x, rnd.y, d->shadow_offset, &so, &sd, &smax,
+                                      &weight, nullptr, false);
+                buf_dir = sd;
+                occluded = smax >= 0.0f && trace_any(s, so, sd, smax);
+            } else {
+                if (s.sky.light >= 0) weight = s.sky.scale * sky_eval(s.sky, buf_dir);
+                buf_dir = mk(0.0f, 0.0f, 0.0f);
+            }
+            const v3 mat = occluded ? mk(0.0f, 0.0f, 0.0f) : mcol;
+            acc = (float(k) * acc + weight * mat) / (float(k) + 1.0f);
+        }
+        out_rgb[3 * (size_t)g] = acc.x;
+        out_rgb[3 * (size_t)g + 1] = acc.y;
+        out_rgb[3 * (size_t)g + 2] = acc.z;
+    }
+    return 0;
+}
+
 // Halton pool of util.cpp:38-51 for pixels [0, n): (h2(i+1), h3(i+1)).
 int orc_halton_pool(int n, float* out) {
     for (int i = 0; i < n; ++i) { out[2 * i] = halton(i + 1, 2); out[2 * i + 1] = halton(i + 1, 3); }

@@ -27,3 +27,22 @@ def test_headless_matches_gb_render(gpu_ctx, tmp_path):
     scene.close()
     # the file is written like save_image: x and y mirrored
     assert np.array_equal(img, ref[::-1, ::-1])
+
+
+def test_headless_gpu_area_lights(gpu_ctx, tmp_path):
+    """--algo gpu_area_lights selects the C++ gpu_area_lights drop-in
+    (registered beside hybrid_pt) and renders gb_render_direct's image."""
+    exe = build.build_headless()
+    sc = scenes.cornell(width=40, height=32)
+    scenes.write_scene_bin(sc, tmp_path / "s.bin")
+    out = tmp_path / "d.pfm"
+    cmd = [str(exe), str(tmp_path / "s.bin"), str(out), "-r", "40x32", "--algo", "gpu_area_lights",
+           "--light-samples", "6"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    img = scenes.read_pfm(out)
+    scene = gpu_ctx.scene(sc)
+    rd = dict(sc.render, width=40, height=32, seed=0, shadow_offset=0.01, background=(1.0, 1.0, 1.0))
+    ref = scene.render_direct(sc.camera, rd, 6)
+    scene.close()
+    assert np.array_equal(img, ref[::-1, ::-1])

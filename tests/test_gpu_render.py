@@ -178,3 +178,24 @@ def test_sky_light_errors(gpu_ctx):
     with pytest.raises(gbpt.GBError, match="rectangular"):
         s.backward(sc.camera, sc.render, np.zeros((16, 16, 3), np.float32))
     s.close()
+
+
+def test_triangle_policies_agree(gpu_ctx):
+    """All traversal triangle policies (incl. the warp-cooperative one)
+    produce bit-identical frames: the closest hit is the (t, id) minimum
+    whatever the visiting order, and any-hit only asks whether one exists."""
+    sc = scenes.icospheres(n_spheres=60, level=3, box=20.0, width=64, height=40, spp=3, max_bounces=5, rr_start=2)
+    s = gpu_ctx.scene(sc)
+    old = gpu_ctx.get_tuning()
+    imgs = []
+    try:
+        for mode in (1, 2, 3, 4):
+            gpu_ctx.set_tuning(tri_mode=mode)
+            imgs.append(s.render(sc.camera, sc.render))
+            st = gpu_ctx.stats()
+            assert st["camera_rays"] == 64 * 40 * 3
+    finally:
+        gpu_ctx.set_tuning(tri_mode=old["tri_mode"])
+    for im in imgs[1:]:
+        assert np.array_equal(imgs[0], im)
+    s.close()
