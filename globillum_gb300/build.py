@@ -65,7 +65,7 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     """Compiles the CUDA kernels and the C ABI into libgbpt.so."""
     BUILD.mkdir(parents=True, exist_ok=True)
     LIBDIR.mkdir(parents=True, exist_ok=True)
-    cu = [CSRC / "gbpt_kernels.cu", CSRC / "gbpt_noalloc.cu"]
+    cu = [CSRC / "gbpt_kernels.cu", CSRC / "gbpt_noalloc.cu", CSRC / "gbpt_build.cu"]
     cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp", CSRC / "gbpt_ingest.cpp"]
     deps = cu + cpp + _sources()
     # the library records the build-time defines it was made with

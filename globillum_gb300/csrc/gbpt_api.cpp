@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <atomic>
 #include <cstdio>
@@ -12,6 +13,7 @@
 #include <vector>
 
 #include "../../include/gbpt.h"
+#include "gbpt_build.h"
 #include "gbpt_bvh.h"
 #include "gbpt_host.h"
 #include "gbpt_kernels.h"
@@ -113,6 +115,10 @@ struct gb_scene {
     std::vector<gb_material> mats;
     std::vector<gb_principled_params> params;
     std::vector<gb_light> lights;
+    // device-built tree (GB_BVH_DEVICE_PLOC) and what a refit rewrites
+    GpuBvh gbvh;
+    std::vector<int> material_index;
+    void* shade_buf = nullptr;
 };
 
 namespace {
@@ -149,6 +155,43 @@ cudaError_t dalloc(std::vector<void*>& list, void** p, size_t bytes) {
 void free_all(std::vector<void*>& list) {
     for (void* p : list) cudaFree(p);
     list.clear();
+}
+
+// Allocations of a device BVH build: kept buffers join the scene's list,
+// temporaries are freed when the build is done.
+struct SceneAllocator : DevAllocator {
+    std::vector<void*>& keep;
+    std::vector<void*> tmp;
+    explicit SceneAllocator(std::vector<void*>& k) : keep(k) {}
+    cudaError_t alloc(void** p, size_t bytes, bool k) override { return dalloc(k ? keep : tmp, p, bytes); }
+    void release_temps() override { free_all(tmp); }
+    ~SceneAllocator() override { free_all(tmp); }
+};
+
+// Shading records, canonical triangle order, 24 floats each: the three
+// vertices (w of the first = material index bits) and the three normals
+// (face normal when none are given).
+void make_shade_records(const float* pos, const float* normals, const int* material_index, int n,
+                        std::vector<float>* out) {
+    std::vector<float>& shade = *out;
+    shade.assign((size_t)n * 24, 0.0f);
+    for (int t = 0; t < n; ++t) {
+        float* s = &shade[(size_t)t * 24];
+        const float* p = pos + 9 * (size_t)t;
+        float nrm[9];
+        if (normals) std::memcpy(nrm, normals + 9 * (size_t)t, sizeof(nrm));
+        else {
+            v3 fn = normalize_div(cross(mk(p[3] - p[0], p[4] - p[1], p[5] - p[2]), mk(p[6] - p[0], p[7] - p[1], p[8] - p[2])));
+            for (int k = 0; k < 3; ++k) { nrm[3 * k] = fn.x; nrm[3 * k + 1] = fn.y; nrm[3 * k + 2] = fn.z; }
+        }
+        uint32_t mi = (uint32_t)material_index[t];
+        for (int v = 0; v < 3; ++v) {
+            s[4 * v] = p[3 * v]; s[4 * v + 1] = p[3 * v + 1]; s[4 * v + 2] = p[3 * v + 2]; s[4 * v + 3] = 0.0f;
+            s[12 + 4 * v] = nrm[3 * v]; s[12 + 4 * v + 1] = nrm[3 * v + 1]; s[12 + 4 * v + 2] = nrm[3 * v + 2];
+            s[12 + 4 * v + 3] = 0.0f;
+        }
+        std::memcpy(&s[3], &mi, 4);
+    }
 }
 
 cudaError_t ensure_scratch(gb_ctx* ctx, int k, size_t bytes) {
@@ -343,8 +386,17 @@ int gb_ctx_set_stream(gb_ctx* ctx, void* stream) {
 }
 
 int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
+    return gb_scene_create_ex(ctx, d, nullptr, out);
+}
+
+int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_options* opts, gb_scene** out) {
     if (!ctx || !d || !out) return fail(ctx, GB_ERR_INVALID, "null argument");
     *out = nullptr;
+    const int builder = opts ? opts->builder : GB_BVH_HOST_SAH;
+    if (builder != GB_BVH_HOST_SAH && builder != GB_BVH_DEVICE_PLOC) return fail(ctx, GB_ERR_INVALID, "unknown BVH builder");
+    if (opts && (opts->ploc_radius < 0 || opts->ploc_radius > 32))
+        return fail(ctx, GB_ERR_INVALID, "clustering radius must be 0 (default) .. 32");
+    const int radius = opts && opts->ploc_radius > 0 ? opts->ploc_radius : 16;
     CK(cudaSetDevice(ctx->device));
     int n = d->num_triangles;
     if (n <= 0 || !d->positions || !d->material_index) return fail(ctx, GB_ERR_INVALID, "no triangles");
@@ -380,26 +432,11 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     }
     CwBvh bvh;
     std::string err;
-    if (!build_cwbvh(d->positions, n, &bvh, &err)) return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);
+    if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err))
+        return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);
 
-    std::vector<float> shade((size_t)n * 24);
-    for (int t = 0; t < n; ++t) {
-        float* s = &shade[(size_t)t * 24];
-        const float* p = d->positions + 9 * (size_t)t;
-        float nrm[9];
-        if (d->normals) std::memcpy(nrm, d->normals + 9 * (size_t)t, sizeof(nrm));
-        else {
-            v3 fn = normalize_div(cross(mk(p[3] - p[0], p[4] - p[1], p[5] - p[2]), mk(p[6] - p[0], p[7] - p[1], p[8] - p[2])));
-            for (int k = 0; k < 3; ++k) { nrm[3 * k] = fn.x; nrm[3 * k + 1] = fn.y; nrm[3 * k + 2] = fn.z; }
-        }
-        uint32_t mi = (uint32_t)d->material_index[t];
-        for (int v = 0; v < 3; ++v) {
-            s[4 * v] = p[3 * v]; s[4 * v + 1] = p[3 * v + 1]; s[4 * v + 2] = p[3 * v + 2]; s[4 * v + 3] = 0.0f;
-            s[12 + 4 * v] = nrm[3 * v]; s[12 + 4 * v + 1] = nrm[3 * v + 1]; s[12 + 4 * v + 2] = nrm[3 * v + 2];
-            s[12 + 4 * v + 3] = 0.0f;
-        }
-        std::memcpy(&s[3], &mi, 4);
-    }
+    std::vector<float> shade;
+    make_shade_records(d->positions, d->normals, d->material_index, n, &shade);
     std::vector<float> mats((size_t)d->num_materials * kMaterialFloats);
     for (int m = 0; m < d->num_materials; ++m)
         pack_material(make_material(d->materials[m], d->params), &mats[(size_t)m * kMaterialFloats]);
@@ -407,19 +444,50 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     gb_scene* sc = new (std::nothrow) gb_scene();
     if (!sc) return fail(ctx, GB_ERR_OOM, "host allocation");
     sc->ctx = ctx;
-    void *pn, *pt, *ps, *pm, *pl;
+    void *pn = nullptr, *pt = nullptr, *ps, *pm, *pl;
     size_t bn = bvh.nodes.size() * 4, bt = bvh.tris.size() * 4, bs = shade.size() * 4, bm = mats.size() * 4,
            bl = sizeof(LightRec) * std::max<size_t>(1, lights.size());
     cudaError_t e;
-    if ((e = dalloc(sc->allocs, &pn, bn)) != cudaSuccess || (e = dalloc(sc->allocs, &pt, bt)) != cudaSuccess ||
+    if (builder == GB_BVH_DEVICE_PLOC) {
+        // positions to the device, tree built there; kept buffers join the scene
+        auto tb = std::chrono::steady_clock::now();
+        SceneAllocator SA(sc->allocs);
+        float* dpos = nullptr;
+        e = SA.alloc((void**)&dpos, sizeof(float) * 9 * (size_t)n, false);
+        if (e == cudaSuccess) e = cudaMemcpy(dpos, d->positions, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = gpu_build_cwbvh(dpos, n, radius, SA, &sc->gbvh, &err, ctx->stream);
+        if (e != cudaSuccess) {
+            SA.release_temps();
+            free_all(sc->allocs);
+            delete sc;
+            if (e == cudaErrorInvalidValue && !err.empty()) return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);
+            return cuda_fail(ctx, e, "device BVH build");
+        }
+        bvh.n_nodes = sc->gbvh.n_nodes;
+        bvh.n_tris = sc->gbvh.n_tris;
+        bvh.depth = sc->gbvh.depth;
+        bvh.binary_nodes = sc->gbvh.binary_nodes;
+        bvh.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
+        pn = sc->gbvh.nodes;
+        pt = sc->gbvh.tris;
+        bn = sc->gbvh.device_bytes;
+        bt = 0;
+        sc->material_index.assign(d->material_index, d->material_index + n);
+    }
+    if ((builder == GB_BVH_HOST_SAH &&
+         ((e = dalloc(sc->allocs, &pn, bn)) != cudaSuccess || (e = dalloc(sc->allocs, &pt, bt)) != cudaSuccess)) ||
         (e = dalloc(sc->allocs, &ps, bs)) != cudaSuccess || (e = dalloc(sc->allocs, &pm, bm)) != cudaSuccess ||
         (e = dalloc(sc->allocs, &pl, bl)) != cudaSuccess) {
         free_all(sc->allocs);
         delete sc;
         return cuda_fail(ctx, e, "scene allocation");
     }
-    e = cudaMemcpy(pn, bvh.nodes.data(), bn, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(pt, bvh.tris.data(), bt, cudaMemcpyHostToDevice);
+    sc->shade_buf = ps;
+    e = cudaSuccess;
+    if (builder == GB_BVH_HOST_SAH) {
+        e = cudaMemcpy(pn, bvh.nodes.data(), bn, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(pt, bvh.tris.data(), bt, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(ps, shade.data(), bs, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(pm, mats.data(), bm, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !lights.empty())
@@ -472,6 +540,8 @@ int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     sc->info.depth = bvh.depth;
     sc->info.binary_nodes = bvh.binary_nodes;
     sc->info.build_ms = bvh.build_ms;
+    sc->info.builder = builder;
+    sc->info.build_passes = sc->gbvh.iterations;
     sc->info.device_bytes = bn + bt + bs + bm + bl;
     sc->info.overall_light_power = sc->S.overall_power;
     *out = sc;
@@ -493,6 +563,30 @@ void gb_scene_destroy(gb_scene* scene) {
 int gb_scene_get_info(const gb_scene* scene, gb_scene_info* info) {
     if (!scene || !info) return GB_ERR_INVALID;
     *info = scene->info;
+    return GB_OK;
+}
+
+int gb_scene_refit(gb_scene* scene, const float* positions, const float* normals) {
+    if (!scene || !positions) return fail(scene ? scene->ctx : nullptr, GB_ERR_INVALID, "null argument");
+    gb_ctx* ctx = scene->ctx;
+    if (scene->info.builder != GB_BVH_DEVICE_PLOC)
+        return fail(ctx, GB_ERR_UNSUPPORTED, "refit needs a scene built with GB_BVH_DEVICE_PLOC");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));  // frames in flight still read the old tree
+    const int n = scene->gbvh.n;
+    SceneAllocator SA(scene->allocs);
+    float* dpos = nullptr;
+    std::string err;
+    cudaError_t e = SA.alloc((void**)&dpos, sizeof(float) * 9 * (size_t)n, false);
+    if (e == cudaSuccess) e = cudaMemcpy(dpos, positions, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = gpu_refit_cwbvh(dpos, SA, &scene->gbvh, &err, ctx->stream);
+    if (e != cudaSuccess) {
+        if (e == cudaErrorInvalidValue && !err.empty()) return fail(ctx, GB_ERR_INVALID, "refit: " + err);
+        return cuda_fail(ctx, e, "refit");
+    }
+    std::vector<float> shade;
+    make_shade_records(positions, normals, scene->material_index.data(), n, &shade);
+    CK(cudaMemcpy(scene->shade_buf, shade.data(), sizeof(float) * shade.size(), cudaMemcpyHostToDevice));
     return GB_OK;
 }
 

@@ -50,7 +50,16 @@ class SceneDesc(C.Structure):
 
 class SceneInfo(C.Structure):
     _fields_ = [("num_triangles", C.c_int), ("num_nodes", C.c_int), ("depth", C.c_int), ("binary_nodes", C.c_int),
-                ("build_ms", C.c_double), ("device_bytes", C.c_size_t), ("overall_light_power", C.c_float)]
+                ("build_ms", C.c_double), ("device_bytes", C.c_size_t), ("overall_light_power", C.c_float),
+                ("builder", C.c_int), ("build_passes", C.c_int)]
+
+
+GB_BVH_HOST_SAH, GB_BVH_DEVICE_PLOC = 0, 1
+BUILDERS = {"host": GB_BVH_HOST_SAH, "device": GB_BVH_DEVICE_PLOC}
+
+
+class BuildOptions(C.Structure):
+    _fields_ = [("builder", C.c_int), ("ploc_radius", C.c_int)]
 
 
 class Camera(C.Structure):
@@ -102,7 +111,7 @@ EXPORTS = [
     "gb_autotune", "gb_scene_param_count", "gb_scene_get_params", "gb_scene_set_params", "gb_forward",
     "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
     "gb_asset_add_obj", "gb_asset_add_lights", "gb_asset_add_light", "gb_asset_get_desc", "gb_asset_material_name",
-    "gb_read_pbrdf", "gb_render_direct",
+    "gb_read_pbrdf", "gb_render_direct", "gb_scene_create_ex", "gb_scene_refit",
 ]
 
 _lib = None
@@ -125,6 +134,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_last_error.restype = C.c_char_p
     lib.gb_ctx_set_stream.argtypes = [vp, vp]
     lib.gb_scene_create.argtypes = [vp, C.POINTER(SceneDesc), C.POINTER(vp)]
+    lib.gb_scene_create_ex.argtypes = [vp, C.POINTER(SceneDesc), C.POINTER(BuildOptions), C.POINTER(vp)]
+    lib.gb_scene_refit.argtypes = [vp, vp, vp]
     lib.gb_scene_destroy.argtypes = [vp]
     lib.gb_scene_destroy.restype = None
     lib.gb_scene_get_info.argtypes = [vp, C.POINTER(SceneInfo)]
@@ -260,8 +271,8 @@ class Context:
     def set_stream(self, stream: int | None):
         self.check(self.lib.gb_ctx_set_stream(self.h, stream))
 
-    def scene(self, scene_data) -> "Scene":
-        return Scene(self, scene_data)
+    def scene(self, scene_data, builder: str = "host", ploc_radius: int = 0) -> "Scene":
+        return Scene(self, scene_data, builder=builder, ploc_radius=ploc_radius)
 
     def stats(self) -> dict:
         s = Stats()
@@ -343,11 +354,24 @@ class Context:
 class Scene:
     """A resident gb_scene."""
 
-    def __init__(self, ctx: Context, scene_data):
+    def __init__(self, ctx: Context, scene_data, builder: str = "host", ploc_radius: int = 0):
+        """builder: "host" (binned SAH on the CPU) or "device" (PLOC on the
+        GPU; refittable)."""
         self.ctx = ctx
         self.h = C.c_void_p()
         desc, self._keep = make_scene_desc(scene_data)
-        ctx.check(ctx.lib.gb_scene_create(ctx.h, C.byref(desc), C.byref(self.h)))
+        if builder not in BUILDERS:
+            raise ValueError(f"builder must be one of {sorted(BUILDERS)}")
+        opts = BuildOptions(BUILDERS[builder], int(ploc_radius))
+        ctx.check(ctx.lib.gb_scene_create_ex(ctx.h, C.byref(desc), C.byref(opts), C.byref(self.h)))
+
+    def refit(self, positions: np.ndarray, normals: np.ndarray | None = None) -> None:
+        """gb_scene_refit: moved vertices (n, 9), same triangle order."""
+        pos = np.ascontiguousarray(positions, np.float32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        if pos.size != 9 * self.info()["num_triangles"] or (nrm is not None and nrm.size != pos.size):
+            raise ValueError("positions / normals must hold 9 floats per triangle of the scene")
+        self.ctx.check(self.ctx.lib.gb_scene_refit(self.h, _ptr(pos), None if nrm is None else _ptr(nrm)))
 
     def close(self):
         if self.h:

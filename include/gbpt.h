@@ -110,17 +110,42 @@ typedef struct {
 
 typedef struct {
     int num_triangles, num_nodes, depth, binary_nodes;
-    double build_ms;              /* host BVH build (binned SAH + collapse)   */
+    double build_ms;              /* BVH build wall time (GB_BVH_* below)     */
     size_t device_bytes;          /* resident scene bytes                     */
     float overall_light_power;    /* sum of light powers (hybrid-pt.cpp:74-78) */
+    int builder;                  /* GB_BVH_* the tree was built with         */
+    int build_passes;             /* clustering passes of GB_BVH_DEVICE_PLOC  */
 } gb_scene_info;
+
+/* BVH builders.  The reference builds a binary binned-SAH tree on the host
+ * through rta (`-b bsah`, hl-main.cpp:375-385).
+ *   GB_BVH_HOST_SAH     binned SAH on the host, collapsed to 8-wide nodes.
+ *   GB_BVH_DEVICE_PLOC  on the GPU: Morton order, parallel locally-ordered
+ *                       clustering, then the same 8-wide collapse rules, level
+ *                       by level; scenes built this way can be refitted.
+ * Both trees give identical frames (closest hits are the minimum (t, id)). */
+enum { GB_BVH_HOST_SAH = 0, GB_BVH_DEVICE_PLOC = 1 };
+typedef struct {
+    int builder;                  /* GB_BVH_*                                 */
+    int ploc_radius;              /* clustering search radius, 1 .. 32; 0 = 16 */
+} gb_build_options;
 
 /* Uploads triangles, materials and lights and builds the BVH (replaces
  * setup_rta's plugin_create_rt_set + convert_and_upload_materials,
- * hl-main.cpp:357-464, and hybrid_pt::activate's light copy). */
+ * hl-main.cpp:357-464, and hybrid_pt::activate's light copy).
+ * gb_scene_create uses GB_BVH_HOST_SAH. */
 int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* desc, gb_scene** out);
+int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* desc, const gb_build_options* opts, gb_scene** out);
 void gb_scene_destroy(gb_scene* scene);
 int gb_scene_get_info(const gb_scene* scene, gb_scene_info* info);
+
+/* Moves the vertices of a GB_BVH_DEVICE_PLOC scene: positions (9 floats per
+ * triangle, same count and order as at creation) and optional normals (NULL:
+ * face normals).  The tree keeps its topology; boxes are recomputed bottom-up
+ * and the nodes re-quantised on the GPU.  No counterpart in the reference,
+ * which rebuilds (plugin_create_rt_set).  GB_ERR_UNSUPPORTED for host-built
+ * scenes. */
+int gb_scene_refit(gb_scene* scene, const float* positions, const float* normals);
 
 /* ----------------------------------------------------------------- camera */
 /* crgs->setup(pos, dir, up, fovy) + jittered_lens_ray_generator

@@ -74,11 +74,12 @@ def test_struct_layouts_match_the_header(tmp_path):
              "gb_scene_desc": gbpt.SceneDesc, "gb_scene_info": gbpt.SceneInfo, "gb_camera": gbpt.Camera,
              "gb_render_desc": gbpt.RenderDesc, "gb_batch_item": gbpt.BatchItem, "gb_hit": gbpt.Hit,
              "gb_stats": gbpt.Stats, "gb_tuning": gbpt.Tuning, "gb_ctx_desc": gbpt.CtxDesc,
-             "gb_adjoint_item": gbpt.AdjointItem}
+             "gb_adjoint_item": gbpt.AdjointItem, "gb_build_options": gbpt.BuildOptions}
     c_fields = {"gb_batch_item": ["scene", "camera", "desc", "out_rgb"],
                 "gb_tuning": ["refill", "slots", "sample_mb", "tri_mode", "graph", "blocks_per_sm"],
                 "gb_render_desc": ["width", "height", "spp", "max_bounces", "rng_mode", "seed", "ray_offset",
                                    "shadow_offset", "background", "rr_start"],
+                "gb_scene_info": ["build_ms", "device_bytes", "overall_light_power", "builder", "build_passes"],
                 "gb_stats": ["camera_rays", "kernel_launches", "render_ms", "stage_ms", "stage_launches",
                              "paths_done"]}
     lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{ROOT / "include" / "gbpt.h"}"',
