@@ -69,8 +69,7 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp", CSRC / "gbpt_ingest.cpp"]
     deps = cu + cpp + _sources()
     # the library records the build-time defines it was made with
-    flags = (f"GB_TRAV_MIN_BLOCKS={os.environ.get('GBPT_TRAV_MIN_BLOCKS', '')} "
-             f"GB_WIDE_STREAM_GRIDS={os.environ.get('GBPT_WIDE_STREAM_GRIDS', '')}")
+    flags = f"GB_TRAV_MIN_BLOCKS={os.environ.get('GBPT_TRAV_MIN_BLOCKS', '')}"
     stamp = LIB.with_suffix(".flags")
     if not stamp.exists() or stamp.read_text() != flags:
         force = True
@@ -88,9 +87,6 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
         mb = os.environ.get("GBPT_TRAV_MIN_BLOCKS")
         if mb:
             c.insert(1, f"-DGB_TRAV_MIN_BLOCKS={int(mb)}")
-        # GBPT_WIDE_STREAM_GRIDS=1: one thread per slot for k_shade / k_regen
-        if os.environ.get("GBPT_WIDE_STREAM_GRIDS"):
-            c.insert(1, f"-DGB_WIDE_STREAM_GRIDS={int(os.environ['GBPT_WIDE_STREAM_GRIDS'])}")
         if verbose_ptxas:
             c.insert(1, "-Xptxas=-v")
         cmds.append(c)

@@ -119,6 +119,7 @@ struct gb_scene {
     GpuBvh gbvh;
     std::vector<int> material_index;
     void* shade_buf = nullptr;
+    std::vector<int> mat_dtex;  // diffuse texture of each material (-1 = none)
 };
 
 namespace {
@@ -218,6 +219,7 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nsc
         float4** bufs[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
         for (float4** b : bufs)
             if ((e = dalloc(ctx->slot_allocs, (void**)b, v4)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&F.rdiff, 3 * v4)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.rng, sizeof(MrgState) * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.pix, 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.pb, 4 * (size_t)nslots)) != cudaSuccess) return e;
@@ -437,9 +439,33 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
 
     std::vector<float> shade;
     make_shade_records(d->positions, d->normals, d->material_index, n, &shade);
+    // textures: checked here, mip chains made on the host (shared with the oracle)
+    if (d->num_textures < 0 || (d->num_textures > 0 && !d->textures)) return fail(ctx, GB_ERR_INVALID, "bad textures");
+    for (int k = 0; k < d->num_textures; ++k) {
+        const gb_texture& t = d->textures[k];
+        if (!t.rgba || t.w <= 0 || t.h <= 0 || t.w > 65536 || t.h > 65536 || (long long)t.w * t.h > (1ll << 26))
+            return fail(ctx, GB_ERR_INVALID, "texture size must be 1 .. 65536 per side and at most 2^26 texels");
+    }
+    std::vector<int> dtex((size_t)d->num_materials, -1);
+    bool any_tex = false;
+    if (d->diffuse_texture)
+        for (int m = 0; m < d->num_materials; ++m) {
+            const int v = d->diffuse_texture[m];
+            if (v < -1 || v >= d->num_textures) return fail(ctx, GB_ERR_INVALID, "diffuse texture index out of range");
+            dtex[m] = v;
+            any_tex = any_tex || v >= 0;
+        }
+    if (any_tex) {
+        if (!d->texcoords) return fail(ctx, GB_ERR_INVALID, "textured materials need texture coordinates");
+        for (size_t i = 0; i < 6 * (size_t)n; ++i)
+            if (!std::isfinite(d->texcoords[i])) return fail(ctx, GB_ERR_INVALID, "non-finite texture coordinate");
+    }
     std::vector<float> mats((size_t)d->num_materials * kMaterialFloats);
-    for (int m = 0; m < d->num_materials; ++m)
-        pack_material(make_material(d->materials[m], d->params), &mats[(size_t)m * kMaterialFloats]);
+    for (int m = 0; m < d->num_materials; ++m) {
+        MaterialRec r = make_material(d->materials[m], d->params);
+        r.dtex = dtex[m];
+        pack_material(r, &mats[(size_t)m * kMaterialFloats]);
+    }
 
     gb_scene* sc = new (std::nothrow) gb_scene();
     if (!sc) return fail(ctx, GB_ERR_OOM, "host allocation");
@@ -515,11 +541,41 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
         sc->S.sky.scale = lights[sky_light].scale;
         sc->S.sky.light = sky_light;
     }
+    sc->S.texcoord = nullptr;
+    sc->S.tex = nullptr;
+    sc->S.n_tex = 0;
+    if (e == cudaSuccess && any_tex) {
+        void* ptc = nullptr;
+        e = dalloc(sc->allocs, &ptc, sizeof(float) * 6 * (size_t)n);
+        if (e == cudaSuccess) e = cudaMemcpy(ptc, d->texcoords, sizeof(float) * 6 * (size_t)n, cudaMemcpyHostToDevice);
+        bs += sizeof(float) * 6 * (size_t)n;
+        std::vector<TexRec> recs((size_t)d->num_textures);
+        std::vector<uint8_t> chain;
+        for (int k = 0; k < d->num_textures && e == cudaSuccess; ++k) {
+            const gb_texture& t = d->textures[k];
+            make_mipmaps(t.rgba, t.w, t.h, &chain, &recs[k].max_mm, &recs[k].size);
+            void* pt_ = nullptr;
+            e = dalloc(sc->allocs, &pt_, chain.size());
+            if (e == cudaSuccess) e = cudaMemcpy(pt_, chain.data(), chain.size(), cudaMemcpyHostToDevice);
+            recs[k].texels = (const uint8_t*)pt_;
+            recs[k].w = t.w;
+            recs[k].h = t.h;
+            bs += chain.size();
+        }
+        void* prec = nullptr;
+        if (e == cudaSuccess) e = dalloc(sc->allocs, &prec, sizeof(TexRec) * std::max<size_t>(1, recs.size()));
+        if (e == cudaSuccess && !recs.empty())
+            e = cudaMemcpy(prec, recs.data(), sizeof(TexRec) * recs.size(), cudaMemcpyHostToDevice);
+        sc->S.texcoord = (const float*)ptc;
+        sc->S.tex = (const TexRec*)prec;
+        sc->S.n_tex = d->num_textures;
+    }
     if (e != cudaSuccess) {
         free_all(sc->allocs);
         delete sc;
         return cuda_fail(ctx, e, "scene upload");
     }
+    sc->mat_dtex = dtex;
     sc->S.nodes = (const float4*)pn;
     sc->S.tris = (const float4*)pt;
     sc->S.shade = (const float4*)ps;
@@ -779,7 +835,7 @@ std::vector<uint64_t> graph_key(const gb_ctx* ctx, const RenderParams& P, int ns
     const void* ptrs[] = {F.scenes, F.ray_o, F.ray_d, F.tp, F.accum, F.sh_o, F.sh_d, F.psc, F.rnd, F.hit_p,
                           F.hit_n, F.rng, F.pix, F.ps, F.pb, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
                           F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr,
-                          F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad};
+                          F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad, F.rdiff};
     for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
     k.push_back(((uint64_t)(uint32_t)F.grad_stride << 32) | (uint32_t)F.grad_replicas);
     static_assert(sizeof(RenderParams) % 4 == 0, "RenderParams is made of 32-bit words");
@@ -871,6 +927,9 @@ int run_chunk(gb_ctx* ctx, int p0, int p1) {
     P.tri_mode = ctx->tri_mode;
     P.blocks_per_sm = ctx->blocks_per_sm;
     P.mode = ctx->mode;
+    P.textured = 0;
+    for (const BatchScene& b : ctx->items)
+        if (b.scene->S.texcoord) P.textured = 1;
     P.p0 = p0;
     P.rounds = p1 - p0;
     long long acc = 0, n_last = 0;
@@ -1074,10 +1133,14 @@ void apply_params(const gb_scene* s, const float* x, std::vector<gb_material>* m
 }
 
 void build_records(const std::vector<gb_material>& mats, const std::vector<gb_principled_params>& params,
-                   const std::vector<gb_light>& lights, std::vector<float>* mrec, std::vector<LightRec>* lrec) {
+                   const std::vector<gb_light>& lights, std::vector<float>* mrec, std::vector<LightRec>* lrec,
+                   const std::vector<int>* dtex = nullptr) {
     mrec->assign(mats.size() * kMaterialFloats, 0.0f);
-    for (size_t m = 0; m < mats.size(); ++m)
-        pack_material(make_material(mats[m], params.empty() ? nullptr : params.data()), &(*mrec)[m * kMaterialFloats]);
+    for (size_t m = 0; m < mats.size(); ++m) {
+        MaterialRec r = make_material(mats[m], params.empty() ? nullptr : params.data());
+        if (dtex && m < dtex->size()) r.dtex = (*dtex)[m];
+        pack_material(r, &(*mrec)[m * kMaterialFloats]);
+    }
     lrec->clear();
     for (const gb_light& l : lights) lrec->push_back(make_light(l));
 }
@@ -1143,7 +1206,7 @@ int gb_scene_set_params(gb_scene* scene, const float* x) {
     apply_params(scene, x, &mats, &params, &lights);
     std::vector<float> mrec;
     std::vector<LightRec> lrec;
-    build_records(mats, params, lights, &mrec, &lrec);
+    build_records(mats, params, lights, &mrec, &lrec, &scene->mat_dtex);
     for (const LightRec& l : lrec)
         if (!(l.power > 0.0f)) return fail(ctx, GB_ERR_INVALID, "light power must be positive");
     CK(cudaSetDevice(ctx->device));
@@ -1165,6 +1228,8 @@ int gb_forward(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_rend
     if (!ctx || !scene || !cam || !desc) return fail(ctx, GB_ERR_INVALID, "null argument");
     if (scene->ctx != ctx) return fail(ctx, GB_ERR_INVALID, "scene belongs to another context");
     if (!all_finite(eval_params, param_count(scene))) return fail(ctx, GB_ERR_INVALID, "non-finite parameter");
+    if (scene->S.texcoord)
+        return fail(ctx, GB_ERR_UNSUPPORTED, "frozen-sampling replay covers scenes without textures only");
     CK(cudaSetDevice(ctx->device));
     std::vector<gb_material> mats;
     std::vector<gb_principled_params> params;
@@ -1214,6 +1279,8 @@ int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg
             return fail(ctx, GB_ERR_INVALID, "the adjoint records at most 16 bounces per path");
         if (items[i].scene->S.sky.light >= 0)
             return fail(ctx, GB_ERR_UNSUPPORTED, "the adjoint covers scenes with rectangular lights only");
+        if (items[i].scene->S.texcoord)
+            return fail(ctx, GB_ERR_UNSUPPORTED, "the adjoint covers scenes without textures only");
         v[i].scene = items[i].scene;
         v[i].cam = items[i].camera;
         v[i].desc = items[i].desc;
@@ -1524,6 +1591,8 @@ int gb_compute_path_contribution_and_bounce(gb_ctx* ctx, gb_scene* scene, int w,
     if (!ray_orig || !ray_dir || !max_t || !hits || !shadow_occluded || !rnd || !throughput || !col_accum ||
         !to_light || !psc)
         return fail(ctx, GB_ERR_INVALID, "null buffer");
+    if (scene->S.texcoord)
+        return fail(ctx, GB_ERR_UNSUPPORTED, "the stage call has no ray-differential buffers; textured scenes need gb_render");
     CK(cudaSetDevice(ctx->device));
     ShadeParams sp = make_shade_params(*desc);
     CK(k_launch_shade_stage(scene->S, w * h, sp, ray_orig, ray_dir, max_t, (const float4*)hits, shadow_occluded, rnd,

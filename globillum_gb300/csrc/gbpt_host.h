@@ -19,6 +19,7 @@ static inline MaterialRec make_material(const gb_material& m, const gb_principle
     MaterialRec r;
     std::memset(&r, 0, sizeof(r));
     for (int k = 0; k < 3; ++k) r.kd[k] = m.diffuse[k];
+    r.dtex = -1;
     if (m.principled < 0) {
         r.kind = MAT_LAMBERT;
         for (int k = 0; k < 3; ++k) r.diffuse[k] = m.diffuse[k];
@@ -37,19 +38,10 @@ static inline MaterialRec make_material(const gb_material& m, const gb_principle
     float roughg = (float)((double)(r.ax * r.ay) * .5 + .5);
     roughg = roughg * roughg;
     r.roughg2 = roughg * roughg;
-    float cdlin[3];
-    for (int k = 0; k < 3; ++k) cdlin[k] = (float)std::pow((double)p.color[k], 2.2);
-    float cdlum = (float)(.3 * cdlin[0] + .6 * cdlin[1] + .1 * cdlin[2]);
-    float ctint[3];
-    for (int k = 0; k < 3; ++k) ctint[k] = cdlum > 0 ? cdlin[k] / cdlum : 1.0f;
-    float spec08 = (float)((double)p.specular * .08);
-    for (int k = 0; k < 3; ++k) {
-        r.cdlin[k] = cdlin[k];
-        r.csheen[k] = (1.0f - p.sheen_tint) * 1.0f + p.sheen_tint * ctint[k];
-        float st = (1.0f - p.specular_tint) * 1.0f + p.specular_tint * ctint[k];
-        float a = spec08 * st;
-        r.cspec0[k] = (1.0f - p.metallic) * a + p.metallic * cdlin[k];
-    }
+    r.sheen_tint = p.sheen_tint;
+    r.specular_tint = p.specular_tint;
+    r.specular = p.specular;
+    material_colour_terms(&r, p.color, false);
     float a = (1.0f - p.clearcoat_gloss) * 0.1f + p.clearcoat_gloss * 0.001f;
     float a2 = a * a;
     r.cc_a = a;
@@ -117,6 +109,53 @@ static inline void pack_material(const MaterialRec& r, float* f) {
     for (int k = 0; k < 3; ++k) { f[13 + k] = r.cdlin[k]; f[16 + k] = r.csheen[k]; f[19 + k] = r.cspec0[k]; }
     f[22] = r.cc_a; f[23] = r.cc_a2m1; f[24] = r.cc_pilog;
     f[25] = r.kd[0]; f[26] = r.kd[1]; f[27] = r.kd[2];
+    f[28] = r.sheen_tint; f[29] = r.specular_tint; f[30] = r.specular;
+    f[31] = (float)r.dtex;
+}
+
+// Mip chain of a texture (texture_data's constructor and compute_mipmaps,
+// material.h:27-36, material.cu:231-275): max_mm = floor(log2(min(w, h)))
+// levels after the image, texel (x, y) of level i+1 the integer mean
+// (truncated) of the 2x2 block at (2x, 2y) of level i.  Parts of the block
+// outside an odd-sized level are left out of the mean; the reference's
+// kernel drops the wrong weight there (w00 instead of w01) and reads an
+// uninitialised texel, which is not reproduced.  Integer floor(log2) is
+// exact where log2f of the size is not (sizes near 2^k above 2^17).
+// Output: all levels, then a zero tail of w + 1 texels (see TexRec).
+static inline void make_mipmaps(const uint8_t* rgba, int w, int h, std::vector<uint8_t>* out, int* max_mm,
+                                int* size) {
+    int mn = w < h ? w : h, mm = 0;
+    while ((2 << mm) <= mn) ++mm;
+    std::vector<int> off(1, 0), lw(1, w), lh(1, h);
+    for (int i = 0; i < mm; ++i) {
+        off.push_back(off.back() + lw.back() * lh.back());
+        lw.push_back((lw.back() + 1) / 2);
+        lh.push_back((lh.back() + 1) / 2);
+    }
+    const int total = off.back() + lw.back() * lh.back();
+    out->assign(4 * (size_t)(total + w + 1), 0);
+    uint8_t* d = out->data();
+    std::memcpy(d, rgba, 4 * (size_t)w * h);
+    for (int i = 0; i < mm; ++i) {
+        const int sw = lw[i], sh = lh[i], tw = lw[i + 1], th = lh[i + 1];
+        const uint8_t* src = d + 4 * (size_t)off[i];
+        uint8_t* dst = d + 4 * (size_t)off[i + 1];
+        for (int y = 0; y < th; ++y)
+            for (int x = 0; x < tw; ++x) {
+                const int X = 2 * x, Y = 2 * y;
+                const bool rx = X + 1 < sw, ry = Y + 1 < sh;
+                const unsigned W = 1u + (rx ? 1u : 0u) + (ry ? 1u : 0u) + (rx && ry ? 1u : 0u);
+                for (int k = 0; k < 4; ++k) {
+                    unsigned t = src[4 * ((size_t)Y * sw + X) + k];
+                    if (rx) t += src[4 * ((size_t)Y * sw + X + 1) + k];
+                    if (ry) t += src[4 * ((size_t)(Y + 1) * sw + X) + k];
+                    if (rx && ry) t += src[4 * ((size_t)(Y + 1) * sw + X + 1) + k];
+                    dst[4 * ((size_t)y * tw + x) + k] = (uint8_t)(t / W);
+                }
+            }
+    }
+    *max_mm = mm;
+    *size = total + w + 1;
 }
 
 // gi::light: a rect light with its fixed basis (arealight-sampler-cpu.cpp:70-73),

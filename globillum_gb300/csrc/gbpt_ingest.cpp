@@ -28,7 +28,12 @@
 
 struct gb_asset {
     std::vector<float> pos, nrm;  // 9 floats per triangle each
+    std::vector<float> tc;        // 6 floats per triangle (vt of the corners, 0 where absent)
     std::vector<int> mat;
+    std::vector<int> dtex;        // diffuse texture of each material (-1 = none)
+    std::vector<std::vector<uint8_t>> tex_pixels;
+    std::vector<gb_texture> textures;
+    std::map<std::string, int> texture_index;  // by file path
     std::vector<gb_material> materials;
     std::vector<gb_principled_params> params;
     std::vector<gb_light> lights;
@@ -98,8 +103,67 @@ bool parse_pbrdf(const std::string& path, gb_principled_params* out) {
 
 struct MtlEntry {
     float kd[3] = {0.0f, 0.0f, 0.0f};
-    bool has_texture = false;
+    std::string texture;  // map_Kd, relative to the MTL file's directory
 };
+
+// Binary (P6) or ASCII (P3) PPM with maxval <= 255 as RGBA8, rows top first.
+bool read_ppm(const std::string& path, std::vector<uint8_t>* rgba, int* w, int* h) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) return false;
+    std::string magic;
+    in >> magic;
+    if (magic != "P6" && magic != "P3") return false;
+    int vals[3], k = 0;
+    while (k < 3 && in) {
+        in >> std::ws;
+        if (in.peek() == '#') { std::string c; std::getline(in, c); continue; }
+        in >> vals[k++];
+    }
+    if (!in || k < 3 || vals[0] <= 0 || vals[1] <= 0 || vals[2] <= 0 || vals[2] > 255 ||
+        (long long)vals[0] * vals[1] > (1ll << 26))
+        return false;
+    *w = vals[0];
+    *h = vals[1];
+    const size_t n = (size_t)vals[0] * vals[1];
+    rgba->assign(4 * n, 255);
+    if (magic == "P6") {
+        in.get();  // the single whitespace after maxval
+        std::vector<uint8_t> raw(3 * n);
+        if (!in.read((char*)raw.data(), (std::streamsize)raw.size())) return false;
+        for (size_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) (*rgba)[4 * i + c] = raw[3 * i + c];
+    } else {
+        for (size_t i = 0; i < 3 * n; ++i) {
+            int v;
+            if (!(in >> v) || v < 0 || v > vals[2]) return false;
+            (*rgba)[4 * (i / 3) + i % 3] = (uint8_t)v;
+        }
+    }
+    if (vals[2] != 255)  // rescale to 0 .. 255
+        for (size_t i = 0; i < 4 * n; ++i)
+            if (i % 4 != 3) (*rgba)[i] = (uint8_t)(((*rgba)[i] * 255 + vals[2] / 2) / vals[2]);
+    return true;
+}
+
+// Index of the texture in file `path`, loading it on first use; -1 when it
+// cannot be read as PPM (counted in textures_ignored).
+int texture_for(gb_asset* a, const std::string& path) {
+    auto it = a->texture_index.find(path);
+    if (it != a->texture_index.end()) return it->second;
+    std::vector<uint8_t> px;
+    int w = 0, h = 0;
+    int idx = -1;
+    if (read_ppm(path, &px, &w, &h)) {
+        idx = (int)a->textures.size();
+        a->tex_pixels.push_back(std::move(px));
+        a->textures.push_back(gb_texture{w, h, nullptr});
+        for (size_t k = 0; k < a->textures.size(); ++k) a->textures[k].rgba = a->tex_pixels[k].data();
+    } else {
+        a->textures_ignored++;
+    }
+    a->texture_index[path] = idx;
+    return idx;
+}
 
 void parse_mtl(const std::string& path, std::map<std::string, MtlEntry>* out) {
     std::ifstream in(path);
@@ -116,7 +180,9 @@ void parse_mtl(const std::string& path, std::map<std::string, MtlEntry>* out) {
             MtlEntry& e = (*out)[cur];
             ls >> e.kd[0] >> e.kd[1] >> e.kd[2];
         } else if (key == "map_Kd" && !cur.empty()) {
-            (*out)[cur].has_texture = true;
+            std::string f, tok;
+            while (ls >> tok) f = tok;  // the file name is the last token (options come first)
+            if (!f.empty()) (*out)[cur].texture = dir_of(path) + "/" + f;
         }
     }
 }
@@ -131,9 +197,10 @@ int material_for(gb_asset* a, const std::string& name, const std::map<std::strin
     std::memset(&m, 0, sizeof(m));
     m.principled = -1;
     auto e = mtl.find(name);
+    int tex = -1;
     if (e != mtl.end()) {
         for (int c = 0; c < 3; ++c) m.diffuse[c] = e->second.kd[c];
-        if (e->second.has_texture) a->textures_ignored++;
+        if (!e->second.texture.empty()) tex = texture_for(a, e->second.texture);
     }
     gb_principled_params p;
     if (!material_dir.empty() && parse_pbrdf(material_dir + "/" + name + ".pbrdf", &p)) {
@@ -142,6 +209,7 @@ int material_for(gb_asset* a, const std::string& name, const std::map<std::strin
     }
     int idx = (int)a->materials.size();
     a->materials.push_back(m);
+    a->dtex.push_back(tex);
     a->material_names.push_back(name);
     a->material_index[name] = idx;
     return idx;
@@ -180,6 +248,7 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
         fb.diffuse[0] = 1.0f;
         fb.principled = -1;
         a->materials.push_back(fb);
+        a->dtex.push_back(-1);
         a->material_names.push_back("gi/fallback");
         a->material_index["gi/fallback"] = 0;
     }
@@ -194,7 +263,7 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
     if (!(std::fabs(det) > 0.0)) return fail(a, GB_ERR_INVALID, "singular transformation");
     if (det < 0.0)  // inverse transpose = cofactors / det: keep det's sign
         for (double& c : cof) c = -c;
-    std::vector<float> v, vn;
+    std::vector<float> v, vn, vt;
     std::map<std::string, MtlEntry> mtl;
     int cur_mat = 0;
     const size_t tri0 = a->mat.size();
@@ -220,6 +289,12 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
                 if (l > 0.0) { nx /= l; ny /= l; nz /= l; }
                 dst.push_back((float)nx); dst.push_back((float)ny); dst.push_back((float)nz);
             }
+        } else if (key == "vt") {
+            double s_, t_ = 0.0;
+            if (!(ls >> s_)) return fail(a, GB_ERR_INVALID, "bad texture coordinate at line " + std::to_string(lineno));
+            ls >> t_;
+            vt.push_back((float)s_);
+            vt.push_back((float)t_);
         } else if (key == "mtllib") {
             std::string f;
             ls >> f;
@@ -230,9 +305,9 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
             // names the MTL does not define fall back (material(name) == -1 and no group material)
             cur_mat = mtl.count(name) ? material_for(a, name, mtl, mdir) : 0;
         } else if (key == "f") {
-            std::vector<int> vi, ni;
+            std::vector<int> vi, ni, ti;
             std::string c;
-            const int nv = (int)v.size() / 3, nn = (int)vn.size() / 3;
+            const int nv = (int)v.size() / 3, nn = (int)vn.size() / 3, nt = (int)vt.size() / 2;
             while (ls >> c) {
                 int iv = 0, it = 0, in_ = 0;
                 size_t s1 = c.find('/');
@@ -242,9 +317,14 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
                     if (s2 != std::string::npos) {
                         if (s2 > s1 + 1) it = std::atoi(c.substr(s1 + 1, s2 - s1 - 1).c_str());
                         in_ = std::atoi(c.substr(s2 + 1).c_str());
+                    } else if (s1 + 1 < c.size()) {
+                        it = std::atoi(c.substr(s1 + 1).c_str());
                     }
                 }
-                (void)it;  // texture coordinates: textures are not modelled
+                int t_ = it ? obj_index(it, nt) : -1;
+                if (it && (t_ < 0 || t_ >= nt))
+                    return fail(a, GB_ERR_INVALID, "texture coordinate index out of range at line " + std::to_string(lineno));
+                ti.push_back(t_);
                 int a_ = obj_index(iv, nv);
                 if (iv == 0 || a_ < 0 || a_ >= nv)
                     return fail(a, GB_ERR_INVALID, "vertex index out of range at line " + std::to_string(lineno));
@@ -258,6 +338,11 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
             for (size_t k = 1; k + 1 < vi.size(); ++k) {  // fan
                 const int cv[3] = {vi[0], vi[k], vi[k + 1]};
                 const int cn[3] = {ni[0], ni[k], ni[k + 1]};
+                const int ct[3] = {ti[0], ti[k], ti[k + 1]};
+                for (int j = 0; j < 3; ++j) {
+                    a->tc.push_back(ct[j] >= 0 ? vt[2 * ct[j]] : 0.0f);
+                    a->tc.push_back(ct[j] >= 0 ? vt[2 * ct[j] + 1] : 0.0f);
+                }
                 float P[9];
                 for (int j = 0; j < 3; ++j)
                     for (int d = 0; d < 3; ++d) P[3 * j + d] = v[3 * cv[j] + d];
@@ -276,7 +361,7 @@ int gb_asset_add_obj(gb_asset* a, const char* obj_path, const char* material_dir
                 a->mat.push_back(cur_mat);
             }
         }
-        // o / g / s / vt lines carry nothing the path needs
+        // o / g / s lines carry nothing the path needs
     }
     if (a->mat.size() == tri0) return fail(a, GB_ERR_INVALID, std::string("no faces in ") + obj_path);
     return GB_OK;
@@ -434,6 +519,12 @@ extern "C" int gb_asset_get_desc(const gb_asset* a, gb_scene_desc* d) {
     d->params = a->params.empty() ? nullptr : a->params.data();
     d->num_lights = (int)a->lights.size();
     d->lights = a->lights.empty() ? nullptr : a->lights.data();
+    bool any_tex = false;
+    for (int t : a->dtex) any_tex = any_tex || t >= 0;
+    d->num_textures = (int)a->textures.size();
+    d->textures = a->textures.empty() ? nullptr : a->textures.data();
+    d->texcoords = any_tex ? a->tc.data() : nullptr;
+    d->diffuse_texture = any_tex ? a->dtex.data() : nullptr;
     return GB_OK;
 }
 

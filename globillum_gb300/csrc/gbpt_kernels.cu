@@ -428,6 +428,22 @@ __global__ void k_jitter_pool(Frame F, RenderParams P) {
     st_mrg(F.jcursor, (size_t)g, s);
 }
 
+// Ray differentials of a slot, 12 floats in 3 planes of nslots float4.
+__device__ __forceinline__ RayDiff ld_rdiff(const Frame& F, uint32_t slot) {
+    const float4 a = F.rdiff[slot], b = F.rdiff[(size_t)F.nslots + slot], c = F.rdiff[2 * (size_t)F.nslots + slot];
+    RayDiff r;
+    r.uo = mk(a.x, a.y, a.z);
+    r.ud = mk(a.w, b.x, b.y);
+    r.ro = mk(b.z, b.w, c.x);
+    r.rd = mk(c.y, c.z, c.w);
+    return r;
+}
+__device__ __forceinline__ void st_rdiff(const Frame& F, uint32_t slot, const RayDiff& r) {
+    F.rdiff[slot] = make_float4(r.uo.x, r.uo.y, r.uo.z, r.ud.x);
+    F.rdiff[(size_t)F.nslots + slot] = make_float4(r.ud.y, r.ud.z, r.ro.x, r.ro.y);
+    F.rdiff[2 * (size_t)F.nslots + slot] = make_float4(r.ro.z, r.rd.x, r.rd.y, r.rd.z);
+}
+
 __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t l) {
     int lo = 0, hi = P.rounds - 1;
     while (lo < hi) {  // round holding path l
@@ -461,6 +477,7 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
     F.pix[slot] = gpix;
     F.ps[slot] = sc;
     F.pb[slot] = ((uint32_t)P.p0 + (uint32_t)lo) << 10;
+    if (R.S.texcoord) st_rdiff(F, slot, camera_diff(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w)));
 }
 
 // Counter set of iteration `it`: [0] queue count, [1] extension head,
@@ -803,7 +820,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                 F.psc[slot] = make_float4(psc.x, psc.y, psc.z, scale);
                 F.rnd[slot] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
                 F.hit_p[slot] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
-                F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, 0.0f);
+                F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id));
             }
         }
         push(fin && hit, slot, qsh, cs + 2);
@@ -845,7 +862,9 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
 }
 
-__device__ __forceinline__ MaterialRec load_material(const float* mats, uint32_t mi) {
+// Material record of index mi; the texture fields (last float4) only when
+// the scene has textures.
+__device__ __forceinline__ MaterialRec load_material(const float* mats, uint32_t mi, bool textured = false) {
     float mf[kMaterialFloats];
     const float4* mp = (const float4*)(mats + (size_t)kMaterialFloats * mi);
 #pragma unroll
@@ -853,6 +872,8 @@ __device__ __forceinline__ MaterialRec load_material(const float* mats, uint32_t
         float4 q = __ldg(mp + k);
         mf[4 * k] = q.x; mf[4 * k + 1] = q.y; mf[4 * k + 2] = q.z; mf[4 * k + 3] = q.w;
     }
+    float4 q = textured ? __ldg(mp + 7) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    mf[28] = q.x; mf[29] = q.y; mf[30] = q.z; mf[31] = q.w;
     return unpack_material(mf);
 }
 
@@ -865,13 +886,34 @@ __device__ __forceinline__ int nee_light(const Frame& F, const SceneRec& R, uint
     return pick_light(R.S.lights, R.S.n_lights, R.S.overall_power, lz);
 }
 
+// Hit of a path in a textured scene: the ray differentials move to the hit
+// (computeRayDiffs, hybrid-pt.cpp:518-519) and a diffuse texture scales the
+// material's base colour.  The hit's barycentrics are recomputed with the
+// traversal's own triangle test (same operands, same bits).
+__device__ __noinline__ void texture_hit(const Frame& F, const SceneRec& R, uint32_t slot, float4 hn,
+                                         MaterialRec* m) {
+    const uint32_t tid = __float_as_uint(hn.w);
+    const float4* sh = R.S.shade + 6 * (size_t)tid;
+    const v3 a = ld3(__ldg(sh)), b = ld3(__ldg(sh + 1)), c = ld3(__ldg(sh + 2));
+    float t, bb = 0.0f, bg = 0.0f;
+    intersect_tri(ld3(F.ray_o[slot]), ld3(F.ray_d[slot]), a, b - a, c - a, &t, &bb, &bg);
+    const float* tcs = R.S.texcoord + 6 * (size_t)tid;
+    float ts, tt;
+    bary2(bb, bg, tcs, &ts, &tt);
+    RayDiff df = ld_rdiff(F, slot);
+    const float diff = ray_diff_hit(&df, a, b, c, tcs, ts, tt, normalize_div(ld3(hn)));
+    st_rdiff(F, slot, df);
+    if (m->dtex >= 0 && m->dtex < R.S.n_tex)
+        *m = textured_material(*m, tex_sample_bilin_lod(R.S.tex[m->dtex], ts, tt, diff));
+}
+
 // BRDF sample/eval, NEE accumulation and next ray for every shadow-queue
 // entry (compute_path_contribution_and_bounce for the hits); paths that end
 // go to the free queue.  MODE_FROZEN evaluates the BRDF with the scene's
 // eval records and carries the sampling throughput in tp0; MODE_ADJOINT
 // writes the vertex record of the path-replay adjoint.  Every path leaves
 // with pb's bounce field = the number of vertices it shaded.
-template <int MODE>
+template <int MODE, bool TEX>
 __global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
@@ -891,7 +933,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
             float4 sd = F.sh_d[slot];
             float4 hp = F.hit_p[slot], hn = F.hit_n[slot];
             uint32_t mi = __float_as_uint(hp.w);
-            MaterialRec m = load_material(R.S.mats, mi);
+            const bool textured = TEX && R.S.texcoord != nullptr;
+            MaterialRec m = load_material(R.S.mats, mi, textured);
+            if (textured) texture_hit(F, R, slot, hn, &m);
             uint32_t pbv = F.pb[slot];
             int bounce = (int)(pbv & 1023u);
             uint32_t path = pbv >> 10;
@@ -1031,6 +1075,16 @@ __global__ void __launch_bounds__(kBlock) k_direct(DevScene S, CameraRec cam, in
         N = bary(hit.beta, hit.gamma, ld3(sh[3]), ld3(sh[4]), ld3(sh[5]));
         const float* mf = S.mats + (size_t)kMaterialFloats * __float_as_uint(a.w);
         mcol = mk(mf[25], mf[26], mf[27]);
+        const int dtex = (int)mf[31];
+        if (S.texcoord && dtex >= 0 && dtex < S.n_tex) {
+            // pixel_evaluate_material_bilin_lod_cpu (material-cpu.cpp:36-77)
+            const float* tcs = S.texcoord + 6 * (size_t)hit.id;
+            float ts, tt;
+            bary2(hit.beta, hit.gamma, tcs, &ts, &tt);
+            RayDiff df = camera_diff(cam, g % w, g / w);
+            const float diff = ray_diff_hit(&df, ld3(a), ld3(sh[1]), ld3(sh[2]), tcs, ts, tt, N);
+            mcol = mcol * tex_sample_bilin_lod(S.tex[dtex], ts, tt, diff);
+        }
     }
     curandStateMRG32k3a st;
     curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &st);
@@ -1292,27 +1346,19 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
     return cudaGetLastError();
 }
 
-// Grid of the streaming per-path kernels (k_shade, k_regen), whose entry
-// counts are known only on the device: with GB_WIDE_STREAM_GRIDS one thread
-// per possible entry (the slot count), so every entry's dependent loads are
-// in flight at once; otherwise a persistent grid looping over the entries.
-#ifndef GB_WIDE_STREAM_GRIDS
-#define GB_WIDE_STREAM_GRIDS 0
-#endif
-inline int stream_grid(int persistent, int nslots) {
-    return GB_WIDE_STREAM_GRIDS ? std::max(1, blocks_for(nslots)) : persistent;
-}
-
-template <int MODE>
+template <int MODE, bool TEX>
 void launch_shade_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
-    static int g = persistent_blocks(k_shade<MODE>);
-    k_shade<MODE><<<stream_grid(g, F.nslots), kBlock, 0, st>>>(F, P);
+    static int g = persistent_blocks(k_shade<MODE, TEX>);
+    k_shade<MODE, TEX><<<g, kBlock, 0, st>>>(F, P);
 }
 
+// The texture path is compiled into its own variant so that frames without
+// textures run the kernel without it; replay and adjoint frames have none.
 cudaError_t k_launch_shade(const Frame& F, const RenderParams& P, cudaStream_t st) {
-    if (P.mode == MODE_FROZEN) launch_shade_t<MODE_FROZEN>(F, P, st);
-    else if (P.mode == MODE_ADJOINT) launch_shade_t<MODE_ADJOINT>(F, P, st);
-    else launch_shade_t<MODE_FORWARD>(F, P, st);
+    if (P.mode == MODE_FROZEN) launch_shade_t<MODE_FROZEN, false>(F, P, st);
+    else if (P.mode == MODE_ADJOINT) launch_shade_t<MODE_ADJOINT, false>(F, P, st);
+    else if (P.textured) launch_shade_t<MODE_FORWARD, true>(F, P, st);
+    else launch_shade_t<MODE_FORWARD, false>(F, P, st);
     return cudaGetLastError();
 }
 
@@ -1347,7 +1393,7 @@ cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, do
 
 cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g0 = persistent_blocks(k_regen);
-    k_regen<<<stream_grid(g0, F.nslots), kBlock, 0, st>>>(F, P);
+    k_regen<<<g0, kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
 }
 

@@ -25,6 +25,11 @@ struct DevScene {
     const float* mats_eval;
     const LightRec* lights_eval;
     SkyRec sky;  // the scene's sky light (sky.light = -1 when it has none)
+    // textures: 6 texture coordinates per canonical triangle (null when the
+    // scene has none; then no ray differentials are kept either)
+    const float* texcoord;
+    const TexRec* tex;
+    int n_tex;
 };
 
 // The six 32-bit component words of a curandStateMRG32k3a (s1[3], s2[3]):
@@ -74,7 +79,8 @@ struct Frame {
     float4* psc;       // potential_sample_contribution
     float4* rnd;       // path draw of this bounce
     float4* hit_p;     // hit point xyz | material index bits
-    float4* hit_n;     // interpolated (unnormalised) normal
+    float4* hit_n;     // interpolated (unnormalised) normal | hit triangle id bits
+    float4* rdiff;     // ray differentials of textured scenes: 3 planes of nslots (RayDiff packed)
     MrgState* rng;     // light/path stream of the slot's path
     uint32_t* pix;     // global pixel of the slot's path
     uint32_t* ps;      // scene of the slot's path
@@ -112,6 +118,7 @@ struct RenderParams {
                        // 3: warp-cooperative triangle tests, then a node
     int blocks_per_sm; // resident blocks per SM of the traversal kernels (0 = occupancy limit)
     int mode;          // MODE_*
+    int textured;      // some scene of the frame has textures (k_shade's texture variant)
     int p0, rounds;    // path samples p0 .. p0+rounds-1
     uint32_t chunk_paths;  // paths of the chunk
     uint32_t round_start[kMaxRounds + 1];  // first path index of each round (prefix sums of N_p)

@@ -130,6 +130,12 @@ GB_HD v3 bary(float beta, float gamma, v3 a, v3 b, v3 c) {
     float w = (1.0f - beta) - gamma;
     return (w * a + beta * b) + gamma * c;
 }
+// The same for texture coordinates: t = 6 floats (ta, tb, tc), out (s, t).
+GB_HD void bary2(float beta, float gamma, const float* t, float* s_out, float* t_out) {
+    float w = (1.0f - beta) - gamma;
+    *s_out = (w * t[0] + beta * t[2]) + gamma * t[4];
+    *t_out = (w * t[1] + beta * t[3]) + gamma * t[5];
+}
 
 // ------------------------------------------------------ ray/triangle test --
 // Moller-Trumbore (intersect_tri_opt in rta is not available; this is the
@@ -151,6 +157,18 @@ GB_HD bool intersect_tri(v3 o, v3 d, v3 v0, v3 e1, v3 e2, float* t, float* beta,
     if (!(tt > 0.0f)) return false;
     *t = tt; *beta = u; *gamma = v;
     return true;
+}
+
+// intersect_tri_opt_nocheck (rta, absent; "actually just a plane
+// intersection", hybrid-pt.cpp:308-313): the same arithmetic without any
+// range check, so the barycentrics of the hit with the triangle's plane.
+GB_HD void plane_bary(v3 o, v3 d, v3 v0, v3 e1, v3 e2, float* beta, float* gamma) {
+    v3 p = fcross(d, e2);
+    float inv = 1.0f / fdot(e1, p);
+    v3 s = o - v0;
+    *beta = fdot(s, p) * inv;
+    v3 q = fcross(s, e1);
+    *gamma = fdot(d, q) * inv;
 }
 
 // closest-hit acceptance: lexicographic minimum of (t, canonical id) over
@@ -242,10 +260,8 @@ GB_HD void camera_frame(v3 view, v3 up, v3* U, v3* V, v3* W) {
 
 // jitter = (rnd.x, rnd.y) of the jitter stream; lens = aperture sample
 // (zero when aperture == 0, where it is multiplied by zero in the reference).
-GB_HD void camera_ray(const CameraRec& c, int x, int y, float jx_r, float jy_r, float lens_x, float lens_y,
-                      v3* org, v3* dir) {
-    float jx = float(x) + jx_r;
-    float jy = float(y) + jy_r;
+// Shirley direction through the image-plane point (jx, jy) in pixels.
+GB_HD v3 camera_dir(const CameraRec& c, float jx, float jy) {
     float u_s = ((jx) / (float)c.w) * 2.0f - 1.0f;
     float v_s = ((jy) / (float)c.h) * 2.0f - 1.0f;
     u_s = c.width * u_s;
@@ -253,12 +269,37 @@ GB_HD void camera_ray(const CameraRec& c, int x, int y, float jx_r, float jy_r, 
     v3 d = c.U * u_s;
     d = d + c.V * v_s;
     d = d + c.W;
-    d = normalize_div(d);
+    return normalize_div(d);
+}
+
+GB_HD void camera_ray(const CameraRec& c, int x, int y, float jx_r, float jy_r, float lens_x, float lens_y,
+                      v3* org, v3* dir) {
+    v3 d = camera_dir(c, float(x) + jx_r, float(y) + jy_r);
     v3 focal = c.pos + (d * (1.0f / dot(d, c.view))) * c.focus;
     v3 jp = (c.pos + (c.U * lens_x) * c.aperture) + (c.V * lens_y) * c.aperture;
     d = focal - jp;
     *dir = normalize_div(d);
     *org = jp;
+}
+
+// Ray differentials of a path (hybrid-pt.cpp:300-328): origin and
+// direction of the "upper" and "right" neighbour rays.
+struct RayDiff { v3 uo, ud, ro, rd; };
+
+// The camera's differentials.  They come from rta's
+// camera_ray_generator_shirley<gpu_ray_generator_with_differentials>, which
+// the jittered lens generator runs first and which "generates ray
+// differentials based on a uniform ray distribution" (raygen.h:49-52, :86-90);
+// rta is not available, so the uniform generator is taken to be the
+// pixel-centre Shirley camera and the neighbours to be pixels (x, y+1) and
+// (x+1, y), both from the eye.
+GB_HD RayDiff camera_diff(const CameraRec& c, int x, int y) {
+    RayDiff r;
+    r.uo = c.pos;
+    r.ud = camera_dir(c, float(x) + 0.5f, float(y + 1) + 0.5f);
+    r.ro = c.pos;
+    r.rd = camera_dir(c, float(x + 1) + 0.5f, float(y) + 0.5f);
+    return r;
 }
 
 // ----------------------------------------------------------------- lights --
@@ -470,6 +511,135 @@ GB_HD void rect_light_sample(const LightRec& l, v3 col, float overall_power, v3 
 // material_t (material.h:142-184) + PrincipledBRDFParameters
 // (principledParameters.h:7-24), flattened with the per-material constants
 // of principledMaterial.h:178-252 precomputed on the host.
+// --------------------------------------------------------------- textures --
+// texture_data (material.h:21-137) after convert_texture
+// (material-conversion.cpp:18-35): RGBA8 texels, row 0 at t = 1, mip levels
+// stored one after the other (level i+1 is ((W+1)/2) x ((H+1)/2) of level
+// i; compute_mipmaps, material.cu:259-275).  The buffer holds `size`
+// texels: the levels and a zero tail, so that the reads sample_bilin_lod
+// makes one row or one texel past a level (t = 0 gives y = H; x = W for the
+// right neighbour of the last column) stay inside it.
+struct TexRec {
+    const uint8_t* texels;   // 4 bytes per texel
+    int w, h, max_mm;        // max_mm = floor(log2(min(w, h)))
+    int size;                // texels in the buffer
+};
+
+GB_HD v3 tex_texel(const TexRec& t, int i) {
+    i = i < 0 ? 0 : (i >= t.size ? t.size - 1 : i);  // never taken by the reads below
+#ifdef __CUDA_ARCH__
+    uchar4 q = __ldg((const uchar4*)t.texels + i);
+    return mk(float(q.x) / 255.0f, float(q.y) / 255.0f, float(q.z) / 255.0f);
+#else
+    const uint8_t* p = t.texels + 4 * (size_t)i;
+    return mk(float(p[0]) / 255.0f, float(p[1]) / 255.0f, float(p[2]) / 255.0f);
+#endif
+}
+
+// Mip levels sample_bilin_lod steps down: its loop `for (i = 0; i < lod; ++i)`
+// with lod = fminf(log2f(x), max_mm) runs min(ceil(log2 x), max_mm) times
+// when x > 1, max_mm times for NaN, none otherwise.  ceil(log2 x) is taken
+// from the binary exponent of x, which is exact; a rounded log2f differs
+// from it only for x within about an ulp above a power of two.
+GB_HD int tex_levels(float x, int max_mm) {
+    if (x != x) return max_mm;
+    if (!(x > 1.0f)) return 0;
+    if (x > FLT_MAX) return max_mm;
+    int e;
+    float m = frexpf(x, &e);  // x = m 2^e, m in [0.5, 1)
+    int c = m == 0.5f ? e - 1 : e;
+    return c < max_mm ? c : max_mm;
+}
+
+// texture_data::sample_bilin_lod (material.h:88-137): level chosen by the
+// footprint `diff` in texture space, coordinates wrapped into [0, 1), the
+// nearest texel and its neighbour towards the sample point blended with
+// weights |neighbour centre - x|.  The neighbour index wraps only when it
+// is negative or more than one past the level (`other_x > W`), as in the
+// reference, so x = W and y = H read the texel after the row / level.
+GB_HD v3 tex_sample_bilin_lod(const TexRec& t, float s, float tt, float diff) {
+    int W = t.w, H = t.h;
+    int levels = tex_levels(diff * fmaxf((float)t.w, (float)t.h), t.max_mm);
+    int offset = 0;
+    for (int i = 0; i < levels; ++i) {
+        offset += W * H;
+        W = (W + 1) / 2;
+        H = (H + 1) / 2;
+    }
+    if (s < 0) s += -truncf(s) + 1;
+    if (s >= 1) s -= truncf(s);
+    if (tt < 0) tt += -truncf(tt) + 1;
+    if (tt >= 1) tt -= truncf(tt);
+    float x = s * (float)W;
+    float y = (1.0f - tt) * (float)H;
+    int nx = int(x), ny = int(y);
+    int ox = nx + 1, oy = ny + 1;
+    if (x - floorf(x) < .5f) ox = nx - 1;
+    if (y - floorf(y) < .5f) oy = ny - 1;
+    // (float(o) + .5 - x) of the reference is exact in double; its float
+    // rounding equals this float subtraction
+    float wx = fabsf(((float)ox + .5f) - x);
+    float wy = fabsf(((float)oy + .5f) - y);
+    if (ox > W) ox -= W;
+    if (ox < 0) ox += W;
+    if (oy > H) oy -= H;
+    if (oy < 0) oy += H;
+    v3 a00 = tex_texel(t, offset + ny * W + nx);
+    v3 a01 = tex_texel(t, offset + ny * W + ox);
+    v3 a10 = tex_texel(t, offset + oy * W + nx);
+    v3 a11 = tex_texel(t, offset + oy * W + ox);
+    v3 a0x = wx * a00 + (1.0f - wx) * a01;
+    v3 a1x = wx * a10 + (1.0f - wx) * a11;
+    return wy * a0x + (1.0f - wy) * a1x;
+}
+
+// computeRayDiffs (hybrid-pt.cpp:300-328) and the footprint of
+// material_t::diffuseColor (material.h:159-170) at a hit on triangle
+// (a, b, c) with texture coordinates tcs (6 floats), hit texture
+// coordinate (ts, tt) and normalised normal N: both neighbour rays meet the
+// triangle's plane, their texture coordinates give the footprint; the
+// origins move to those points and the upper direction is reflected about
+// N (the right direction is left as it was, as in the reference).
+GB_HD float ray_diff_hit(RayDiff* rd, v3 a, v3 b, v3 c, const float* tcs, float ts, float tt, v3 N) {
+    v3 e1 = b - a, e2 = c - a;
+    float ub, ug, rb, rg, us, ut, rs, rt;
+    plane_bary(rd->uo, rd->ud, a, e1, e2, &ub, &ug);
+    bary2(ub, ug, tcs, &us, &ut);
+    v3 up = bary(ub, ug, a, b, c);
+    plane_bary(rd->ro, rd->rd, a, e1, e2, &rb, &rg);
+    bary2(rb, rg, tcs, &rs, &rt);
+    v3 rp = bary(rb, rg, a, b, c);
+    rd->uo = up;
+    rd->ro = rp;
+    rd->ud = reflect(rd->ud, N);
+    float dx = fabsf(ts - us);
+    float dy = fabsf(tt - ut);
+    dx = fmaxf(fabsf(ts - rs), dx);
+    dy = fmaxf(fabsf(tt - rt), dy);
+    return fmaxf(dx, dy);
+}
+
+// x^2.2 in double for the textured colours of principled materials
+// (mon2lin, principledMaterial.h:226): ln x from the atanh series of the
+// mantissa reduced to [sqrt(1/2), sqrt(2)), exp by reduction to
+// |r| <= ln(2)/2 and its Taylor polynomial.  Written out here (not pow) so
+// that host and device give the same bits; error below 1e-14 relative.
+GB_HD double pow22(double x) {
+    if (x != x || x < 0.0) return (x - x) / (x - x);  // NaN, as pow of a negative base
+    if (x == 0.0) return 0.0;
+    const double kLn2 = 0.69314718055994530942;
+    int e;
+    double m = frexp(x, &e);
+    if (m < 0.70710678118654752440) { m *= 2.0; e -= 1; }
+    double z = (m - 1.0) / (m + 1.0), z2 = z * z, p = 1.0 / 25.0;
+    for (int k = 23; k >= 1; k -= 2) p = p * z2 + 1.0 / (double)k;
+    double y = 2.2 * (2.0 * z * p + (double)e * kLn2);
+    double kf = floor(y / kLn2 + 0.5);
+    double r = y - kf * kLn2, q = 1.0;
+    for (int k = 18; k >= 1; --k) q = q * (r / (double)k) + 1.0;
+    return ldexp(q, (int)kf);
+}
+
 enum { MAT_LAMBERT = 0, MAT_PRINCIPLED = 1 };
 struct MaterialRec {
     int kind;
@@ -481,6 +651,8 @@ struct MaterialRec {
     float cspec0[3];           // :231
     float cc_a, cc_a2m1, cc_pilog;  // GTR1 constants        :186-192, :241
     float kd[3];               // material_t::diffuse_color (evaluate_material, material-cpu.cpp:20-80)
+    float sheen_tint, specular_tint, specular;  // to recompute the colour terms for a texture
+    int dtex;                  // diffuse texture (index into the scene's textures) or -1
 };
 static const int kMaterialFloats = 32;  // padded device record size
 
@@ -494,6 +666,47 @@ GB_HD MaterialRec unpack_material(const float* f) {
     for (int k = 0; k < 3; ++k) { r.cdlin[k] = f[13 + k]; r.csheen[k] = f[16 + k]; r.cspec0[k] = f[19 + k]; }
     r.cc_a = f[22]; r.cc_a2m1 = f[23]; r.cc_pilog = f[24];
     r.kd[0] = f[25]; r.kd[1] = f[26]; r.kd[2] = f[27];
+    r.sheen_tint = f[28]; r.specular_tint = f[29]; r.specular = f[30];
+    r.dtex = (int)f[31];
+    return r;
+}
+
+// The colour terms of a principled record (make_material) for base colour
+// c, principledMaterial.h:226-231, :276.  Shared by the host set-up and the
+// texture path so both give the same bits.
+GB_HD void material_colour_terms(MaterialRec* r, const float* c, bool own_pow) {
+    float cdlin[3];
+    for (int k = 0; k < 3; ++k) {
+        r->diffuse[k] = c[k];
+#ifdef __CUDA_ARCH__
+        cdlin[k] = (float)pow22((double)c[k]);
+        (void)own_pow;
+#else
+        cdlin[k] = own_pow ? (float)pow22((double)c[k]) : (float)pow((double)c[k], 2.2);
+#endif
+    }
+    float cdlum = (float)(.3 * cdlin[0] + .6 * cdlin[1] + .1 * cdlin[2]);
+    float ctint[3];
+    for (int k = 0; k < 3; ++k) ctint[k] = cdlum > 0 ? cdlin[k] / cdlum : 1.0f;
+    float spec08 = (float)((double)r->specular * .08);
+    for (int k = 0; k < 3; ++k) {
+        r->cdlin[k] = cdlin[k];
+        r->csheen[k] = (1.0f - r->sheen_tint) * 1.0f + r->sheen_tint * ctint[k];
+        float st = (1.0f - r->specular_tint) * 1.0f + r->specular_tint * ctint[k];
+        float a = spec08 * st;
+        r->cspec0[k] = (1.0f - r->metallic) * a + r->metallic * cdlin[k];
+    }
+}
+
+// material_t::diffuseColor with a diffuse texture (material.h:159-170): the
+// base colour (diffuse_color, or parameters->color for principled
+// materials) times the texture sample, used by both the Lambert and the
+// principled model (simpleMaterial.h:95, principledMaterial.h:327).
+GB_HD MaterialRec textured_material(const MaterialRec& m, v3 tex) {
+    MaterialRec r = m;
+    float c[3] = {m.diffuse[0] * tex.x, m.diffuse[1] * tex.y, m.diffuse[2] * tex.z};
+    if (m.kind == MAT_PRINCIPLED) material_colour_terms(&r, c, true);
+    else for (int k = 0; k < 3; ++k) r.diffuse[k] = c[k];
     return r;
 }
 

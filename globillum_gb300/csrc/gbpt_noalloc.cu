@@ -129,6 +129,8 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
         return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad fovy");
     int dev = scene_device(scene);
     if (dev < 0 || dev >= kMaxDevices) return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad scene device");
+    if (scene_device_view(scene)->texcoord)
+        return fail(scene, GB_ERR_UNSUPPORTED, "gb_render_noalloc: scenes with texture coordinates need gb_render");
     if (cudaSetDevice(dev) != cudaSuccess) { cudaGetLastError(); return fail(scene, GB_ERR_CUDA, "cudaSetDevice failed"); }
     unsigned char* base = nullptr;
     if (scratch_on_device(dev, &base) != cudaSuccess) {

@@ -41,11 +41,16 @@ class Light(C.Structure):
                 ("sky_scale", C.c_float), ("sky_diameter", C.c_float)]
 
 
+class Texture(C.Structure):
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("rgba", C.c_void_p)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("num_triangles", C.c_int), ("positions", C.c_void_p), ("normals", C.c_void_p),
                 ("material_index", C.c_void_p), ("num_materials", C.c_int), ("materials", C.POINTER(Material)),
                 ("num_params", C.c_int), ("params", C.POINTER(PrincipledParams)), ("num_lights", C.c_int),
-                ("lights", C.POINTER(Light))]
+                ("lights", C.POINTER(Light)), ("num_textures", C.c_int), ("textures", C.POINTER(Texture)),
+                ("texcoords", C.c_void_p), ("diffuse_texture", C.c_void_p)]
 
 
 class SceneInfo(C.Structure):
@@ -238,9 +243,20 @@ def make_scene_desc(scene) -> tuple[SceneDesc, list]:
         else:
             lights[i] = Light(t, float(l.get("power", -1.0)), _f3(l["center"]), _f3(l["dir"]),
                               _f3(l.get("up", (0, 0, 1))), _f3(l["col"]), (C.c_float * 2)(*[float(x) for x in l["wh"]]))
+    # textures: (h, w, 4) uint8 images, texcoords (n, 6), material key "diffuse_texture"
+    texs = [np.ascontiguousarray(t, np.uint8) for t in (getattr(scene, "textures", None) or [])]
+    tex_arr = (Texture * max(1, len(texs)))()
+    for i, t in enumerate(texs):
+        if t.ndim != 3 or t.shape[2] != 4:
+            raise ValueError("textures must be (h, w, 4) uint8 arrays")
+        tex_arr[i] = Texture(int(t.shape[1]), int(t.shape[0]), _ptr(t))
+    tc = getattr(scene, "texcoords", None)
+    tc = None if tc is None else np.ascontiguousarray(tc, np.float32)
+    dt = np.array([int(m.get("diffuse_texture", -1)) for m in scene.materials], np.int32)
     d = SceneDesc(int(pos.shape[0]), _ptr(pos), _ptr(nrm), _ptr(mid), len(scene.materials), mats,
-                  len(scene.params), params, len(scene.lights), lights)
-    return d, [pos, nrm, mid, mats, params, lights, maps]
+                  len(scene.params), params, len(scene.lights), lights, len(texs), tex_arr, _ptr(tc),
+                  _ptr(dt) if (dt >= 0).any() else None)
+    return d, [pos, nrm, mid, mats, params, lights, maps, texs, tex_arr, tc, dt]
 
 
 class Context:
@@ -549,5 +565,15 @@ class Asset:
             l = d.lights[i]
             lights.append({"type": int(l.type), "power": float(l.power), "center": tuple(l.center), "dir": tuple(l.dir),
                            "up": tuple(l.up), "col": tuple(l.col), "wh": tuple(l.wh)})
+        textures, tc = [], None
+        if d.diffuse_texture:
+            dt = np.ctypeslib.as_array(C.cast(d.diffuse_texture, C.POINTER(C.c_int)), shape=(d.num_materials,))
+            for i, m in enumerate(mats):
+                m["diffuse_texture"] = int(dt[i])
+            for k in range(d.num_textures):
+                t = d.textures[k]
+                textures.append(np.ctypeslib.as_array(C.cast(t.rgba, C.POINTER(C.c_uint8)),
+                                                      shape=(t.h, t.w, 4)).copy())
+            tc = np.ctypeslib.as_array(C.cast(d.texcoords, fp), shape=(n, 6)).copy()
         return SceneData(pos.astype(np.float32), nrm.astype(np.float32), mid.astype(np.int32), mats, params, lights,
-                         dict(camera or {}), dict(render or {}), name=name)
+                         dict(camera or {}), dict(render or {}), name=name, textures=textures, texcoords=tc)

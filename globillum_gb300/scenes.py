@@ -35,6 +35,8 @@ class SceneData:
     camera: dict = field(default_factory=dict)
     render: dict = field(default_factory=dict)
     name: str = ""
+    textures: list = field(default_factory=list)  # (h, w, 4) uint8 images, row 0 at t = 1
+    texcoords: np.ndarray | None = None            # (n, 6) float32: ta, tb, tc
 
     @property
     def num_triangles(self) -> int:
@@ -249,6 +251,42 @@ def procedural_sky(width: int = 64, height: int = 32, sun=(0.35, 0.2), seed: int
     sky = sky + (np.exp(-d2 / (2 * 0.08 ** 2)) * 40.0)[..., None] * np.array([1.0, 0.9, 0.7])
     sky = sky * (1.0 + 0.05 * rng.standard_normal(sky.shape))
     return np.clip(sky, 0.0, None).astype(np.float32)
+
+
+def checker_texture(size: int = 64, cells: int = 8, seed: int = 0) -> np.ndarray:
+    """(size, size, 4) uint8 checkerboard of two seeded colours with value
+    noise on top (so that mip levels differ from the base level)."""
+    rng = np.random.default_rng(seed)
+    c0, c1 = rng.integers(30, 226, size=(2, 3))
+    y, x = np.mgrid[0:size, 0:size]
+    chk = ((x * cells // size + y * cells // size) % 2)[..., None]
+    img = np.where(chk == 1, c1, c0).astype(np.float64)
+    img += rng.integers(-25, 26, size=img.shape)
+    out = np.empty((size, size, 4), np.uint8)
+    out[..., :3] = np.clip(img, 0, 255).astype(np.uint8)
+    out[..., 3] = 255
+    return out
+
+
+def with_textures(scene: SceneData, n_textures: int = 2, size: int = 64, fraction: float = 0.5, scale: float = 1.0,
+                  seed: int = 0) -> SceneData:
+    """A copy of `scene` with diffuse textures: planar texture coordinates
+    (s, t) = scale * (x + z, y + 0.5 z) per corner, n_textures checkerboards,
+    each material textured with probability `fraction`."""
+    rng = np.random.default_rng(seed)
+    p = scene.positions.reshape(-1, 3, 3).astype(np.float64)
+    tc = np.stack([scale * (p[..., 0] + p[..., 2]), scale * (p[..., 1] + 0.5 * p[..., 2])], axis=-1)
+    mats = []
+    for m in scene.materials:
+        m = dict(m)
+        m["diffuse_texture"] = int(rng.integers(0, n_textures)) if rng.uniform() < fraction else -1
+        mats.append(m)
+    if all(m["diffuse_texture"] < 0 for m in mats):
+        mats[0]["diffuse_texture"] = 0
+    return SceneData(scene.positions, scene.normals, scene.material_index, mats, scene.params, scene.lights,
+                     dict(scene.camera), dict(scene.render), name=scene.name + "+tex",
+                     textures=[checker_texture(size, 4 + 4 * k, seed + k) for k in range(n_textures)],
+                     texcoords=tc.reshape(-1, 6).astype(np.float32))
 
 
 def param_vector(scene: SceneData) -> np.ndarray:

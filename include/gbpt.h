@@ -95,6 +95,12 @@ typedef struct {
     float sky_scale, sky_diameter;
 } gb_light;
 
+/* An RGBA8 image of w x h texels (4 bytes each, rows top first). */
+typedef struct {
+    int w, h;
+    const uint8_t* rgba;
+} gb_texture;
+
 typedef struct {
     int num_triangles;
     const float* positions;       /* 9 floats per triangle: a, b, c           */
@@ -106,6 +112,17 @@ typedef struct {
     const gb_principled_params* params;
     int num_lights;
     const gb_light* lights;
+    /* Diffuse textures (material_t::diffuse_texture, material.h:142-170):
+     * textures[k] is RGBA8 with row 0 at t = 1 (texture_data after
+     * convert_texture, material-conversion.cpp:18-35); mip levels are made at
+     * scene creation (compute_mipmaps, material.cu:259-275).  texcoords holds
+     * 6 floats per triangle (ta, tb, tc as (s, t)); diffuse_texture holds one
+     * texture index or -1 per material.  All three may be 0 / NULL; a
+     * description must be zero-initialised for callers without textures. */
+    int num_textures;
+    const gb_texture* textures;
+    const float* texcoords;
+    const int* diffuse_texture;
 } gb_scene_desc;
 
 typedef struct {
@@ -278,8 +295,10 @@ int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg
 /* Scene assets gathered on the host into one gb_scene_desc, as the
  * reference's loader does (add_objfile_to_flat_tri_list, hl-main.cpp:277-354;
  * convert_and_upload_materials, material-conversion.cpp:59-148; the light /
- * add-rectlight forms, lights.scm:4-9 and lights.cpp:84-96).  Textures and
- * sky lights are not modelled (texture maps are ignored, sky forms skipped). */
+ * add-rectlight forms, lights.scm:4-9 and lights.cpp:84-96).  Diffuse
+ * texture maps (MTL map_Kd) are read when they are PPM files (P6 or P3, maxval
+ * <= 255); other image formats are left out (the material keeps its Kd).
+ * Sky forms of scene scripts are skipped. */
 typedef struct gb_asset gb_asset;
 int gb_asset_create(gb_asset** out);
 void gb_asset_destroy(gb_asset* asset);
@@ -291,7 +310,8 @@ const char* gb_asset_last_error(const gb_asset* asset);
  * becomes a principled material when material_dir/<name>.pbrdf exists
  * (material_dir may be NULL), else Lambert with the MTL's Kd; faces without a
  * known material use the fallback material 0 (Lambert (1, 0, 0), created with
- * the first OBJ). */
+ * the first OBJ).  Texture coordinates (vt, "v/vt/vn" corners) are kept, 0 for
+ * corners without one. */
 int gb_asset_add_obj(gb_asset* asset, const char* obj_path, const char* material_dir, const float* trafo);
 /* Appends the rectangular lights of a scene script: every (light "name"
  * :type :rect :color (list r g b) :pos (list ...) :dir (list ...) :up (list ...)

@@ -66,6 +66,12 @@ struct OScene {
     // sky light tables (sky.light = -1 without one)
     SkyTables sky_tab;
     SkyRec sky{};
+    // textures (orc_scene_set_textures): 6 texture coordinates per triangle,
+    // mip chains; textured = some material has a diffuse texture
+    bool textured = false;
+    std::vector<float> tc;
+    std::vector<std::vector<uint8_t>> tex_data;
+    std::vector<TexRec> tex;
     // descriptions the differentiable parameters come from
     std::vector<gb_material> mats_in;
     std::vector<gb_principled_params> params_in;
@@ -408,6 +414,10 @@ struct AdjVertex {
     v3 wo, wi, N, ld;
 };
 
+int shade_stage(const OScene& s, int w, int h, const gb_render_desc* desc, float* ray_orig, float* ray_dir,
+                float* max_t, const gb_hit* hits, const uint8_t* occl, const float* rnd, float* tp, float* accum,
+                const float* to_light, const float* psc, int path, int bounce, int pixel_base, RayDiff* rdiff);
+
 }  // namespace
 
 extern "C" {
@@ -465,6 +475,34 @@ void* orc_scene_create(int n, const float* pos, const float* nrm, const int* mat
 
 void orc_scene_destroy(void* s) { delete (OScene*)s; }
 
+// Diffuse textures of a scene (gb_scene_desc's texture fields): mip chains
+// by make_mipmaps, texture index per material.  Returns 1 for bad input.
+int orc_scene_set_textures(void* sp, int ntex, const gb_texture* tex, const float* texcoords, const int* dtex) {
+    OScene& s = *(OScene*)sp;
+    if (ntex < 0 || (ntex > 0 && !tex)) return 1;
+    s.tex_data.assign((size_t)ntex, std::vector<uint8_t>());
+    s.tex.assign((size_t)ntex, TexRec{});
+    for (int k = 0; k < ntex; ++k) {
+        if (!tex[k].rgba || tex[k].w <= 0 || tex[k].h <= 0) return 1;
+        make_mipmaps(tex[k].rgba, tex[k].w, tex[k].h, &s.tex_data[k], &s.tex[k].max_mm, &s.tex[k].size);
+        s.tex[k].texels = s.tex_data[k].data();
+        s.tex[k].w = tex[k].w;
+        s.tex[k].h = tex[k].h;
+    }
+    s.textured = false;
+    for (size_t m = 0; m < s.mats.size(); ++m) {
+        const int v = dtex ? dtex[m] : -1;
+        if (v < -1 || v >= ntex) return 1;
+        s.mats[m].dtex = v;
+        s.textured = s.textured || v >= 0;
+    }
+    if (s.textured) {
+        if (!texcoords) return 1;
+        s.tc.assign(texcoords, texcoords + 6 * (size_t)s.n);
+    }
+    return 0;
+}
+
 int orc_trace_closest(void* sp, int n, const float* o, const float* d, const float* tmax, gb_hit* hits,
                       uint64_t* counts) {
     const OScene& s = *(const OScene*)sp;
@@ -516,7 +554,21 @@ int orc_compute_path_contribution_and_bounce(void* sp, int w, int h, const gb_re
                                              const uint8_t* occl, const float* rnd, float* tp, float* accum,
                                              const float* to_light, const float* psc, int path, int bounce,
                                              int pixel_base) {
-    const OScene& s = *(const OScene*)sp;
+    return shade_stage(*(const OScene*)sp, w, h, desc, ray_orig, ray_dir, max_t, hits, occl, rnd, tp, accum, to_light,
+                       psc, path, bounce, pixel_base, nullptr);
+}
+
+}  // extern "C"
+
+namespace {
+
+// compute_path_contribution_and_bounce (hybrid-pt.cpp:450-584) over a
+// w x h block; rdiff (textured scenes) holds each pixel's ray
+// differentials, moved to the hit by computeRayDiffs (:300-328) before the
+// material is set up with the texture's colour.
+int shade_stage(const OScene& s, int w, int h, const gb_render_desc* desc, float* ray_orig, float* ray_dir,
+                float* max_t, const gb_hit* hits, const uint8_t* occl, const float* rnd, float* tp, float* accum,
+                const float* to_light, const float* psc, int path, int bounce, int pixel_base, RayDiff* rdiff) {
     ShadeParams par = make_shade_params(*desc);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = 0; y < h; ++y)
@@ -529,7 +581,17 @@ int orc_compute_path_contribution_and_bounce(void* sp, int w, int h, const gb_re
             if (hh.ref != 0xffffffffu) {
                 v3 P = tri_interp(s.pos, (int)hh.ref, hh.beta, hh.gamma);
                 v3 N = tri_interp(s.nrm, (int)hh.ref, hh.beta, hh.gamma);
-                const MaterialRec& m = s.mats[s.mat[hh.ref]];
+                MaterialRec m = s.mats[s.mat[hh.ref]];
+                if (s.textured && rdiff) {
+                    const float* p = &s.pos[9 * (size_t)hh.ref];
+                    const float* tcs = &s.tc[6 * (size_t)hh.ref];
+                    float ts, tt;
+                    bary2(hh.beta, hh.gamma, tcs, &ts, &tt);
+                    const float diff = ray_diff_hit(&rdiff[id], mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]),
+                                                    mk(p[6], p[7], p[8]), tcs, ts, tt, normalize_div(N));
+                    if (m.dtex >= 0 && m.dtex < (int)s.tex.size())
+                        m = textured_material(m, tex_sample_bilin_lod(s.tex[m.dtex], ts, tt, diff));
+                }
                 ShadeOut o = shade_hit(m, P, N, mk(ray_dir[3 * id], ray_dir[3 * id + 1], ray_dir[3 * id + 2]), t,
                                        mk(rnd[3 * id], rnd[3 * id + 1], rnd[3 * id + 2]), occl[id] == 0,
                                        mk(to_light[3 * id], to_light[3 * id + 1], to_light[3 * id + 2]),
@@ -560,6 +622,11 @@ int orc_compute_path_contribution_and_bounce(void* sp, int w, int h, const gb_re
     return 0;
 }
 
+
+}  // namespace
+
+extern "C" {
+
 // Full progressive frame over rows [row0, row1) of a w x h image.
 // pool: `pool_updates` updates of the rows' pixels, layout
 // [update][pixel - row0*w][3]; needs spp*L updates.  out_rgb: (row1-row0)*w*3.
@@ -578,6 +645,7 @@ int orc_render(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0
         ps(3 * (size_t)n), tp(3 * (size_t)n), ac(3 * (size_t)n), lr(3 * (size_t)n), rnd(3 * (size_t)n);
     std::vector<gb_hit> hits(n);
     std::vector<uint8_t> occl(n);
+    std::vector<RayDiff> rdf(s.textured ? (size_t)n : 0);
     std::fill(out_rgb, out_rgb + 3 * (size_t)n, 0.0f);
     uint64_t n_cam = 0, n_ext = 0, n_sh = 0, n_vis = 0, n_tst = 0;
     for (int p = 0; p < d->spp; ++p) {
@@ -598,6 +666,7 @@ int orc_render(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0
             ro[3 * i] = o.x; ro[3 * i + 1] = o.y; ro[3 * i + 2] = o.z;
             rd[3 * i] = dd.x; rd[3 * i + 1] = dd.y; rd[3 * i + 2] = dd.z;
             mt[i] = FLT_MAX;
+            if (s.textured) rdf[i] = camera_diff(C, x, y);
             tp[3 * i] = tp[3 * i + 1] = tp[3 * i + 2] = 1.0f;
             ac[3 * i] = ac[3 * i + 1] = ac[3 * i + 2] = 0.0f;
         }
@@ -638,9 +707,8 @@ int orc_render(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0
                 cs += 1;
             }
             n_sh += cs;
-            orc_compute_path_contribution_and_bounce(sp, W, h, d, ro.data(), rd.data(), mt.data(), hits.data(),
-                                                     occl.data(), rnd.data(), tp.data(), ac.data(), sd.data(),
-                                                     ps.data(), p, b, base);
+            shade_stage(s, W, h, d, ro.data(), rd.data(), mt.data(), hits.data(), occl.data(), rnd.data(), tp.data(),
+                        ac.data(), sd.data(), ps.data(), p, b, base, s.textured ? rdf.data() : nullptr);
         }
         // new_path: moving average
 #pragma omp parallel for schedule(static)
@@ -799,6 +867,17 @@ int orc_render_direct(void* sp, const gb_camera* cam, const gb_render_desc* d, i
             N = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
             const MaterialRec& m = s.mats[s.mat[h.ref]];
             mcol = mk(m.kd[0], m.kd[1], m.kd[2]);
+            if (s.textured && m.dtex >= 0 && m.dtex < (int)s.tex.size()) {
+                // pixel_evaluate_material_bilin_lod_cpu (material-cpu.cpp:36-77)
+                const float* p = &s.pos[9 * (size_t)h.ref];
+                const float* tcs = &s.tc[6 * (size_t)h.ref];
+                float ts, tt;
+                bary2(h.beta, h.gamma, tcs, &ts, &tt);
+                RayDiff df = camera_diff(C, g % W, g / W);
+                const float diff = ray_diff_hit(&df, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]),
+                                                tcs, ts, tt, N);
+                mcol = mcol * tex_sample_bilin_lod(s.tex[m.dtex], ts, tt, diff);
+            }
         }
         v3 buf_dir = dd, acc = mk(0.0f, 0.0f, 0.0f);
         for (int k = 0; k < samples; ++k) {
@@ -909,6 +988,35 @@ int orc_dist1d(int n, const float* data, int m, const float* u, float* x, float*
     std::vector<float> pdf(n), cdf(n + 1);
     dist1d_init(data, n, pdf.data(), cdf.data());
     for (int i = 0; i < m; ++i) dist1d_sample(cdf.data(), pdf.data(), n, u[i], &x[i], &p[i]);
+    return 0;
+}
+
+// Texture helpers for the known-answer tests: the mip chain of make_mipmaps
+// (out must hold 4 * (total + w + 1) bytes; returns the texel count in
+// *size), sample_bilin_lod of n points, and pow22.
+int orc_mipmaps(const uint8_t* rgba, int w, int h, uint8_t* out, long long cap_bytes, int* max_mm, int* size) {
+    std::vector<uint8_t> v;
+    make_mipmaps(rgba, w, h, &v, max_mm, size);
+    if ((long long)v.size() > cap_bytes) return 1;
+    std::memcpy(out, v.data(), v.size());
+    return 0;
+}
+int orc_tex_sample(const uint8_t* rgba, int w, int h, int n, const float* sc, const float* tc, const float* diff,
+                   float* out) {
+    std::vector<uint8_t> v;
+    TexRec t;
+    make_mipmaps(rgba, w, h, &v, &t.max_mm, &t.size);
+    t.texels = v.data();
+    t.w = w;
+    t.h = h;
+    for (int i = 0; i < n; ++i) {
+        v3 c = tex_sample_bilin_lod(t, sc[i], tc[i], diff[i]);
+        out[3 * i] = c.x; out[3 * i + 1] = c.y; out[3 * i + 2] = c.z;
+    }
+    return 0;
+}
+int orc_pow22(int n, const double* x, double* out) {
+    for (int i = 0; i < n; ++i) out[i] = pow22(x[i]);
     return 0;
 }
 

@@ -29,6 +29,7 @@ def load() -> C.CDLL:
         vp, ip, fp = C.c_void_p, C.c_int, C.c_float
         lib.orc_scene_create.restype = vp
         lib.orc_scene_create.argtypes = [ip, vp, vp, vp, ip, vp, ip, vp, ip, vp, ip]
+        lib.orc_scene_set_textures.argtypes = [vp, ip, vp, vp, vp]
         lib.orc_scene_destroy.argtypes = [vp]
         lib.orc_scene_destroy.restype = None
         lib.orc_trace_closest.argtypes = [vp, ip, vp, vp, vp, vp, vp]
@@ -67,6 +68,10 @@ class OracleScene:
                                            C.cast(desc.lights, C.c_void_p), 1 if use_bvh else 0)
         if not self.h:
             raise ValueError("oracle scene creation failed")
+        if desc.diffuse_texture:
+            if self.lib.orc_scene_set_textures(self.h, desc.num_textures, C.cast(desc.textures, C.c_void_p),
+                                               desc.texcoords, desc.diffuse_texture) != 0:
+                raise ValueError("oracle texture set-up failed")
 
     def close(self):
         if self.h:
@@ -242,6 +247,36 @@ def dist1d(data, u):
     p = np.empty_like(u)
     load().orc_dist1d(d.shape[0], _p(d), u.shape[0], _p(u), _p(x), _p(p))
     return x, p
+
+
+def mipmaps(rgba: np.ndarray):
+    """make_mipmaps of an (h, w, 4) uint8 image: (chain of texels (N, 4), max_mm, size)."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    h, w = img.shape[:2]
+    cap = 4 * (2 * w * h + 4 * (w + h) + 64)
+    out = np.zeros(cap, np.uint8)
+    mm, size = C.c_int(), C.c_int()
+    lib = load()
+    if lib.orc_mipmaps(_p(img), w, h, _p(out), C.c_longlong(cap), C.byref(mm), C.byref(size)) != 0:
+        raise ValueError("mip chain larger than the buffer")
+    return out[:4 * size.value].reshape(-1, 4), mm.value, size.value
+
+
+def tex_sample(rgba: np.ndarray, s, t, diff) -> np.ndarray:
+    """sample_bilin_lod of the points (s, t) with footprints diff: (n, 3)."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    h, w = img.shape[:2]
+    s, t, diff = (np.ascontiguousarray(a, np.float32) for a in (s, t, diff))
+    out = np.empty((s.size, 3), np.float32)
+    load().orc_tex_sample(_p(img), w, h, s.size, _p(s), _p(t), _p(diff), _p(out))
+    return out
+
+
+def pow22(x) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty_like(x)
+    load().orc_pow22(x.size, _p(x), _p(out))
+    return out
 
 
 def threads() -> int:

@@ -125,3 +125,32 @@ def test_reference_bundled_assets(lib_path):
         a.add_lights(REF / script)
     assert len(a.scene_data().lights) >= 1
     a.close()
+
+
+def test_obj_texture_coordinates_and_ppm_maps(tmp_path, lib_path):
+    """vt / "v/vt/vn" corners and MTL map_Kd with PPM images (P6 and P3);
+    a map in another format leaves the material untextured."""
+    rgb = np.arange(2 * 3 * 3, dtype=np.uint8).reshape(2, 3, 3) * 10
+    (tmp_path / "tex").mkdir()
+    with open(tmp_path / "tex" / "a.ppm", "wb") as f:
+        f.write(b"P6\n# comment\n3 2\n255\n" + rgb.tobytes())
+    (tmp_path / "b.ppm").write_text("P3\n1 1\n15\n15 0 5\n")
+    (tmp_path / "m.mtl").write_text("newmtl A\nKd 1 1 1\nmap_Kd tex/a.ppm\n"
+                                    "newmtl B\nKd 0.5 0.5 0.5\nmap_Kd -s 1 1 1 b.ppm\n"
+                                    "newmtl C\nKd 0.2 0.2 0.2\nmap_Kd c.png\n")
+    (tmp_path / "t.obj").write_text(
+        "mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0.25 0.75\nvn 0 0 1\n"
+        "usemtl A\nf 1/1/1 2/2/1 3/3/1 4/4/1\nusemtl B\nf 1/1 3/3 4\nusemtl C\nf 1 2 3\n")
+    a = gbpt.Asset()
+    a.add_obj(tmp_path / "t.obj")
+    sd = a.scene_data()
+    assert [m["diffuse_texture"] for m in sd.materials] == [-1, 0, 1, -1]
+    assert np.array_equal(sd.textures[0][..., :3], rgb) and (sd.textures[0][..., 3] == 255).all()
+    assert sd.textures[1][0, 0].tolist() == [255, 0, 85, 255]  # maxval 15 rescaled
+    assert np.allclose(sd.texcoords[0], [0, 0, 1, 0, 1, 1]) and np.allclose(sd.texcoords[1], [0, 0, 1, 1, 0.25, 0.75])
+    assert np.allclose(sd.texcoords[2], [0, 0, 1, 1, 0, 0])  # the corner without vt
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nvt 0 0\nf 1/1 2/2 3/1\n")
+    with pytest.raises(gbpt.GBError, match="texture coordinate index"):
+        a.add_obj(bad)
+    a.close()
