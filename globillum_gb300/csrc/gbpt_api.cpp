@@ -70,7 +70,7 @@ struct gb_ctx {
     int paths_done = 0;                 // rounds done
     bool active = false;
     bool instrument = false;
-    bool use_graph = false;             // run chunks as CUDA graphs (conditional while loop)
+    bool use_graph = true;              // run chunks as CUDA graphs (conditional while loop)
     int mode = MODE_FORWARD;            // render mode of the next chunks
     // frozen-sampling replay and adjoint buffers
     std::vector<void*> adj_allocs;
@@ -1467,6 +1467,38 @@ int gb_render_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const g
     CK(k_launch_direct(scene->S, make_camera(*cam, d->width, d->height), d->width, d->height, light_samples, d->seed,
                        d->shadow_offset, mk(d->background[0], d->background[1], d->background[2]), dst,
                        ctx->d_status, ctx->stream));
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (!out_is_device) CK(cudaMemcpyAsync(out_rgb, dst, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->stats.render_ms = ms;
+    ctx->stats.kernel_launches = 1;
+    cudaGetLastError();
+    return check_status(ctx);
+}
+
+int gb_render_hybrid_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* d,
+                            int camera_samples, int light_samples, float* out_rgb, int out_is_device) {
+    if (!ctx || !scene) return fail(ctx, GB_ERR_INVALID, "null context or scene");
+    int rc = check_render_desc(ctx, cam, d);
+    if (rc != GB_OK) return rc;
+    if (camera_samples <= 0 || light_samples <= 0 || (long long)camera_samples * light_samples > (1 << 20))
+        return fail(ctx, GB_ERR_INVALID, "bad camera / light sample counts");
+    if (!out_rgb) return fail(ctx, GB_ERR_INVALID, "null output");
+    CK(cudaSetDevice(ctx->device));
+    const int n = d->width * d->height;
+    const size_t bytes = sizeof(float) * 3 * (size_t)n;
+    float* dst = out_rgb;
+    if (!out_is_device) {
+        CK(ensure_scratch(ctx, 0, bytes));
+        dst = (float*)ctx->scratch[0].p;
+    }
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    CK(k_launch_direct_hybrid(scene->S, make_camera(*cam, d->width, d->height), d->width, d->height, camera_samples,
+                              light_samples, d->seed, d->shadow_offset,
+                              mk(d->background[0], d->background[1], d->background[2]), dst, ctx->d_status,
+                              ctx->stream));
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!out_is_device) CK(cudaMemcpyAsync(out_rgb, dst, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

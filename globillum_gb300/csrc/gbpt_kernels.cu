@@ -1120,6 +1120,95 @@ __global__ void __launch_bounds__(kBlock) k_direct(DevScene S, CameraRec cam, in
     out[3 * g + 2] = acc.z;
 }
 
+// hybrid_area_lights (direct-lighting.cpp:203-316, direct-lighting.h:137-215):
+// per pixel `cam_samples` jittered camera rays (jittered lens generator,
+// jitter pool update c), the material colour of each camera hit
+// (evaluate_material, material-cpu.cpp:20-80; footprint from the camera
+// differentials), and `light_samples` samples of the CPU area-light sampler
+// per camera sample (generate_arealight_sample, arealight-sampler-cpu.cpp:
+// 25-143) folded into one moving average over sample c * L + j.  Sample j of
+// a camera sample is set up before the pool's update of that step, so
+// samples 0 and 1 share update c*L and sample j >= 2 takes c*L + j - 1; the
+// L-th update of each camera sample goes unused.  All pools are seeded
+// alike in the reference (curand_init(0, pixel, 0), util-kernels.cu:276-285),
+// so the jitter and light draws are one stream read twice.
+__global__ void __launch_bounds__(kBlock) k_direct_hybrid(DevScene S, CameraRec cam, int w, int h, int cam_samples,
+                                                          int light_samples, uint32_t seed, float shadow_offset,
+                                                          v3 background, float* out, uint32_t* status) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= w * h) return;
+    const int px = g % w, py = g / w;
+    curandStateMRG32k3a js, ls, lens;
+    curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &js);
+    curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &ls);
+    const bool aperture = cam.aperture != 0.0f;
+    if (aperture) curand_init((unsigned long long)seed, (unsigned long long)((g + 17) % (w * h)), 0ull, &lens);
+    const int L = light_samples;
+    v3 acc = mk(0.0f, 0.0f, 0.0f);
+    for (int c = 0; c < cam_samples; ++c) {
+        const v3 j = draw3(&js);
+        float lx = 0.0f, ly = 0.0f;
+        if (aperture) {
+            const v3 lj = draw3(&lens);
+            lx = lj.z - 0.5f;
+            ly = lj.y - 0.5f;
+        }
+        v3 o, d;
+        camera_ray(cam, px, py, j.x, j.y, lx, ly, &o, &d);
+        TraceOut hit;
+        const bool is_hit = traverse<false>(S, make_ray(o, d), FLT_MAX, &hit, status);
+        v3 P = mk(0.0f, 0.0f, 0.0f), N = P, mcol = background;
+        if (is_hit) {
+            const float4* sh = S.shade + 6 * (size_t)hit.id;
+            const float4 a = sh[0];
+            P = bary(hit.beta, hit.gamma, ld3(a), ld3(sh[1]), ld3(sh[2]));
+            N = bary(hit.beta, hit.gamma, ld3(sh[3]), ld3(sh[4]), ld3(sh[5]));
+            const float* mf = S.mats + (size_t)kMaterialFloats * __float_as_uint(a.w);
+            mcol = mk(mf[25], mf[26], mf[27]);
+            const int dtex = (int)mf[31];
+            if (S.texcoord && dtex >= 0 && dtex < S.n_tex) {
+                const float* tcs = S.texcoord + 6 * (size_t)hit.id;
+                float ts, tt;
+                bary2(hit.beta, hit.gamma, tcs, &ts, &tt);
+                RayDiff df = camera_diff(cam, px, py);
+                const float diff = ray_diff_hit(&df, ld3(a), ld3(sh[1]), ld3(sh[2]), tcs, ts, tt, N);
+                mcol = mcol * tex_sample_bilin_lod(S.tex[dtex], ts, tt, diff);
+            }
+        }
+        v3 buf_dir = d;
+        v3 rnd = draw3(&ls);
+        for (int k = 0; k < L; ++k) {
+            if (k >= 2) rnd = draw3(&ls);
+            v3 weight = mk(0.0f, 0.0f, 0.0f);
+            bool occluded = false;
+            if (is_hit && S.n_lights > 0) {
+                const int l = pick_light(S.lights, S.n_lights, S.overall_power, rnd.z);
+                const LightRec Lr = S.lights[l];
+                v3 so, sd;
+                float smax;
+                if (Lr.type == 1)
+                    sky_light_sample(S.sky, Lr.power, S.overall_power, P, N, rnd.x, rnd.y, shadow_offset, &so, &sd,
+                                     &smax, &weight);
+                else
+                    rect_light_sample(Lr, Lr.col, S.overall_power, P, N, rnd.x, rnd.y, shadow_offset, &so, &sd,
+                                      &smax, &weight);
+                buf_dir = sd;
+                occluded = smax >= 0.0f && traverse<true>(S, make_ray(so, sd), smax, nullptr, status);
+            } else {
+                if (S.sky.light >= 0) weight = S.sky.scale * sky_eval(S.sky, buf_dir);
+                buf_dir = mk(0.0f, 0.0f, 0.0f);
+            }
+            const v3 mat = occluded ? mk(0.0f, 0.0f, 0.0f) : mcol;
+            const float s = float(c * L + k);
+            acc = (s * acc + weight * mat) / (s + 1.0f);
+        }
+        if (L >= 2) draw3(&ls);
+    }
+    out[3 * g] = acc.x;
+    out[3 * g + 1] = acc.y;
+    out[3 * g + 2] = acc.z;
+}
+
 __global__ void k_dimg_pack(const float* __restrict__ src, int n, float scale, float4* dst) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1376,6 +1465,15 @@ cudaError_t k_launch_direct(const DevScene& S, const CameraRec& cam, int w, int 
                             float shadow_offset, v3 background, float* out, uint32_t* status, cudaStream_t st) {
     if (w * h <= 0) return cudaSuccess;
     k_direct<<<blocks_for(w * h), kBlock, 0, st>>>(S, cam, w, h, samples, seed, shadow_offset, background, out, status);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_direct_hybrid(const DevScene& S, const CameraRec& cam, int w, int h, int cam_samples,
+                                   int light_samples, uint32_t seed, float shadow_offset, v3 background, float* out,
+                                   uint32_t* status, cudaStream_t st) {
+    if (w * h <= 0) return cudaSuccess;
+    k_direct_hybrid<<<blocks_for(w * h), kBlock, 0, st>>>(S, cam, w, h, cam_samples, light_samples, seed,
+                                                          shadow_offset, background, out, status);
     return cudaGetLastError();
 }
 

@@ -140,6 +140,9 @@ cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t
 cudaError_t k_launch_adjoint(const Frame& F, const RenderParams& P, cudaStream_t st);
 cudaError_t k_launch_direct(const DevScene& S, const CameraRec& cam, int w, int h, int samples, uint32_t seed,
                             float shadow_offset, v3 background, float* out, uint32_t* status, cudaStream_t st);
+cudaError_t k_launch_direct_hybrid(const DevScene& S, const CameraRec& cam, int w, int h, int cam_samples,
+                                   int light_samples, uint32_t seed, float shadow_offset, v3 background, float* out,
+                                   uint32_t* status, cudaStream_t st);
 int k_adjoint_grid();
 cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st);
 cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, double* out, cudaStream_t st);

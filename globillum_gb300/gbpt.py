@@ -116,7 +116,7 @@ EXPORTS = [
     "gb_autotune", "gb_scene_param_count", "gb_scene_get_params", "gb_scene_set_params", "gb_forward",
     "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
     "gb_asset_add_obj", "gb_asset_add_lights", "gb_asset_add_light", "gb_asset_get_desc", "gb_asset_material_name",
-    "gb_read_pbrdf", "gb_render_direct", "gb_scene_create_ex", "gb_scene_refit",
+    "gb_read_pbrdf", "gb_render_direct", "gb_scene_create_ex", "gb_scene_refit", "gb_render_hybrid_direct",
 ]
 
 _lib = None
@@ -183,6 +183,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_asset_material_name.argtypes = [vp, ip, C.POINTER(C.c_char_p)]
     lib.gb_read_pbrdf.argtypes = [C.c_char_p, C.POINTER(PrincipledParams)]
     lib.gb_render_direct.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), ip, vp, ip]
+    lib.gb_render_hybrid_direct.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), ip, ip, vp, ip]
     if path is None:
         _lib = lib
     return lib
@@ -418,6 +419,16 @@ class Scene:
         out = np.empty((rd.height, rd.width, 3), dtype=np.float32)
         self.ctx.check(self.ctx.lib.gb_render_direct(self.ctx.h, self.h, C.byref(make_camera(cam)), C.byref(rd),
                                                      int(light_samples), _ptr(out), 0))
+        return out
+
+    def render_hybrid_direct(self, cam: dict, rdesc: dict, camera_samples: int = 2,
+                             light_samples: int = 2) -> np.ndarray:
+        """gb_render_hybrid_direct: the hybrid_area_lights image (h, w, 3)."""
+        rd = make_render_desc(rdesc)
+        out = np.empty((rd.height, rd.width, 3), dtype=np.float32)
+        self.ctx.check(self.ctx.lib.gb_render_hybrid_direct(self.ctx.h, self.h, C.byref(make_camera(cam)),
+                                                            C.byref(rd), int(camera_samples), int(light_samples),
+                                                            _ptr(out), 0))
         return out
 
     # ------------------------------------------------------ differentiation

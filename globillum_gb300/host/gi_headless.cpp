@@ -5,7 +5,8 @@
 //
 //   gi_headless <scene.bin> <out.pfm> [-r WxH] [-s spp] [-l path_length]
 //               [--offsets ray shadow] [--halton] [--rr bounce]
-//               [--algo hybrid_pt|gpu_area_lights] [--light-samples n]
+//               [--algo hybrid_pt|gpu_area_lights|hybrid_area_lights] [--light-samples n]
+//               (hybrid_area_lights: -s camera samples, --light-samples per camera sample)
 //
 // scene.bin (written by globillum_gb300.scenes.write_scene_bin): magic
 // "GBSC", version 2, counts, then positions, normals, material indices,
@@ -89,7 +90,7 @@ int main(int argc, char** argv) {
     if (argc < 3) {
         std::fprintf(stderr,
                      "usage: %s scene.bin out.pfm [-r WxH] [-s spp] [-l len] [--offsets r s] [--halton] [--rr b]"
-                     " [--algo hybrid_pt|gpu_area_lights] [--light-samples n]\n",
+                     " [--algo hybrid_pt|gpu_area_lights|hybrid_area_lights] [--light-samples n]\n",
                      argv[0]);
         return 2;
     }
@@ -130,9 +131,11 @@ int main(int argc, char** argv) {
     try {
         gb::init_path_samples() = spp;
         gb::init_path_length() = len;
-        // both algorithms register, one is selected (hl-main.cpp:617-628)
+        // the algorithms register, one is selected (hl-main.cpp:612-628)
         gb::hybrid_pt algo(w, h);
         gb::gpu_area_lights direct(w, h);
+        gb::hybrid_area_lights hybrid_direct(w, h);
+        hybrid_direct.render_desc().shadow_offset = so;
         algo.render_desc().ray_offset = ro;
         algo.render_desc().shadow_offset = so;
         algo.render_desc().rng_mode = halton ? GB_RNG_HALTON_LIGHT : GB_RNG_MRG32K3A_POOL;
@@ -140,15 +143,18 @@ int main(int argc, char** argv) {
         gb::gi_algorithm::original_rt_set() = &set;
         gb::gi_algorithm::select(algo_name);
         gb::gi_algorithm* a = gb::gi_algorithm::selected();
-        if (a == &direct) a->light_samples(light_samples);
+        if (a == &direct || a == &hybrid_direct) a->light_samples(light_samples);
+        if (a == &hybrid_direct) a->path_samples(spp);
         a->compute();
         while (a->in_progress()) a->update();
-        std::vector<float> img = a == &algo ? algo.result() : direct.result();
+        std::vector<float> img = a == &algo ? algo.result() : a == &direct ? direct.result() : hybrid_direct.result();
         if (!write_pfm(argv[2], w, h, img)) { std::fprintf(stderr, "cannot write %s\n", argv[2]); return 1; }
         if (a == &algo)
             std::printf("rendered %dx%d, %d paths of length %d per pixel\n", w, h, algo.paths_done(), len);
-        else
+        else if (a == &direct)
             std::printf("rendered %dx%d, %d direct light samples per pixel\n", w, h, light_samples);
+        else
+            std::printf("rendered %dx%d, %d camera x %d light samples per pixel\n", w, h, spp, light_samples);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "error: %s\n", e.what());
         return 1;

@@ -230,4 +230,63 @@ public:
     std::vector<float> result() const { return image; }
 };
 
+// hybrid_area_lights (direct-lighting.cpp:203-316): `path_samples` jittered
+// camera samples per pixel, each with `light_samples` samples of the CPU
+// area-light sampler, over gb_render_hybrid_direct.  The reference's
+// constructor hands init_light_samples to the camera-sample count and
+// init_path_samples to the per-camera light-sample count
+// (direct-lighting.cpp:222-226 against direct-lighting.h:152-157); the
+// knobs then set each count by its own name.  Both start at 2.
+class hybrid_area_lights : public gi_algorithm {
+protected:
+    int w, h;
+    gb_ctx* ctx = nullptr;
+    gb_scene* scene = nullptr;
+    gb_camera cam{};
+    gb_render_desc desc{};
+    int cam_samples = 2, samples_per_cam = 2;
+    std::vector<float> image;
+
+public:
+    hybrid_area_lights(int w, int h, const std::string& name = "hybrid_area_lights")
+        : gi_algorithm(name), w(w), h(h) {
+        desc.width = w; desc.height = h;
+        desc.spp = 1; desc.max_bounces = 1;
+        desc.rng_mode = GB_RNG_MRG32K3A_POOL;
+        desc.seed = 0;
+        desc.shadow_offset = 0.9f;  // the CPU sampler's offset (arealight-sampler-cpu.cpp:115)
+        desc.background[0] = desc.background[1] = desc.background[2] = 1.0f;
+        desc.rr_start = -1;
+    }
+    ~hybrid_area_lights() override {
+        if (scene) gb_scene_destroy(scene);
+        if (ctx) gb_ctx_destroy(ctx);
+    }
+    void activate(rt_set* set) override {
+        if (activated) return;
+        if (!set || !set->scene) throw std::runtime_error("hybrid_area_lights::activate: no scene");
+        gi_algorithm::activate(set);
+        gb_ctx_desc cd{set->device, nullptr};
+        int rc = gb_ctx_create(&cd, &ctx);
+        if (rc != GB_OK) throw std::runtime_error("gb_ctx_create failed (" + std::to_string(rc) + ")");
+        gb_check(ctx, gb_scene_create(ctx, set->scene, &scene), "gb_scene_create");
+        cam = set->camera;
+    }
+    void set_camera(const gb_camera& c) { cam = c; }
+    gb_render_desc& render_desc() { return desc; }
+    void compute() override {
+        if (!activated) throw std::runtime_error("hybrid_area_lights::compute before activate");
+        desc.width = w; desc.height = h;
+        image.assign((size_t)w * h * 3, 0.0f);
+        gb_check(ctx, gb_render_hybrid_direct(ctx, scene, &cam, &desc, cam_samples, samples_per_cam, image.data(), 0),
+                 "gb_render_hybrid_direct");
+    }
+    void update() override {}
+    bool progressive() override { return true; }
+    bool in_progress() override { return false; }
+    void light_samples(int n) override { samples_per_cam = n; }
+    void path_samples(int n) override { cam_samples = n; }
+    std::vector<float> result() const { return image; }
+};
+
 }  // namespace gb

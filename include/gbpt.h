@@ -222,6 +222,19 @@ int gb_render_read(gb_ctx* ctx, float* out_rgb, int out_is_device);
  * pixel's MRG32k3a stream, as the reference's pool updates fall. */
 int gb_render_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
                      int light_samples, float* out_rgb, int out_is_device);
+/* The reference's hybrid direct-lighting integrator hybrid_area_lights
+ * (direct-lighting.cpp:203-316, direct-lighting.h:137-215): per pixel
+ * `camera_samples` jittered camera rays (the jittered lens generator of
+ * hybrid_pt, jitter update c for camera sample c), the material colour of
+ * each camera hit as in gb_render_direct, and per camera sample
+ * `light_samples` samples of the CPU area-light sampler (the one hybrid_pt's
+ * light samples use: desc->shadow_offset, 0.9 in the reference, and
+ * importance-sampled sky), averaged over all camera x light samples.  Light
+ * sample j of camera sample c draws update c*L + max(0, j-1) of the pixel's
+ * MRG32k3a stream, as the reference's pool updates fall; jitter and light
+ * draws come from the same stream (the reference seeds all its pools alike). */
+int gb_render_hybrid_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
+                            int camera_samples, int light_samples, float* out_rgb, int out_is_device);
 
 /* ------------------------------------------------------------ batching */
 /* One scene of a batch: its own camera, resolution, spp, bounces, RNG mode
@@ -409,7 +422,7 @@ typedef struct {
                        4 = the warp tests all lanes' pending triangles together
                        (32 at a time), then every lane visits one node */
     int graph;      /* 1 = the host drives the slot-pool loop of single renders; 2 = each
-                       chunk runs as one CUDA graph with a conditional while loop */
+                       chunk runs as one CUDA graph with a conditional while loop (default) */
     int blocks_per_sm; /* resident 128-thread blocks per SM of the persistent traversal
                           kernels + 1: 1 = as many as occupancy allows, k + 1 = at most k */
 } gb_tuning;

@@ -912,6 +912,69 @@ int orc_render_direct(void* sp, const gb_camera* cam, const gb_render_desc* d, i
     return 0;
 }
 
+// hybrid_area_lights (direct-lighting.cpp:203-316, direct-lighting.h:137-215)
+// on pools [update][pixel][3]: camera sample c takes jitter update c (and the
+// lens jitter of pixel (g + 17) mod n, update c), light sample j of camera
+// sample c takes update c*L + max(0, j-1); needs max(C, C*L) updates.
+int orc_render_hybrid_direct(void* sp, const gb_camera* cam, const gb_render_desc* d, int cam_samples,
+                             int light_samples, const float* pool, int pool_updates, float* out_rgb) {
+    const OScene& s = *(const OScene*)sp;
+    const int W = d->width, H = d->height, n = W * H, L = light_samples;
+    if (cam_samples <= 0 || L <= 0 || pool_updates < std::max(cam_samples, cam_samples * L)) return 1;
+    CameraRec C = make_camera(*cam, W, H);
+    const v3 bg = mk(d->background[0], d->background[1], d->background[2]);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int g = 0; g < n; ++g) {
+        const int x = g % W, y = g / W;
+        v3 acc = mk(0.0f, 0.0f, 0.0f);
+        for (int c = 0; c < cam_samples; ++c) {
+            const float* jp = pool + ((size_t)c * n + g) * 3;
+            float lx = 0.0f, ly = 0.0f;
+            if (C.aperture != 0.0f) {
+                const float* lp = pool + ((size_t)c * n + (g + 17) % n) * 3;
+                lx = lp[2] - 0.5f;
+                ly = lp[1] - 0.5f;
+            }
+            v3 o, dd;
+            camera_ray(C, x, y, jp[0], jp[1], lx, ly, &o, &dd);
+            gb_hit h = trace_closest(s, o, dd, FLT_MAX, nullptr, nullptr);
+            const bool hit = h.ref != 0xffffffffu;
+            v3 mcol = bg;
+            if (hit) {
+                const v3 N = tri_interp(s.nrm, (int)h.ref, h.beta, h.gamma);
+                const MaterialRec& m = s.mats[s.mat[h.ref]];
+                mcol = mk(m.kd[0], m.kd[1], m.kd[2]);
+                if (s.textured && m.dtex >= 0 && m.dtex < (int)s.tex.size()) {
+                    const float* p = &s.pos[9 * (size_t)h.ref];
+                    const float* tcs = &s.tc[6 * (size_t)h.ref];
+                    float ts, tt;
+                    bary2(h.beta, h.gamma, tcs, &ts, &tt);
+                    RayDiff df = camera_diff(C, x, y);
+                    const float diff = ray_diff_hit(&df, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]),
+                                                    mk(p[6], p[7], p[8]), tcs, ts, tt, N);
+                    mcol = mcol * tex_sample_bilin_lod(s.tex[m.dtex], ts, tt, diff);
+                }
+            }
+            v3 buf_dir = dd;
+            for (int j = 0; j < L; ++j) {
+                const float* up = pool + ((size_t)(c * L + std::max(0, j - 1)) * n + g) * 3;
+                v3 so, sd = buf_dir, psc;
+                float smax;
+                nee_pixel(s, g, h, mk(up[0], up[1], up[2]), d->shadow_offset, &so, &sd, &smax, &psc);
+                buf_dir = sd;
+                const bool occluded = hit && !s.lights.empty() && smax >= 0.0f && trace_any(s, so, sd, smax);
+                const v3 mat = occluded ? mk(0.0f, 0.0f, 0.0f) : mcol;
+                const float sc = float(c * L + j);
+                acc = (sc * acc + psc * mat) / (sc + 1.0f);
+            }
+        }
+        out_rgb[3 * (size_t)g] = acc.x;
+        out_rgb[3 * (size_t)g + 1] = acc.y;
+        out_rgb[3 * (size_t)g + 2] = acc.z;
+    }
+    return 0;
+}
+
 // Halton pool of util.cpp:38-51 for pixels [0, n): (h2(i+1), h3(i+1)).
 int orc_halton_pool(int n, float* out) {
     for (int i = 0; i < n; ++i) { out[2 * i] = halton(i + 1, 2); out[2 * i + 1] = halton(i + 1, 3); }

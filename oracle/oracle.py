@@ -40,6 +40,7 @@ def load() -> C.CDLL:
         lib.orc_render.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp]
         lib.orc_adjoint_f64.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp, vp]
         lib.orc_render_direct.argtypes = [vp, vp, vp, ip, vp, ip, vp]
+        lib.orc_render_hybrid_direct.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp]
         lib.orc_halton_pool.argtypes = [ip, vp]
         lib.orc_material_sample_eval.argtypes = [vp] * 12
         lib.orc_sincos_2pi.argtypes = [ip, vp, vp, vp]
@@ -147,6 +148,19 @@ class OracleScene:
                                         _p(out))
         if rc != 0:
             raise ValueError(f"orc_render_direct failed ({rc})")
+        return out
+
+    def render_hybrid_direct(self, cam: dict, rdesc: dict, cam_samples: int, light_samples: int,
+                             pool: np.ndarray) -> np.ndarray:
+        """hybrid_area_lights frame; pool: (updates, pixels, 3), updates >= max(C, C * L)."""
+        rd = _gbpt.make_render_desc(rdesc)
+        cm = _gbpt.make_camera(cam)
+        pool = np.ascontiguousarray(pool, np.float32)
+        out = np.empty((rd.height, rd.width, 3), np.float32)
+        rc = self.lib.orc_render_hybrid_direct(self.h, C.byref(cm), C.byref(rd), int(cam_samples), int(light_samples),
+                                               _p(pool), pool.shape[0], _p(out))
+        if rc != 0:
+            raise ValueError(f"orc_render_hybrid_direct failed ({rc})")
         return out
 
     def generate_arealight_sample(self, w, h, shadow_offset, rnd, hits, ray_dir, serial=False):

@@ -46,3 +46,22 @@ def test_headless_gpu_area_lights(gpu_ctx, tmp_path):
     ref = scene.render_direct(sc.camera, rd, 6)
     scene.close()
     assert np.array_equal(img, ref[::-1, ::-1])
+
+
+def test_headless_hybrid_area_lights(gpu_ctx, tmp_path):
+    """--algo hybrid_area_lights: -s camera samples, --light-samples per
+    camera sample, the CPU sampler's shadow offset from --offsets."""
+    exe = build.build_headless()
+    sc = scenes.cornell(width=40, height=32)
+    scenes.write_scene_bin(sc, tmp_path / "s.bin")
+    out = tmp_path / "h.pfm"
+    cmd = [str(exe), str(tmp_path / "s.bin"), str(out), "-r", "40x32", "--algo", "hybrid_area_lights", "-s", "2",
+           "--light-samples", "3", "--offsets", "0.0003", "0.0009"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    img = scenes.read_pfm(out)
+    scene = gpu_ctx.scene(sc)
+    rd = dict(sc.render, width=40, height=32, seed=0, shadow_offset=0.0009, background=(1.0, 1.0, 1.0))
+    ref = scene.render_hybrid_direct(sc.camera, rd, 2, 3)
+    scene.close()
+    assert np.array_equal(img, ref[::-1, ::-1])
