@@ -29,6 +29,10 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+# DRAM bytes (read + write) k_extend moves per closest-hit ray on the 1M-triangle
+# workload, from an ncu capture of a whole 4-spp frame with a warm L2
+# (profiles/k_extend_dram_traffic_icospheres1m_4spp.txt).
+K_EXTEND_DRAM_BYTES_PER_RAY = 851.7
 METRIC = "Mpaths/s"
 
 
@@ -580,7 +584,11 @@ def run_gbpt(args, rank, world):
             "stage_launches_per_frame": [int(x) for x in stage_n],
             "roofline": {"bound": "hbm", "kernel": "k_extend (closest-hit traversal + light sample)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / peak) if achieved else None,
+                         "traffic": (K_EXTEND_DRAM_BYTES_PER_RAY * ext_rays / max(1.0, ext_launches)
+                                     if args.workload == "icospheres-1m" else None),
+                         "traffic_source": "ncu dram__bytes_read+write of k_extend per closest-hit ray "
+                                           "(warm L2, whole 4-spp frame of this workload) x rays per launch",
                          "algorithmic_bytes_per_launch": closest_bytes / max(1.0, ext_launches),
                          "bytes_model": "node visits*80 + tri tests*36 + 48 per ray (counted by the instrumented "
                                         "traversal of the same frame)"},
