@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--graph", type=int, default=0, help="1 = host-driven slot-pool loop, 2 = CUDA graph per chunk")
     ap.add_argument("--builder", default="host", choices=["host", "device"],
                     help="BVH builder of the main scene: binned SAH on the host or PLOC on the GPU")
+    ap.add_argument("--wide-collapse", type=int, default=0,
+                    help="host tree: 0 = greedy 8-wide grouping, 1 = SAH-optimal grouping")
+    ap.add_argument("--prim-cost", type=float, default=0.0, help="triangle test cost of --wide-collapse 1")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the mixed batch leg (0 = skip it)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the path-replay adjoint leg")
     ap.add_argument("--rmse-spp", type=int, default=1024, help="spp of the converged reference image (0 = skip)")
@@ -487,7 +490,7 @@ def run_gbpt(args, rank, world):
     if args.refill or args.slots or args.tri_mode or args.graph:
         ctx.set_tuning(refill=args.refill, slots=args.slots, tri_mode=args.tri_mode, graph=args.graph)
     t0 = time.perf_counter()
-    scene = ctx.scene(sc, builder=args.builder)
+    scene = ctx.scene(sc, builder=args.builder, wide_collapse=args.wide_collapse, prim_cost=args.prim_cost)
     upload_s = time.perf_counter() - t0
     info = scene.info()
     out = torch.empty((H, W, 3), device="cuda", dtype=torch.float32)
@@ -568,7 +571,7 @@ def run_gbpt(args, rank, world):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config_of(sc, {"parallelism": f"replicas x{world}", "bvh_build_ms": info["build_ms"],
-                                     "bvh_builder": args.builder,
+                                     "bvh_builder": args.builder, "wide_collapse": args.wide_collapse,
                                      "scene_upload_s": upload_s, "bvh_nodes": info["num_nodes"],
                                      "bvh_depth": info["depth"], "tuning": ctx.get_tuning()}),
             "mrays_per_s": mrays,

@@ -434,7 +434,14 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
     }
     CwBvh bvh;
     std::string err;
-    if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err))
+    WideCollapse wide;
+    if (opts) {
+        if (opts->wide_collapse < 0 || opts->wide_collapse > 1 || !(opts->prim_cost >= 0.0f))
+            return fail(ctx, GB_ERR_INVALID, "wide_collapse must be 0 or 1 and prim_cost >= 0");
+        wide.sah = opts->wide_collapse == 1;
+        wide.prim_cost = opts->prim_cost;
+    }
+    if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err, &wide))
         return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);
 
     std::vector<float> shade;

@@ -2,7 +2,9 @@
 #include "gbpt_bvh.h"
 
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <memory>
 #include <cmath>
 #include <cstring>
 
@@ -115,14 +117,95 @@ void pad_box(Box& b) {
 
 inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 
+// SAH-optimal grouping of a binary tree into 8-wide nodes (Ylitie, Karras &
+// Laine 2017, section 4.1): cost[n][i] is the least SAH cost of the subtree
+// of binary node n as at most i slots of its wide parent; one slot is a leaf
+// (at most kLeafTris triangles, cost A * p * prim_cost) or a wide node (cost
+// A * node_cost + the best split of 8 slots between the two children).
+struct WideDp {
+    static const int kLeafTris = 3;
+    const std::vector<BNode>& bn;
+    double node_cost, prim_cost;
+    std::vector<int> prims;                 // triangles under each binary node
+    std::vector<std::array<double, 9>> cost;
+    std::vector<std::array<int8_t, 9>> how;  // i: 0 fewer slots, k > 0 left gets k; i = 1: 1 leaf, 2 wide node
+    std::vector<int8_t> split8;              // best split of 8 slots (wide node)
+    WideDp(const std::vector<BNode>& bn_, double nc, double pc) : bn(bn_), node_cost(nc), prim_cost(pc) {
+        const int n = (int)bn.size();
+        prims.assign(n, 0);
+        cost.assign(n, {});
+        how.assign(n, {});
+        split8.assign(n, 0);
+        // children come after their parent in `bn`: a reverse sweep is post-order
+        for (int v = n - 1; v >= 0; --v) {
+            const BNode& b = bn[v];
+            const double A = b.box.area();
+            if (b.count > 0) {
+                prims[v] = b.count;
+                for (int i = 1; i <= 8; ++i) { cost[v][i] = A * b.count * prim_cost; how[v][i] = i == 1 ? 1 : 0; }
+                continue;
+            }
+            const int l = b.left, r = b.right;
+            prims[v] = prims[l] + prims[r];
+            double dist[9];
+            int8_t dk[9];
+            for (int j = 2; j <= 8; ++j) {
+                dist[j] = 1e300;
+                dk[j] = 1;
+                for (int k = 1; k < j; ++k) {
+                    double c = cost[l][k] + cost[r][j - k];
+                    if (c < dist[j]) { dist[j] = c; dk[j] = (int8_t)k; }
+                }
+            }
+            split8[v] = dk[8];
+            const double wide = A * node_cost + dist[8];
+            const double leaf = prims[v] <= kLeafTris ? A * prims[v] * prim_cost : 1e300;
+            cost[v][1] = leaf <= wide ? leaf : wide;
+            how[v][1] = leaf <= wide ? 1 : 2;
+            for (int i = 2; i <= 8; ++i) {
+                if (dist[i] < cost[v][i - 1]) { cost[v][i] = dist[i]; how[v][i] = dk[i]; }
+                else { cost[v][i] = cost[v][i - 1]; how[v][i] = 0; }
+            }
+        }
+    }
+    // Slots of the subtree of v given at most i of them: (binary node, leaf?).
+    void collect(int v, int i, std::vector<std::pair<int, bool>>* out) const {
+        while (i > 1 && how[v][i] == 0) --i;
+        if (i == 1 || bn[v].count > 0) {
+            out->push_back(std::make_pair(v, bn[v].count > 0 || how[v][1] == 1));
+            return;
+        }
+        const int k = how[v][i];
+        collect(bn[v].left, k, out);
+        collect(bn[v].right, i - k, out);
+    }
+    // Children of the wide node made from binary node v.
+    void children(int v, std::vector<std::pair<int, bool>>* out) const {
+        if (bn[v].count > 0) { out->push_back(std::make_pair(v, true)); return; }
+        collect(bn[v].left, split8[v], out);
+        collect(bn[v].right, 8 - split8[v], out);
+    }
+};
+
 struct Collapser {
     const std::vector<BNode>& bn;
     const std::vector<int>& order;
     const float* pos;
     CwBvh& out;
     int max_depth = 0;
+    const WideDp* dp = nullptr;  // SAH-optimal grouping; greedy largest-area expansion without it
     Collapser(const std::vector<BNode>& bn_, const std::vector<int>& order_, const float* pos_, CwBvh& out_)
         : bn(bn_), order(order_), pos(pos_), out(out_) {}
+
+    // Triangles under binary node v, left to right.
+    void subtree_tris(int v, std::vector<int>* t) const {
+        if (bn[v].count > 0) {
+            for (int j = 0; j < bn[v].count; ++j) t->push_back(order[bn[v].first + j]);
+            return;
+        }
+        subtree_tris(bn[v].left, t);
+        subtree_tris(bn[v].right, t);
+    }
 
     void emit_tri(int t) {
         const float* a = pos + 9 * t;
@@ -141,16 +224,24 @@ struct Collapser {
     void fill(int ci, int b, int depth) {
         max_depth = std::max(max_depth, depth);
         std::vector<int> ch;
-        if (bn[b].count > 0) ch.push_back(b);
-        else { ch.push_back(bn[b].left); ch.push_back(bn[b].right); }
-        while ((int)ch.size() < 8) {
-            int best = -1; float ba = -1.0f;
-            for (int i = 0; i < (int)ch.size(); ++i)
-                if (bn[ch[i]].count == 0 && bn[ch[i]].box.area() > ba) { ba = bn[ch[i]].box.area(); best = i; }
-            if (best < 0) break;
-            int x = ch[best];
-            ch[best] = bn[x].left;
-            ch.push_back(bn[x].right);
+        std::vector<bool> is_leaf;
+        if (dp) {
+            std::vector<std::pair<int, bool>> slots;
+            dp->children(b, &slots);
+            for (const auto& s : slots) { ch.push_back(s.first); is_leaf.push_back(s.second); }
+        } else {
+            if (bn[b].count > 0) ch.push_back(b);
+            else { ch.push_back(bn[b].left); ch.push_back(bn[b].right); }
+            while ((int)ch.size() < 8) {
+                int best = -1; float ba = -1.0f;
+                for (int i = 0; i < (int)ch.size(); ++i)
+                    if (bn[ch[i]].count == 0 && bn[ch[i]].box.area() > ba) { ba = bn[ch[i]].box.area(); best = i; }
+                if (best < 0) break;
+                int x = ch[best];
+                ch[best] = bn[x].left;
+                ch.push_back(bn[x].right);
+            }
+            for (int c : ch) is_leaf.push_back(bn[c].count > 0);
         }
         int nc = (int)ch.size();
         // padded child boxes and their union
@@ -199,7 +290,7 @@ struct Collapser {
         w[0] = fbits(nb.lo[0]); w[1] = fbits(nb.lo[1]); w[2] = fbits(nb.lo[2]);
         uint32_t imask = 0;
         for (int s = 0; s < 8; ++s)
-            if (child_at[s] >= 0 && bn[ch[child_at[s]]].count == 0) imask |= 1u << s;
+            if (child_at[s] >= 0 && !is_leaf[child_at[s]]) imask |= 1u << s;
         w[3] = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) | (imask << 24);
         uint8_t meta[8] = {0};
         uint8_t q[6][8] = {{0}};
@@ -226,14 +317,16 @@ struct Collapser {
                 while (qh < 255 && nb.lo[a] + (float)qh * sc[a] < cbx[i].hi[a]) ++qh;
                 q[a][s] = (uint8_t)ql; q[3 + a][s] = (uint8_t)qh;
             }
-            if (bn[c].count == 0) {
+            if (!is_leaf[i]) {
                 meta[s] = 0x20;
                 todo.push_back(std::make_pair(base_child + k_inner, c));
                 ++k_inner;
             } else {
-                int cnt = bn[c].count;
+                std::vector<int> tl;
+                subtree_tris(c, &tl);
+                int cnt = (int)tl.size();
                 meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | (uint32_t)tri_off);
-                for (int j = 0; j < cnt; ++j) emit_tri(order[bn[c].first + j]);
+                for (int t : tl) emit_tri(t);
                 tri_off += cnt;
             }
         }
@@ -251,7 +344,7 @@ struct Collapser {
 
 }  // namespace
 
-bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err) {
+bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err, const WideCollapse* wide) {
     auto t0 = std::chrono::steady_clock::now();
     *out = CwBvh();
     if (n <= 0) { *err = "empty triangle list"; return false; }
@@ -276,6 +369,11 @@ bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err) {
     out->nodes.assign(kNodeWords, 0);
     out->tris.reserve((size_t)n * kTriWords);
     Collapser C(bn, order, pos, *out);
+    std::unique_ptr<WideDp> dp;
+    if (wide && wide->sah) {
+        dp.reset(new WideDp(bn, 1.0, wide->prim_cost > 0.0 ? wide->prim_cost : 0.3));
+        C.dp = dp.get();
+    }
     C.fill(0, 0, 1);
     out->n_tris = (int)(out->tris.size() / kTriWords);
     out->depth = C.max_depth;

@@ -35,9 +35,18 @@ struct CwBvh {
     double build_ms = 0.0;
 };
 
+// How binary nodes are grouped into 8-wide nodes: greedily (the child of
+// largest area is opened until 8) or by the SAH-optimal dynamic programme
+// over slot counts, with a node visit costing 1 and a triangle test
+// prim_cost (0 = 0.3).
+struct WideCollapse {
+    bool sah = false;
+    double prim_cost = 0.0;
+};
+
 // pos: 9 floats per triangle (a, b, c) in canonical order.  Returns false
 // and fills err on failure (too deep, degenerate extents).
-bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err);
+bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err, const WideCollapse* wide = nullptr);
 
 // Consistency check of a built tree (child / triangle ranges in bounds,
 // every triangle referenced once).  Used before any upload.

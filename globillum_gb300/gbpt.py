@@ -64,7 +64,7 @@ BUILDERS = {"host": GB_BVH_HOST_SAH, "device": GB_BVH_DEVICE_PLOC}
 
 
 class BuildOptions(C.Structure):
-    _fields_ = [("builder", C.c_int), ("ploc_radius", C.c_int)]
+    _fields_ = [("builder", C.c_int), ("ploc_radius", C.c_int), ("wide_collapse", C.c_int), ("prim_cost", C.c_float)]
 
 
 class Camera(C.Structure):
@@ -288,8 +288,10 @@ class Context:
     def set_stream(self, stream: int | None):
         self.check(self.lib.gb_ctx_set_stream(self.h, stream))
 
-    def scene(self, scene_data, builder: str = "host", ploc_radius: int = 0) -> "Scene":
-        return Scene(self, scene_data, builder=builder, ploc_radius=ploc_radius)
+    def scene(self, scene_data, builder: str = "host", ploc_radius: int = 0, wide_collapse: int = 0,
+              prim_cost: float = 0.0) -> "Scene":
+        return Scene(self, scene_data, builder=builder, ploc_radius=ploc_radius, wide_collapse=wide_collapse,
+                     prim_cost=prim_cost)
 
     def stats(self) -> dict:
         s = Stats()
@@ -371,15 +373,16 @@ class Context:
 class Scene:
     """A resident gb_scene."""
 
-    def __init__(self, ctx: Context, scene_data, builder: str = "host", ploc_radius: int = 0):
+    def __init__(self, ctx: Context, scene_data, builder: str = "host", ploc_radius: int = 0,
+                 wide_collapse: int = 0, prim_cost: float = 0.0):
         """builder: "host" (binned SAH on the CPU) or "device" (PLOC on the
-        GPU; refittable)."""
+        GPU; refittable); wide_collapse 1: SAH-optimal 8-wide grouping (host)."""
         self.ctx = ctx
         self.h = C.c_void_p()
         desc, self._keep = make_scene_desc(scene_data)
         if builder not in BUILDERS:
             raise ValueError(f"builder must be one of {sorted(BUILDERS)}")
-        opts = BuildOptions(BUILDERS[builder], int(ploc_radius))
+        opts = BuildOptions(BUILDERS[builder], int(ploc_radius), int(wide_collapse), float(prim_cost))
         ctx.check(ctx.lib.gb_scene_create_ex(ctx.h, C.byref(desc), C.byref(opts), C.byref(self.h)))
 
     def refit(self, positions: np.ndarray, normals: np.ndarray | None = None) -> None:

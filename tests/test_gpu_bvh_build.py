@@ -152,3 +152,23 @@ def test_device_tree_traversal_cost(gpu_ctx):
         cost[b] = (st["closest_node_visits"] + st["closest_tri_tests"]) / rays
         s.close()
     assert cost["device"] <= 1.3 * cost["host"], cost
+
+
+@pytest.mark.parametrize("prim_cost", [0.0, 1.0])
+def test_sah_wide_collapse_hits_and_frame(gpu_ctx, prim_cost):
+    """The SAH-optimal 8-wide grouping of the host tree (wide_collapse 1)
+    gives the oracle's hits and frame, with fewer nodes than the greedy one."""
+    sc = scenes.icospheres(n_spheres=12, level=2, box=10.0, width=48, height=32, spp=3, max_bounces=4, n_lights=2)
+    s = gpu_ctx.scene(sc, wide_collapse=1, prim_cost=prim_cost)
+    g = gpu_ctx.scene(sc)
+    assert s.info()["num_nodes"] < g.info()["num_nodes"]
+    orc = _oracle(sc)
+    o, d = scenes.random_rays(sc, 50000, seed=9)
+    tmax = np.full(o.shape[0], 3.4e38, np.float32)
+    _same_hits(s.trace_closest(o, d, tmax), orc.trace_closest(o, d, tmax))
+    img, ref = _frame_and_ref(gpu_ctx, sc, dict(sc.render), s)
+    assert np.array_equal(img, ref.astype(np.float32))
+    s.close()
+    g.close()
+    with pytest.raises(gbpt.GBError, match="wide_collapse"):
+        gpu_ctx.scene(sc, wide_collapse=2)
