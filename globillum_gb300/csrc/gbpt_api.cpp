@@ -434,12 +434,14 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
     }
     CwBvh bvh;
     std::string err;
-    WideCollapse wide;
+    WideCollapse wide;  // default: SAH-optimal grouping, triangle test 1.2 node visits
+    wide.sah = true;
+    wide.prim_cost = 1.2;
     if (opts) {
-        if (opts->wide_collapse < 0 || opts->wide_collapse > 1 || !(opts->prim_cost >= 0.0f))
-            return fail(ctx, GB_ERR_INVALID, "wide_collapse must be 0 or 1 and prim_cost >= 0");
-        wide.sah = opts->wide_collapse == 1;
-        wide.prim_cost = opts->prim_cost;
+        if (opts->wide_collapse < 0 || opts->wide_collapse > 2 || !(opts->prim_cost >= 0.0f))
+            return fail(ctx, GB_ERR_INVALID, "wide_collapse must be 0, 1 or 2 and prim_cost >= 0");
+        if (opts->wide_collapse == 2) wide.sah = false;
+        if (opts->prim_cost > 0.0f) wide.prim_cost = opts->prim_cost;
     }
     if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err, &wide))
         return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);
@@ -488,7 +490,8 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
         float* dpos = nullptr;
         e = SA.alloc((void**)&dpos, sizeof(float) * 9 * (size_t)n, false);
         if (e == cudaSuccess) e = cudaMemcpy(dpos, d->positions, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = gpu_build_cwbvh(dpos, n, radius, SA, &sc->gbvh, &err, ctx->stream);
+        if (e == cudaSuccess)
+            e = gpu_build_cwbvh(dpos, n, radius, SA, &sc->gbvh, &err, ctx->stream, wide.sah, (float)wide.prim_cost);
         if (e != cudaSuccess) {
             SA.release_temps();
             free_all(sc->allocs);

@@ -232,9 +232,45 @@ __global__ void k_ploc_compact(const int* __restrict__ nn, int n, int inner_base
 // at most kLeafMax triangles is stored as one leaf when count <= 0.5 +
 // (A_l c_l + A_r c_r) / A).  Refit mode: boxes from the moved vertices.
 // bad = 2 if a parent chain is longer than the tree.
+// SAH-optimal 8-wide grouping (WideDp of gbpt_bvh.cpp), when dcost is
+// given: dcost[8v + i-1] = least cost of v's subtree as at most i slots of
+// its wide parent, dhow[8v + i-1] = 0 (fewer slots) or the slots the left
+// child gets (i = 1: 1 leaf, 2 wide node), dsplit[v] = the left child's share
+// of the 8 slots of a wide node at v.  The leaf flag is then dhow[8v] == 1.
+__device__ void wide_dp_node(int v, int l, int r, int cnt, float area, float prim_cost, float* dcost,
+                             int8_t* dhow, int8_t* dsplit, uint8_t* bleaf) {
+    float cl[8], cr[8];
+    for (int k = 0; k < 8; ++k) {
+        cl[k] = __ldcg(&dcost[8 * (size_t)l + k]);
+        cr[k] = __ldcg(&dcost[8 * (size_t)r + k]);
+    }
+    float dist[9];
+    int8_t dk[9];
+    for (int j = 2; j <= 8; ++j) {
+        dist[j] = 3.0e38f;
+        dk[j] = 1;
+        for (int k = 1; k < j; ++k) {
+            const float c = cl[k - 1] + cr[j - k - 1];
+            if (c < dist[j]) { dist[j] = c; dk[j] = (int8_t)k; }
+        }
+    }
+    dsplit[v] = dk[8];
+    const float wide = area + dist[8];
+    const float leaf = cnt <= kLeafMax ? area * (float)cnt * prim_cost : 3.0e38f;
+    float prev = leaf <= wide ? leaf : wide;
+    dcost[8 * (size_t)v] = prev;
+    dhow[8 * (size_t)v] = leaf <= wide ? 1 : 2;
+    bleaf[v] = leaf <= wide ? 1 : 0;
+    for (int i = 2; i <= 8; ++i) {
+        if (dist[i] < prev) { prev = dist[i]; dhow[8 * (size_t)v + i - 1] = dk[i]; }
+        else dhow[8 * (size_t)v + i - 1] = 0;
+        dcost[8 * (size_t)v + i - 1] = prev;
+    }
+}
+
 __global__ void k_bottom_up(int n, const int* __restrict__ bparent, const int2* __restrict__ bchild, float4* blo,
                             float4* bhi, int* bcount, uint8_t* bleaf, unsigned* visit, const float* __restrict__ pos,
-                            int refit, int* bad) {
+                            int refit, int* bad, float* dcost, int8_t* dhow, int8_t* dsplit, float prim_cost) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (refit) {
@@ -245,6 +281,13 @@ __global__ void k_bottom_up(int n, const int* __restrict__ bparent, const int2* 
     } else {
         bcount[i] = 1;
         bleaf[i] = 1;
+        if (dcost) {
+            const float c = box_area(blo[i], bhi[i]) * prim_cost;
+            for (int k = 0; k < 8; ++k) {
+                dcost[8 * (size_t)i + k] = c;
+                dhow[8 * (size_t)i + k] = k == 0 ? 1 : 0;
+            }
+        }
     }
     int node = bparent[i];
     for (int guard = 0; node >= 0; ++guard) {
@@ -269,6 +312,8 @@ __global__ void k_bottom_up(int n, const int* __restrict__ bparent, const int2* 
             float best = box_area(llo, lhi) * (float)cl + box_area(rlo, rhi) * (float)cr;
             float split = 0.5f + (pa > 0.0f ? best / pa : 0.0f);
             bleaf[node] = (cnt <= kLeafMax && (float)cnt <= split) ? 1 : 0;
+            if (dcost) wide_dp_node(node, c.x, c.y, cnt, pa, prim_cost, dcost, dhow, dsplit, bleaf);
+            __threadfence();
         }
         node = bparent[node];
     }
@@ -295,7 +340,8 @@ __device__ __forceinline__ void pad_box_d(float4* lo, float4* hi) {
 __global__ void k_collapse_plan(const int* __restrict__ q, int m, int node_base, const float4* __restrict__ blo,
                                 const float4* __restrict__ bhi, const int2* __restrict__ bchild,
                                 const uint8_t* __restrict__ bleaf, const int* __restrict__ bcount, int* plan,
-                                unsigned long long* flags) {
+                                unsigned long long* flags, const int8_t* __restrict__ dhow,
+                                const int8_t* __restrict__ dsplit, int n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     int b = q[k];
@@ -304,13 +350,31 @@ __global__ void k_collapse_plan(const int* __restrict__ q, int m, int node_base,
     if (bleaf[b]) {
         ch[0] = b;
         nc = 1;
+    } else if (dhow) {
+        // the slots of the SAH-optimal grouping, left to right
+        int sv[8], si[8], sp = 0;
+        const int2 c = bchild[b];
+        sv[sp] = c.y; si[sp] = 8 - dsplit[b]; ++sp;
+        sv[sp] = c.x; si[sp] = dsplit[b]; ++sp;
+        nc = 0;
+        while (sp > 0 && nc < 8) {
+            const int v = sv[--sp];
+            int i = si[sp];
+            while (i > 1 && dhow[8 * (size_t)v + i - 1] == 0) --i;
+            if (i <= 1 || v < n) { ch[nc++] = v; continue; }
+            const int kk = dhow[8 * (size_t)v + i - 1];
+            const int2 cc = bchild[v];
+            if (sp + 2 > 8) { ch[nc++] = v; continue; }  // never taken: slot counts only shrink
+            sv[sp] = cc.y; si[sp] = i - kk; ++sp;
+            sv[sp] = cc.x; si[sp] = kk; ++sp;
+        }
     } else {
         int2 c = bchild[b];
         ch[0] = c.x;
         ch[1] = c.y;
         nc = 2;
     }
-    while (nc < 8) {
+    while (!dhow && nc < 8) {
         int best = -1;
         float ba = -1.0f;
         for (int i = 0; i < nc; ++i)
@@ -524,7 +588,7 @@ struct TempGuard {
     } while (0)
 
 cudaError_t gpu_build_cwbvh(const float* d_pos, int n, int radius, DevAllocator& A, GpuBvh* out,
-                            std::string* err, cudaStream_t st) {
+                            std::string* err, cudaStream_t st, bool sah_collapse, float prim_cost) {
     TempGuard guard(A);
     *out = GpuBvh();
     if (n <= 0) { *err = "empty triangle list"; return cudaErrorInvalidValue; }
@@ -619,8 +683,15 @@ cudaError_t gpu_build_cwbvh(const float* d_pos, int n, int radius, DevAllocator&
     B.binary_nodes = (int)N2;
 
     GB_TRY(cudaMemsetAsync(visit, 0, sizeof(unsigned) * N2, st));
+    float* dcost = nullptr;
+    int8_t *dhow = nullptr, *dsplit = nullptr;
+    if (sah_collapse) {
+        GB_TRY(A.alloc((void**)&dcost, sizeof(float) * 8 * N2, false));
+        GB_TRY(A.alloc((void**)&dhow, 8 * N2, false));
+        GB_TRY(A.alloc((void**)&dsplit, N2, false));
+    }
     k_bottom_up<<<blocks_of(n, T), T, 0, st>>>(n, B.bparent, B.bchild, B.blo, B.bhi, bcount, B.bleaf, visit, d_pos, 0,
-                                               bad);
+                                               bad, dcost, dhow, dsplit, prim_cost);
     GB_TRY(cudaGetLastError());
 
     // collapse, one level of 8-wide nodes per pass
@@ -632,7 +703,7 @@ cudaError_t gpu_build_cwbvh(const float* d_pos, int n, int radius, DevAllocator&
         int next_base = node_base + m;
         if (next_base > cap) { *err = "8-wide node count out of range"; return cudaErrorInvalidValue; }
         k_collapse_plan<<<blocks_of(m, T), T, 0, st>>>(q[cur], m, node_base, B.blo, B.bhi, B.bchild, B.bleaf, bcount,
-                                                      plan_tmp, flags);
+                                                      plan_tmp, flags, dhow, dsplit, n);
         GB_TRY(cudaGetLastError());
         GB_TRY(cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, flags, offs, m, st));
         k_collapse_emit<<<blocks_of(m, T), T, 0, st>>>(plan_tmp, m, node_base, next_base, tri_base, offs, flags, B.blo,
@@ -698,7 +769,7 @@ cudaError_t gpu_refit_cwbvh(const float* d_pos, DevAllocator& A, GpuBvh* bvh, st
     if (h_bad) { *err = "non-finite vertex"; return cudaErrorInvalidValue; }
     GB_TRY(cudaMemsetAsync(visit, 0, sizeof(unsigned) * N2, st));
     k_bottom_up<<<blocks_of(n, T), T, 0, st>>>(n, B.bparent, B.bchild, B.blo, B.bhi, nullptr, nullptr, visit, d_pos, 1,
-                                               bad);
+                                               bad, nullptr, nullptr, nullptr, 0.0f);
     GB_TRY(cudaGetLastError());
     k_collapse_emit<<<blocks_of(B.n_nodes, T), T, 0, st>>>(B.plan, B.n_nodes, 0, 0, 0, nullptr, nullptr, B.blo, B.bhi,
                                                           B.bchild, B.bleaf, n, d_pos, (uint4*)B.nodes, B.tris,

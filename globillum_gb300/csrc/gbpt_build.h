@@ -52,11 +52,14 @@ struct GpuBvh {
 
 // Builds the tree of the n triangles at d_pos (9 floats each, device
 // memory) on stream st.  radius: clustering search radius (1 .. 32).
+// sah_collapse: group binary nodes into 8-wide nodes by the SAH-optimal
+// dynamic programme (node visit 1, triangle test prim_cost) instead of the
+// host collapser's greedy rules.
 // Returns cudaErrorInvalidValue with *err set for bad input (non-finite
 // vertex, tree deeper than the traversal stack), any other error for CUDA
 // failures.  The stream is synchronised on return.
 cudaError_t gpu_build_cwbvh(const float* d_pos, int n, int radius, DevAllocator& A, GpuBvh* out,
-                            std::string* err, cudaStream_t st);
+                            std::string* err, cudaStream_t st, bool sah_collapse = false, float prim_cost = 1.2f);
 
 // Recomputes the boxes of a built tree for moved vertices (same triangle
 // count and order) and rewrites nodes and triangle records in place.

@@ -371,7 +371,7 @@ bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err, const Wi
     Collapser C(bn, order, pos, *out);
     std::unique_ptr<WideDp> dp;
     if (wide && wide->sah) {
-        dp.reset(new WideDp(bn, 1.0, wide->prim_cost > 0.0 ? wide->prim_cost : 0.3));
+        dp.reset(new WideDp(bn, 1.0, wide->prim_cost > 0.0 ? wide->prim_cost : 1.2));
         C.dp = dp.get();
     }
     C.fill(0, 0, 1);

@@ -38,7 +38,7 @@ struct CwBvh {
 // How binary nodes are grouped into 8-wide nodes: greedily (the child of
 // largest area is opened until 8) or by the SAH-optimal dynamic programme
 // over slot counts, with a node visit costing 1 and a triangle test
-// prim_cost (0 = 0.3).
+// prim_cost (0 = 1.2).
 struct WideCollapse {
     bool sah = false;
     double prim_cost = 0.0;

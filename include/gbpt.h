@@ -145,11 +145,12 @@ enum { GB_BVH_HOST_SAH = 0, GB_BVH_DEVICE_PLOC = 1 };
 typedef struct {
     int builder;                  /* GB_BVH_*                                 */
     int ploc_radius;              /* clustering search radius, 1 .. 32; 0 = 16 */
-    int wide_collapse;            /* GB_BVH_HOST_SAH: 0 = open the largest child until 8
-                                     (default), 1 = SAH-optimal grouping by dynamic
-                                     programming over slot counts (Ylitie et al. 2017) */
-    float prim_cost;              /* triangle test cost against a node visit for
-                                     wide_collapse 1; 0 = 0.3 */
+    int wide_collapse;            /* grouping of binary nodes into 8-wide nodes (both
+                                     builders): 0 / 1 = SAH-optimal grouping by dynamic
+                                     programming over slot counts (Ylitie et al. 2017; the
+                                     default), 2 = open the largest child until 8 */
+    float prim_cost;              /* triangle test cost against a node visit for the
+                                     SAH-optimal grouping; 0 = 1.2 */
 } gb_build_options;
 
 /* Uploads triangles, materials and lights and builds the BVH (replaces

@@ -154,13 +154,14 @@ def test_device_tree_traversal_cost(gpu_ctx):
     assert cost["device"] <= 1.3 * cost["host"], cost
 
 
-@pytest.mark.parametrize("prim_cost", [0.0, 1.0])
-def test_sah_wide_collapse_hits_and_frame(gpu_ctx, prim_cost):
-    """The SAH-optimal 8-wide grouping of the host tree (wide_collapse 1)
-    gives the oracle's hits and frame, with fewer nodes than the greedy one."""
+@pytest.mark.parametrize("builder,prim_cost", [("host", 0.0), ("host", 1.0), ("device", 0.0), ("device", 2.0)])
+def test_sah_wide_collapse_hits_and_frame(gpu_ctx, builder, prim_cost):
+    """The SAH-optimal 8-wide grouping (wide_collapse 1, the default) of
+    either builder's tree gives the oracle's hits and frame, with fewer nodes
+    than the greedy grouping (wide_collapse 2) of the same builder."""
     sc = scenes.icospheres(n_spheres=12, level=2, box=10.0, width=48, height=32, spp=3, max_bounces=4, n_lights=2)
-    s = gpu_ctx.scene(sc, wide_collapse=1, prim_cost=prim_cost)
-    g = gpu_ctx.scene(sc)
+    s = gpu_ctx.scene(sc, builder=builder, wide_collapse=1, prim_cost=prim_cost)
+    g = gpu_ctx.scene(sc, builder=builder, wide_collapse=2)
     assert s.info()["num_nodes"] < g.info()["num_nodes"]
     orc = _oracle(sc)
     o, d = scenes.random_rays(sc, 50000, seed=9)
@@ -171,4 +172,4 @@ def test_sah_wide_collapse_hits_and_frame(gpu_ctx, prim_cost):
     s.close()
     g.close()
     with pytest.raises(gbpt.GBError, match="wide_collapse"):
-        gpu_ctx.scene(sc, wide_collapse=2)
+        gpu_ctx.scene(sc, wide_collapse=3)
