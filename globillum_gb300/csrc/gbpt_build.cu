@@ -331,9 +331,10 @@ __device__ __forceinline__ void pad_box_d(float4* lo, float4* hi) {
     hi->x += d; hi->y += d; hi->z += d;
 }
 
-// Children of one 8-wide node (Collapser::fill of gbpt_bvh.cpp): start from
-// the binary node's two children and replace the stored-inner child of
-// largest area by its two children while fewer than 8; then give each child
+// Children of one 8-wide node (Collapser::fill of gbpt_bvh.cpp): the slots
+// of the SAH-optimal grouping (dhow / dsplit from k_bottom_up), or, without
+// it, the binary node's two children with the stored-inner child of largest
+// area replaced by its two children while fewer than 8; then give each child
 // the octant slot whose rays should visit it first (greedy on the centroid
 // offset along the octant's diagonal).  plan gets the child of each slot
 // (-1 = empty); flags = inner children << 32 | leaf triangles.

@@ -7,10 +7,11 @@
 // Clustering (Meister & Bittner, "Parallel Locally-Ordered Clustering for
 // Bounding Volume Hierarchy Construction", IEEE TVCG 2018), and the tree is
 // collapsed level by level into the compressed 8-wide nodes the traversal
-// kernels read.  The collapse applies the host builder's rules (leaf rule,
-// greedy expansion of the largest child, octant slot order, box padding and
-// 8-bit quantisation), so for a given binary tree it writes the nodes the
-// host collapse would write; only the node numbering differs (level order).
+// kernels read.  The collapse applies the host builder's rules (the
+// SAH-optimal grouping of binary nodes into wide nodes, or the greedy one;
+// octant slot order, box padding and 8-bit quantisation), so for a given
+// binary tree it writes the nodes the host collapse would write; only the
+// node numbering differs (level order).
 //
 // The binary tree and the 8-wide grouping are kept, so a scene whose
 // vertices move can be refitted: boxes are recomputed bottom-up and the
