@@ -442,6 +442,9 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
             return fail(ctx, GB_ERR_INVALID, "wide_collapse must be 0, 1 or 2 and prim_cost >= 0");
         if (opts->wide_collapse == 2) wide.sah = false;
         if (opts->prim_cost > 0.0f) wide.prim_cost = opts->prim_cost;
+        if (opts->sah_bins < 0 || opts->sah_bins == 1 || opts->sah_bins > 64)
+            return fail(ctx, GB_ERR_INVALID, "sah_bins must be 2 .. 64 (0 = 16)");
+        wide.bins = opts->sah_bins;
     }
     if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err, &wide))
         return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);

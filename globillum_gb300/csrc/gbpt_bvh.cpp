@@ -41,7 +41,8 @@ struct Builder {
     const std::vector<float>& cen;  // 3 per triangle
     std::vector<int>& order;
     std::vector<BNode> nodes;
-    static const int kBins = 16;
+    static const int kMaxBins = 64;
+    int nbins = 16;  // SAH bins per axis and node
     static const int kMaxLeaf = 3;
 
     Builder(const std::vector<Box>& tb_, const std::vector<float>& cen_, std::vector<int>& order_)
@@ -63,19 +64,19 @@ struct Builder {
         for (int a = 0; a < 3; ++a) {
             float ext = cb.hi[a] - cb.lo[a];
             if (!(ext > 0.0f)) continue;
-            Box bins[kBins]; int cnt[kBins];
-            for (int k = 0; k < kBins; ++k) { bins[k].empty(); cnt[k] = 0; }
-            float scale = (float)kBins * (1.0f - 1e-6f) / ext;
+            Box bins[kMaxBins]; int cnt[kMaxBins];
+            for (int k = 0; k < nbins; ++k) { bins[k].empty(); cnt[k] = 0; }
+            float scale = (float)nbins * (1.0f - 1e-6f) / ext;
             for (int i = b; i < e; ++i) {
                 int t = order[i];
-                int k = std::min(kBins - 1, (int)((cen[3 * t + a] - cb.lo[a]) * scale));
+                int k = std::min(nbins - 1, (int)((cen[3 * t + a] - cb.lo[a]) * scale));
                 bins[k].grow(tb[t]); cnt[k]++;
             }
-            float rarea[kBins]; int rcnt[kBins];
+            float rarea[kMaxBins]; int rcnt[kMaxBins];
             Box acc; acc.empty(); int c = 0;
-            for (int k = kBins - 1; k > 0; --k) { acc.grow(bins[k]); c += cnt[k]; rarea[k] = acc.area(); rcnt[k] = c; }
+            for (int k = nbins - 1; k > 0; --k) { acc.grow(bins[k]); c += cnt[k]; rarea[k] = acc.area(); rcnt[k] = c; }
             acc.empty(); c = 0;
-            for (int k = 0; k < kBins - 1; ++k) {
+            for (int k = 0; k < nbins - 1; ++k) {
                 acc.grow(bins[k]); c += cnt[k];
                 if (c == 0 || rcnt[k + 1] == 0) continue;
                 float cost = acc.area() * c + rarea[k + 1] * rcnt[k + 1];
@@ -93,9 +94,9 @@ struct Builder {
             mid = b + count / 2;  // all centroids coincide: split the range
         } else {
             float ext = cb.hi[best_axis] - cb.lo[best_axis];
-            float scale = (float)kBins * (1.0f - 1e-6f) / ext;
+            float scale = (float)nbins * (1.0f - 1e-6f) / ext;
             int* p = std::partition(order.data() + b, order.data() + e, [&](int t) {
-                int k = std::min(kBins - 1, (int)((cen[3 * t + best_axis] - cb.lo[best_axis]) * scale));
+                int k = std::min(nbins - 1, (int)((cen[3 * t + best_axis] - cb.lo[best_axis]) * scale));
                 return k <= best_split;
             });
             mid = (int)(p - order.data());
@@ -361,6 +362,7 @@ bool build_cwbvh(const float* pos, int n, CwBvh* out, std::string* err, const Wi
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     Builder B(tb, cen, order);
+    if (wide && wide->bins > 0) B.nbins = std::min(wide->bins, (int)Builder::kMaxBins);
     std::vector<BNode> bn;
     bn.reserve(2 * (size_t)n);
     B.build(bn, 0, n);

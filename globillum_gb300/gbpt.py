@@ -64,7 +64,8 @@ BUILDERS = {"host": GB_BVH_HOST_SAH, "device": GB_BVH_DEVICE_PLOC}
 
 
 class BuildOptions(C.Structure):
-    _fields_ = [("builder", C.c_int), ("ploc_radius", C.c_int), ("wide_collapse", C.c_int), ("prim_cost", C.c_float)]
+    _fields_ = [("builder", C.c_int), ("ploc_radius", C.c_int), ("wide_collapse", C.c_int), ("prim_cost", C.c_float),
+                ("sah_bins", C.c_int)]
 
 
 class Camera(C.Structure):
@@ -289,9 +290,9 @@ class Context:
         self.check(self.lib.gb_ctx_set_stream(self.h, stream))
 
     def scene(self, scene_data, builder: str = "host", ploc_radius: int = 0, wide_collapse: int = 0,
-              prim_cost: float = 0.0) -> "Scene":
+              prim_cost: float = 0.0, sah_bins: int = 0) -> "Scene":
         return Scene(self, scene_data, builder=builder, ploc_radius=ploc_radius, wide_collapse=wide_collapse,
-                     prim_cost=prim_cost)
+                     prim_cost=prim_cost, sah_bins=sah_bins)
 
     def stats(self) -> dict:
         s = Stats()
@@ -374,7 +375,7 @@ class Scene:
     """A resident gb_scene."""
 
     def __init__(self, ctx: Context, scene_data, builder: str = "host", ploc_radius: int = 0,
-                 wide_collapse: int = 0, prim_cost: float = 0.0):
+                 wide_collapse: int = 0, prim_cost: float = 0.0, sah_bins: int = 0):
         """builder: "host" (binned SAH on the CPU) or "device" (PLOC on the
         GPU; refittable); wide_collapse 1: SAH-optimal 8-wide grouping (host)."""
         self.ctx = ctx
@@ -382,7 +383,7 @@ class Scene:
         desc, self._keep = make_scene_desc(scene_data)
         if builder not in BUILDERS:
             raise ValueError(f"builder must be one of {sorted(BUILDERS)}")
-        opts = BuildOptions(BUILDERS[builder], int(ploc_radius), int(wide_collapse), float(prim_cost))
+        opts = BuildOptions(BUILDERS[builder], int(ploc_radius), int(wide_collapse), float(prim_cost), int(sah_bins))
         ctx.check(ctx.lib.gb_scene_create_ex(ctx.h, C.byref(desc), C.byref(opts), C.byref(self.h)))
 
     def refit(self, positions: np.ndarray, normals: np.ndarray | None = None) -> None:

@@ -151,6 +151,8 @@ typedef struct {
                                      default), 2 = open the largest child until 8 */
     float prim_cost;              /* triangle test cost against a node visit for the
                                      SAH-optimal grouping; 0 = 1.2 */
+    int sah_bins;                 /* GB_BVH_HOST_SAH: bins per axis of the binned SAH,
+                                     2 .. 64; 0 = 16 */
 } gb_build_options;
 
 /* Uploads triangles, materials and lights and builds the BVH (replaces
