@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--wide-collapse", type=int, default=0,
                     help="8-wide grouping: 0 = library default (SAH-optimal), 1 = SAH-optimal, 2 = greedy")
     ap.add_argument("--prim-cost", type=float, default=0.0, help="triangle test cost of the SAH grouping (0 = default)")
-    ap.add_argument("--sah-bins", type=int, default=0, help="binned-SAH bins per axis of the host builder (0 = 16)")
+    ap.add_argument("--sah-bins", type=int, default=0, help="binned-SAH bins per axis of the host builder (0 = 32)")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the mixed batch leg (0 = skip it)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the path-replay adjoint leg")
     ap.add_argument("--rmse-spp", type=int, default=1024, help="spp of the converged reference image (0 = skip)")

@@ -443,7 +443,7 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
         if (opts->wide_collapse == 2) wide.sah = false;
         if (opts->prim_cost > 0.0f) wide.prim_cost = opts->prim_cost;
         if (opts->sah_bins < 0 || opts->sah_bins == 1 || opts->sah_bins > 64)
-            return fail(ctx, GB_ERR_INVALID, "sah_bins must be 2 .. 64 (0 = 16)");
+            return fail(ctx, GB_ERR_INVALID, "sah_bins must be 2 .. 64 (0 = 32)");
         wide.bins = opts->sah_bins;
     }
     if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err, &wide))

@@ -42,7 +42,7 @@ struct Builder {
     std::vector<int>& order;
     std::vector<BNode> nodes;
     static const int kMaxBins = 64;
-    int nbins = 16;  // SAH bins per axis and node
+    int nbins = 32;  // SAH bins per axis and node
     static const int kMaxLeaf = 3;
 
     Builder(const std::vector<Box>& tb_, const std::vector<float>& cen_, std::vector<int>& order_)

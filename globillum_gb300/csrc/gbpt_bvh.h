@@ -42,7 +42,7 @@ struct CwBvh {
 struct WideCollapse {
     bool sah = false;
     double prim_cost = 0.0;
-    int bins = 0;  // binned-SAH bins per axis of the binary build (0 = 16, at most 64)
+    int bins = 0;  // binned-SAH bins per axis of the binary build (0 = 32, at most 64)
 };
 
 // pos: 9 floats per triangle (a, b, c) in canonical order.  Returns false

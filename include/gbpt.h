@@ -152,7 +152,7 @@ typedef struct {
     float prim_cost;              /* triangle test cost against a node visit for the
                                      SAH-optimal grouping; 0 = 1.2 */
     int sah_bins;                 /* GB_BVH_HOST_SAH: bins per axis of the binned SAH,
-                                     2 .. 64; 0 = 16 */
+                                     2 .. 64; 0 = 32 */
 } gb_build_options;
 
 /* Uploads triangles, materials and lights and builds the BVH (replaces
