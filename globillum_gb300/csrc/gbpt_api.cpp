@@ -387,6 +387,43 @@ int gb_ctx_set_stream(gb_ctx* ctx, void* stream) {
     return GB_OK;
 }
 
+// 8-wide grouping and binned-SAH options of gb_build_options (defaults:
+// SAH-optimal grouping with a triangle test worth 1.2 node visits, 32 bins).
+static bool wide_options(const gb_build_options* opts, WideCollapse* wide, std::string* why) {
+    wide->sah = true;
+    wide->prim_cost = 1.2;
+    wide->bins = 0;
+    if (!opts) return true;
+    if (opts->wide_collapse < 0 || opts->wide_collapse > 2 || !(opts->prim_cost >= 0.0f)) {
+        *why = "wide_collapse must be 0, 1 or 2 and prim_cost >= 0";
+        return false;
+    }
+    if (opts->sah_bins < 0 || opts->sah_bins == 1 || opts->sah_bins > 64) {
+        *why = "sah_bins must be 2 .. 64 (0 = 32)";
+        return false;
+    }
+    if (opts->wide_collapse == 2) wide->sah = false;
+    if (opts->prim_cost > 0.0f) wide->prim_cost = opts->prim_cost;
+    wide->bins = opts->sah_bins;
+    return true;
+}
+
+int gb_bvh_build_stats(const float* positions, int n, const gb_build_options* opts, gb_bvh_stats* out) {
+    if (!positions || !out || n <= 0 || n > (1 << 28)) return GB_ERR_INVALID;
+    if (opts && opts->builder != GB_BVH_HOST_SAH) return GB_ERR_UNSUPPORTED;
+    WideCollapse wide;
+    std::string why;
+    if (!wide_options(opts, &wide, &why)) return GB_ERR_INVALID;
+    CwBvh bvh;
+    if (!build_cwbvh(positions, n, &bvh, &why, &wide)) return GB_ERR_INVALID;
+    out->num_nodes = bvh.n_nodes;
+    out->depth = bvh.depth;
+    out->binary_nodes = bvh.binary_nodes;
+    out->num_triangles = bvh.n_tris;
+    out->build_ms = bvh.build_ms;
+    return GB_OK;
+}
+
 int gb_scene_create(gb_ctx* ctx, const gb_scene_desc* d, gb_scene** out) {
     return gb_scene_create_ex(ctx, d, nullptr, out);
 }
@@ -434,17 +471,10 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
     }
     CwBvh bvh;
     std::string err;
-    WideCollapse wide;  // default: SAH-optimal grouping, triangle test 1.2 node visits
-    wide.sah = true;
-    wide.prim_cost = 1.2;
-    if (opts) {
-        if (opts->wide_collapse < 0 || opts->wide_collapse > 2 || !(opts->prim_cost >= 0.0f))
-            return fail(ctx, GB_ERR_INVALID, "wide_collapse must be 0, 1 or 2 and prim_cost >= 0");
-        if (opts->wide_collapse == 2) wide.sah = false;
-        if (opts->prim_cost > 0.0f) wide.prim_cost = opts->prim_cost;
-        if (opts->sah_bins < 0 || opts->sah_bins == 1 || opts->sah_bins > 64)
-            return fail(ctx, GB_ERR_INVALID, "sah_bins must be 2 .. 64 (0 = 32)");
-        wide.bins = opts->sah_bins;
+    WideCollapse wide;
+    {
+        std::string why;
+        if (!wide_options(opts, &wide, &why)) return fail(ctx, GB_ERR_INVALID, why);
     }
     if (builder == GB_BVH_HOST_SAH && !build_cwbvh(d->positions, n, &bvh, &err, &wide))
         return fail(ctx, GB_ERR_INVALID, "BVH build: " + err);

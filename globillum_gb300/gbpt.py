@@ -63,6 +63,24 @@ GB_BVH_HOST_SAH, GB_BVH_DEVICE_PLOC = 0, 1
 BUILDERS = {"host": GB_BVH_HOST_SAH, "device": GB_BVH_DEVICE_PLOC}
 
 
+class BvhStats(C.Structure):
+    _fields_ = [("num_nodes", C.c_int), ("depth", C.c_int), ("binary_nodes", C.c_int), ("num_triangles", C.c_int),
+                ("build_ms", C.c_double)]
+
+
+def bvh_build_stats(positions: np.ndarray, wide_collapse: int = 0, prim_cost: float = 0.0, sah_bins: int = 0) -> dict:
+    """gb_bvh_build_stats: the host-built tree of `positions` (n, 9), summarised
+    (no device needed)."""
+    lib = load_library()
+    pos = np.ascontiguousarray(positions, np.float32)
+    opts = BuildOptions(GB_BVH_HOST_SAH, 0, int(wide_collapse), float(prim_cost), int(sah_bins))
+    st = BvhStats()
+    rc = lib.gb_bvh_build_stats(_ptr(pos), int(pos.shape[0]), C.byref(opts), C.byref(st))
+    if rc != GB_OK:
+        raise GBError(rc, "gb_bvh_build_stats failed")
+    return {k: getattr(st, k) for k, _ in BvhStats._fields_}
+
+
 class BuildOptions(C.Structure):
     _fields_ = [("builder", C.c_int), ("ploc_radius", C.c_int), ("wide_collapse", C.c_int), ("prim_cost", C.c_float),
                 ("sah_bins", C.c_int)]
@@ -118,6 +136,7 @@ EXPORTS = [
     "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
     "gb_asset_add_obj", "gb_asset_add_lights", "gb_asset_add_light", "gb_asset_get_desc", "gb_asset_material_name",
     "gb_read_pbrdf", "gb_render_direct", "gb_scene_create_ex", "gb_scene_refit", "gb_render_hybrid_direct",
+    "gb_bvh_build_stats",
 ]
 
 _lib = None
@@ -142,6 +161,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_scene_create.argtypes = [vp, C.POINTER(SceneDesc), C.POINTER(vp)]
     lib.gb_scene_create_ex.argtypes = [vp, C.POINTER(SceneDesc), C.POINTER(BuildOptions), C.POINTER(vp)]
     lib.gb_scene_refit.argtypes = [vp, vp, vp]
+    lib.gb_bvh_build_stats.argtypes = [vp, ip, vp, vp]
     lib.gb_scene_destroy.argtypes = [vp]
     lib.gb_scene_destroy.restype = None
     lib.gb_scene_get_info.argtypes = [vp, C.POINTER(SceneInfo)]

@@ -155,6 +155,15 @@ typedef struct {
                                      2 .. 64; 0 = 32 */
 } gb_build_options;
 
+/* Host BVH build alone (GB_BVH_HOST_SAH; no device needed): the tree
+ * gb_scene_create_ex would upload, summarised.  For inspecting build options
+ * before a scene is made. */
+typedef struct {
+    int num_nodes, depth, binary_nodes, num_triangles;
+    double build_ms;
+} gb_bvh_stats;
+int gb_bvh_build_stats(const float* positions, int num_triangles, const gb_build_options* opts, gb_bvh_stats* out);
+
 /* Uploads triangles, materials and lights and builds the BVH (replaces
  * setup_rta's plugin_create_rt_set + convert_and_upload_materials,
  * hl-main.cpp:357-464, and hybrid_pt::activate's light copy).
