@@ -1493,6 +1493,7 @@ int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, i
 int gb_render_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* d,
                      int light_samples, float* out_rgb, int out_is_device) {
     if (!ctx || !scene) return fail(ctx, GB_ERR_INVALID, "null context or scene");
+    if (scene->ctx != ctx) return fail(ctx, GB_ERR_INVALID, "scene belongs to another context");
     int rc = check_render_desc(ctx, cam, d);
     if (rc != GB_OK) return rc;
     if (light_samples <= 0 || light_samples > (1 << 20)) return fail(ctx, GB_ERR_INVALID, "bad light sample count");
@@ -1523,6 +1524,7 @@ int gb_render_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const g
 int gb_render_hybrid_direct(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_render_desc* d,
                             int camera_samples, int light_samples, float* out_rgb, int out_is_device) {
     if (!ctx || !scene) return fail(ctx, GB_ERR_INVALID, "null context or scene");
+    if (scene->ctx != ctx) return fail(ctx, GB_ERR_INVALID, "scene belongs to another context");
     int rc = check_render_desc(ctx, cam, d);
     if (rc != GB_OK) return rc;
     if (camera_samples <= 0 || light_samples <= 0 || (long long)camera_samples * light_samples > (1 << 20))
