@@ -9,8 +9,10 @@
 //               (hybrid_area_lights: -s camera samples, --light-samples per camera sample)
 //
 // scene.bin (written by globillum_gb300.scenes.write_scene_bin): magic
-// "GBSC", version 2, counts, then positions, normals, material indices,
-// materials, principled parameters, lights and the camera, little endian.
+// "GBSC", version 2 or 3, counts, then positions, normals, material indices,
+// materials, principled parameters, lights and the camera; version 3 adds
+// the diffuse textures, texture coordinates and per-material texture
+// indices.  Little endian.
 // The image is written like save_image (util.cpp:111-150): pixel (x, y) to
 // (w-1-x, h-1-y), here as a float PFM.
 #include <cstdio>
@@ -32,6 +34,11 @@ struct SceneFile {
     std::vector<gb_principled_params> params;
     std::vector<gb_light> lights;
     gb_camera cam{};
+    // version 3: diffuse textures
+    std::vector<std::vector<uint8_t>> pixels;
+    std::vector<gb_texture> textures;
+    std::vector<float> texcoords;  // 6 per triangle, empty without textures
+    std::vector<int> dtex;         // per material, empty without textures
 };
 
 template <typename T> bool rd(std::ifstream& f, T* p, size_t n) {
@@ -53,7 +60,8 @@ bool load_scene(const char* path, SceneFile* s) {
     if (!f) return false;
     char magic[4];
     int32_t hdr[5];  // version, triangles, materials, params, lights
-    if (!rd(f, magic, 4) || std::memcmp(magic, "GBSC", 4) != 0 || !rd(f, hdr, 5) || hdr[0] != 2) return false;
+    if (!rd(f, magic, 4) || std::memcmp(magic, "GBSC", 4) != 0 || !rd(f, hdr, 5) || (hdr[0] != 2 && hdr[0] != 3))
+        return false;
     int nt = hdr[1], nm = hdr[2], np = hdr[3], nl = hdr[4];
     if (nt <= 0 || nm <= 0 || np < 0 || nl < 0) return false;
     s->pos.resize(9 * (size_t)nt);
@@ -62,10 +70,31 @@ bool load_scene(const char* path, SceneFile* s) {
     s->mats.resize(nm);
     s->params.resize(np);
     s->lights.resize(nl);
-    return rd(f, s->pos.data(), s->pos.size()) && rd(f, s->nrm.data(), s->nrm.size()) &&
-           rd(f, s->mat.data(), s->mat.size()) && rd(f, s->mats.data(), s->mats.size()) &&
-           (np == 0 || rd(f, s->params.data(), s->params.size())) &&
-           (nl == 0 || rd(f, s->lights.data(), s->lights.size())) && rd(f, &s->cam, 1) && no_sky_maps(s);
+    if (!(rd(f, s->pos.data(), s->pos.size()) && rd(f, s->nrm.data(), s->nrm.size()) &&
+          rd(f, s->mat.data(), s->mat.size()) && rd(f, s->mats.data(), s->mats.size()) &&
+          (np == 0 || rd(f, s->params.data(), s->params.size())) &&
+          (nl == 0 || rd(f, s->lights.data(), s->lights.size())) && rd(f, &s->cam, 1) && no_sky_maps(s)))
+        return false;
+    if (hdr[0] == 2) return true;
+    // version 3: int32 texture count, then per texture int32 w, h and w*h*4 bytes;
+    // int32 flag, then (flag = 1) 6 floats per triangle and one int32 per material
+    int32_t ntex = 0, flag = 0;
+    if (!rd(f, &ntex, 1) || ntex < 0 || ntex > 4096) return false;
+    s->pixels.resize(ntex);
+    for (int k = 0; k < ntex; ++k) {
+        int32_t wh[2];
+        if (!rd(f, wh, 2) || wh[0] <= 0 || wh[1] <= 0 || (long long)wh[0] * wh[1] > (1ll << 26)) return false;
+        s->pixels[k].resize(4 * (size_t)wh[0] * wh[1]);
+        if (!rd(f, s->pixels[k].data(), s->pixels[k].size())) return false;
+        s->textures.push_back(gb_texture{wh[0], wh[1], s->pixels[k].data()});
+    }
+    if (!rd(f, &flag, 1)) return false;
+    if (flag == 1) {
+        s->texcoords.resize(6 * (size_t)nt);
+        s->dtex.resize(nm);
+        if (!rd(f, s->texcoords.data(), s->texcoords.size()) || !rd(f, s->dtex.data(), s->dtex.size())) return false;
+    }
+    return true;
 }
 
 bool write_pfm(const char* path, int w, int h, const std::vector<float>& rgb) {
@@ -124,6 +153,10 @@ int main(int argc, char** argv) {
     sd.params = sf.params.empty() ? nullptr : sf.params.data();
     sd.num_lights = (int)sf.lights.size();
     sd.lights = sf.lights.empty() ? nullptr : sf.lights.data();
+    sd.num_textures = (int)sf.textures.size();
+    sd.textures = sf.textures.empty() ? nullptr : sf.textures.data();
+    sd.texcoords = sf.texcoords.empty() ? nullptr : sf.texcoords.data();
+    sd.diffuse_texture = sf.dtex.empty() ? nullptr : sf.dtex.data();
     gb::rt_set set;
     set.scene = &sd;
     set.camera = sf.cam;

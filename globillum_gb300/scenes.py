@@ -347,9 +347,11 @@ def random_rays(scene: SceneData, n: int, seed: int = 0, spread: float = 0.2):
 
 def write_scene_bin(scene: SceneData, path) -> None:
     """Binary scene file read by the headless front-end (host/gi_headless.cpp):
-    magic "GBSC", int32 version 2 (gb_light with its sky fields; rect lights
-    only), triangles, materials, params, lights, then the gb_scene_desc arrays
-    and the gb_camera, little endian."""
+    magic "GBSC", int32 version 3, triangles, materials, params, lights, then
+    the gb_scene_desc arrays (gb_light with its sky fields; rect lights only)
+    and the gb_camera; then the textures (int32 count, per texture int32 w, h
+    and RGBA8 pixels) and an int32 flag followed, when 1, by 6 texture
+    coordinates per triangle and a texture index per material.  Little endian."""
     import ctypes as C
     from . import gbpt
     desc, keep = gbpt.make_scene_desc(scene)
@@ -358,7 +360,7 @@ def write_scene_bin(scene: SceneData, path) -> None:
     mid = np.ascontiguousarray(scene.material_index, np.int32)
     with open(path, "wb") as f:
         f.write(b"GBSC")
-        f.write(np.array([2, pos.shape[0], len(scene.materials), len(scene.params), len(scene.lights)],
+        f.write(np.array([3, pos.shape[0], len(scene.materials), len(scene.params), len(scene.lights)],
                          np.int32).tobytes())
         f.write(pos.tobytes())
         f.write(nrm.tobytes())
@@ -370,6 +372,17 @@ def write_scene_bin(scene: SceneData, path) -> None:
             f.write(C.string_at(C.addressof(desc.lights.contents), C.sizeof(gbpt.Light) * len(scene.lights)))
         cam = gbpt.make_camera(scene.camera)
         f.write(C.string_at(C.addressof(cam), C.sizeof(gbpt.Camera)))
+        texs = [np.ascontiguousarray(t, np.uint8) for t in (scene.textures or [])]
+        f.write(np.int32(len(texs)).tobytes())
+        for t in texs:
+            f.write(np.array([t.shape[1], t.shape[0]], np.int32).tobytes())
+            f.write(t.tobytes())
+        dt = np.array([int(m.get("diffuse_texture", -1)) for m in scene.materials], np.int32)
+        textured = scene.texcoords is not None and (dt >= 0).any()
+        f.write(np.int32(1 if textured else 0).tobytes())
+        if textured:
+            f.write(np.ascontiguousarray(scene.texcoords, np.float32).tobytes())
+            f.write(dt.tobytes())
 
 
 def read_pfm(path) -> np.ndarray:

@@ -65,3 +65,21 @@ def test_headless_hybrid_area_lights(gpu_ctx, tmp_path):
     ref = scene.render_hybrid_direct(sc.camera, rd, 2, 3)
     scene.close()
     assert np.array_equal(img, ref[::-1, ::-1])
+
+
+def test_headless_textured_scene(gpu_ctx, tmp_path):
+    """Scene file version 3 carries textures: the drop-in renders the
+    textured frame of gb_render."""
+    exe = build.build_headless()
+    sc = scenes.with_textures(scenes.cornell(width=40, height=32, spp=2, max_bounces=3), fraction=1.0, scale=2.0)
+    scenes.write_scene_bin(sc, tmp_path / "t.bin")
+    r = sc.render
+    out = tmp_path / "t.pfm"
+    cmd = [str(exe), str(tmp_path / "t.bin"), str(out), "-r", f"{r['width']}x{r['height']}", "-s", str(r["spp"]),
+           "-l", str(r["max_bounces"]), "--offsets", repr(r["ray_offset"]), repr(r["shadow_offset"]), "--halton"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    scene = gpu_ctx.scene(sc)
+    ref = scene.render(sc.camera, dict(r))
+    scene.close()
+    assert np.array_equal(scenes.read_pfm(out), ref[::-1, ::-1])
