@@ -476,7 +476,8 @@ def inverse_leg(ctx, args, torch, dist):
 def run_gbpt(args, rank, world):
     import torch
     from globillum_gb300 import build, gbpt
-    build.build_lib()
+    if not build.LIB.exists():  # an existing build is used as it is (with its own compile options)
+        build.build_lib()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dist = None
