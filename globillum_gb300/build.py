@@ -69,7 +69,10 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     cpp = [CSRC / "gbpt_api.cpp", CSRC / "gbpt_bvh.cpp", CSRC / "gbpt_ingest.cpp"]
     deps = cu + cpp + _sources()
     # the library records the build-time defines it was made with
-    flags = f"GB_TRAV_MIN_BLOCKS={os.environ.get('GBPT_TRAV_MIN_BLOCKS', '')}"
+    # experimental compile options (GBPT_<name> in the environment -> -DGB_<name>)
+    knobs = ("TRAV_MIN_BLOCKS", "SMEM_STACK", "PREFETCH", "SPLIT_NEE", "SHADE_MIN_BLOCKS", "STREAM_MIN_BLOCKS",
+             "WIDE_STREAM_GRIDS")
+    flags = " ".join(f"GB_{k}={os.environ.get('GBPT_' + k, '')}" for k in knobs)
     stamp = LIB.with_suffix(".flags")
     if not stamp.exists() or stamp.read_text() != flags:
         force = True
@@ -82,11 +85,12 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
         objs.append(o)
         c = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
              "-Xcompiler", "-ffp-contract=off", "-c", str(s), "-o", str(o)]
-        # GBPT_TRAV_MIN_BLOCKS: resident 128-thread blocks per SM the traversal
-        # kernels are compiled for (register budget; default 7)
-        mb = os.environ.get("GBPT_TRAV_MIN_BLOCKS")
-        if mb:
-            c.insert(1, f"-DGB_TRAV_MIN_BLOCKS={int(mb)}")
+        # e.g. GBPT_TRAV_MIN_BLOCKS: resident 128-thread blocks per SM the
+        # traversal kernels are compiled for (register budget; default 7)
+        for k in knobs:
+            v = os.environ.get("GBPT_" + k)
+            if v:
+                c.insert(1, f"-DGB_{k}={int(v)}")
         if verbose_ptxas:
             c.insert(1, "-Xptxas=-v")
         cmds.append(c)

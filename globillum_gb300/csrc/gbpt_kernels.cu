@@ -42,6 +42,44 @@ constexpr int kBlock = 128;
 #endif
 constexpr int kStack = 32;
 constexpr int kIterLimit = 1 << 22;
+// Experimental build options, each off by default (measured in the design
+// notes): traversal stack entries kept in shared memory, L2 prefetch of hit
+// child nodes, light samples in a kernel of their own, register budgets and
+// grid of the streaming kernels.
+#ifndef GB_SMEM_STACK
+#define GB_SMEM_STACK 0
+#endif
+#ifndef GB_PREFETCH
+#define GB_PREFETCH 0
+#endif
+#ifndef GB_SPLIT_NEE
+#define GB_SPLIT_NEE 0
+#endif
+#ifndef GB_SHADE_MIN_BLOCKS
+#define GB_SHADE_MIN_BLOCKS 1
+#endif
+#ifndef GB_STREAM_MIN_BLOCKS
+#define GB_STREAM_MIN_BLOCKS 1
+#endif
+#ifndef GB_WIDE_STREAM_GRIDS
+#define GB_WIDE_STREAM_GRIDS 1
+#endif
+constexpr int kSmemStack = GB_SMEM_STACK;
+
+// A thread's traversal stack: entry e < kSmemStack at top[e * stride]
+// (a column of a shared-memory array), deeper entries in deep[e - kSmemStack].
+struct StackRef {
+    uint2* top;
+    uint2* deep;
+    int stride;
+};
+__device__ __forceinline__ void stack_put(const StackRef& k, int e, uint2 v) {
+    if (e < kSmemStack) k.top[e * k.stride] = v;
+    else k.deep[e - kSmemStack] = v;
+}
+__device__ __forceinline__ uint2 stack_get(const StackRef& k, int e) {
+    return e < kSmemStack ? k.top[e * k.stride] : k.deep[e - kSmemStack];
+}
 
 __device__ __forceinline__ v3 ld3(const float4 a) { return mk(a.x, a.y, a.z); }
 
@@ -179,6 +217,15 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
         uint32_t meta = __byte_perm(slot < 4u ? meta_lo : meta_hi, 0u, 0x4440u | (slot & 3u));
         hits_t |= (meta >> 5) << (meta & 31u);
     }
+#if GB_PREFETCH
+    // the hit inner children will be visited: start their fetch into L2 now
+    for (uint32_t m = inner; m; m &= m - 1u) {
+        const uint32_t s = (uint32_t)__ffs(m) - 1u;
+        const float4* cp = nodes + 5 * (size_t)(__float_as_uint(n1.x) + (uint32_t)__popc(imask & ((1u << s) - 1u)));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(cp)));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(cp + 4)));
+    }
+#endif
     *ng = make_uint2(__float_as_uint(n1.x), (xor_permute8(inner, r.oxor) << 24) | imask);
     *tg = make_uint2(__float_as_uint(n1.y), hits_t);
 }
@@ -228,7 +275,7 @@ __device__ __forceinline__ bool tri_step(const float4* __restrict__ tris, const 
 // is the (t, id)-minimum in s (any-hit: best_id != none when found).
 template <bool INSTR>
 __device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, const RayInv& r, float tmax, Trav& s,
-                                          uint2* stack, uint32_t* status, uint32_t* nvis) {
+                                          const StackRef& stack, uint32_t* status, uint32_t* nvis) {
     if (s.ng.y > 0x00ffffffu) {
         uint32_t k = 31u - (uint32_t)__clz(s.ng.y);
         s.ng.y &= ~(1u << k);
@@ -237,14 +284,14 @@ __device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, cons
         uint32_t child = s.ng.x + (uint32_t)__popc(imask & ((1u << slot) - 1u));
         if (s.ng.y > 0x00ffffffu) {
             if (s.sp >= kStack) { atomicOr(status, ST_STACK_OVERFLOW); return true; }
-            stack[s.sp++] = s.ng;
+            stack_put(stack, s.sp++, s.ng);
         }
         if (INSTR) ++*nvis;
         intersect_node(nodes, child, r, fminf(s.best_t, tmax), &s.ng, &s.tg);
         return false;
     }
     if (s.sp > 0) {
-        uint2 g = stack[--s.sp];
+        uint2 g = stack_get(stack, --s.sp);
         if (g.y > 0x00ffffffu) s.ng = g;
         else s.tg = g;
         return false;
@@ -255,7 +302,7 @@ __device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, cons
 // Whole traversal of one ray without warp cooperation.
 template <bool ANY, bool INSTR>
 __device__ __forceinline__ bool trav_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                          const RayInv& r, float tmax, Trav& s, uint2* stack, uint32_t* status,
+                                          const RayInv& r, float tmax, Trav& s, const StackRef& stack, uint32_t* status,
                                           uint32_t* nvis, uint32_t* ntri) {
     while (s.tg.y != 0u)
         if (tri_step<ANY, INSTR>(tris, r, tmax, s, ntri)) return true;
@@ -273,7 +320,8 @@ __device__ __forceinline__ bool traverse(const DevScene& S, const RayInv& r, flo
                                          uint32_t* status) {
     Trav s;
     trav_init(s, r);
-    uint2 stack[kStack];
+    uint2 lstack[kStack];
+    const StackRef stack{lstack, lstack + kSmemStack, 1};
     uint32_t nv = 0, nt = 0;
     int iters = 0;
     while (!trav_step<ANY, false>(S.nodes, S.tris, r, tmax, s, stack, status, &nv, &nt)) {
@@ -495,7 +543,7 @@ __device__ __forceinline__ void end_paths(const Frame& F, bool ended, uint32_t s
 // Stores the sample of every ended path (new_path's input to the moving
 // average) and starts the next paths of the chunk on the freed slots,
 // appending them to the next extension queue.
-__global__ void __launch_bounds__(kBlock) k_regen(Frame F, RenderParams P) {
+__global__ void __launch_bounds__(kBlock, GB_STREAM_MIN_BLOCKS) k_regen(Frame F, RenderParams P) {
     const int it = *F.iter;
     const uint32_t* cn = ctr_set(F, it + 1);
     const uint32_t count = cn[4];   // ended paths of this iteration (free queue)
@@ -655,7 +703,9 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
     RayInv r;
     float tmax = 0.0f;
     Trav s;
-    uint2 stack[kStack];
+    __shared__ uint2 s_stack[kSmemStack > 0 ? kSmemStack * kBlock : 1];
+    uint2 deep[kStack - kSmemStack];
+    const StackRef stack{s_stack + threadIdx.x, deep, kBlock};
     const float4* nodes = nullptr;
     const float4* tris = nullptr;
     const float4* shade = nullptr;
@@ -726,7 +776,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
                 const uint32_t ma = __ballot_sync(0xffffffffu, act);
                 bool do_tri = want_tri;
                 if (want_tri && 5u * (uint32_t)__popc(mt) < (uint32_t)__popc(ma) && s.sp < kStack) {
-                    stack[s.sp++] = s.tg;
+                    stack_put(stack, s.sp++, s.tg);
                     s.tg.y = 0u;
                     do_tri = false;
                 }
@@ -752,6 +802,38 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
 // Closest hit of the extension queue.  Misses add handle_no_hit's
 // contribution and end their path; hits draw the bounce's uniforms and emit
 // the area-light shadow ray (arealight-sampler-cpu.cpp:25-143).
+// The light sample of a hit (generate_arealight_sample,
+// arealight-sampler-cpu.cpp:25-143) on the path's light draw: shadow ray,
+// potential_sample_contribution and the path draw of this bounce.
+__device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, uint32_t slot, v3 Pp, v3 Nr) {
+    const DevScene& S = R.S;
+    MrgState st = ld_mrg(F.rng, slot);
+    v3 rnd = draw3(&st);
+    st_mrg(F.rng, slot, st);
+    v3 lr = rnd;
+    if (R.rng_mode == 1) {
+        int pid = (int)(F.pix[slot] - R.pixel_base) + 1;
+        float hy = halton(pid, 3);
+        lr = mk(halton(pid, 2), hy, hy);
+    }
+    v3 so = mk(0.0f, 0.0f, 0.0f), sd = mk(0.0f, 0.0f, 0.0f), psc = mk(0.0f, 0.0f, 0.0f);
+    float smax = -1.0f, scale = 0.0f;
+    if (S.n_lights > 0) {
+        int l = pick_light(S.lights, S.n_lights, S.overall_power, lr.z);
+        LightRec L = S.lights[l];
+        if (L.type == 1)
+            sky_light_sample(S.sky, L.power, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset, &so, &sd,
+                             &smax, &psc);
+        else
+            rect_light_sample(L, S.lights_eval[l].col, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset,
+                              &so, &sd, &smax, &psc, &scale);
+    }
+    F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
+    F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+    F.psc[slot] = make_float4(psc.x, psc.y, psc.z, scale);
+    F.rnd[slot] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
+}
+
 template <bool INSTR, int MODE>
 __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, RenderParams P) {
     const int it = *F.iter;
@@ -794,31 +876,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                 float4 na = __ldg(sh + 3), nb = __ldg(sh + 4), nc = __ldg(sh + 5);
                 v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
                 v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
-                MrgState st = ld_mrg(F.rng, slot);
-                v3 rnd = draw3(&st);
-                st_mrg(F.rng, slot, st);
-                v3 lr = rnd;
-                if (R.rng_mode == 1) {
-                    int pid = (int)(F.pix[slot] - R.pixel_base) + 1;
-                    float hy = halton(pid, 3);
-                    lr = mk(halton(pid, 2), hy, hy);
-                }
-                v3 so = mk(0.0f, 0.0f, 0.0f), sd = mk(0.0f, 0.0f, 0.0f), psc = mk(0.0f, 0.0f, 0.0f);
-                float smax = -1.0f, scale = 0.0f;
-                if (S.n_lights > 0) {
-                    int l = pick_light(S.lights, S.n_lights, S.overall_power, lr.z);
-                    LightRec L = S.lights[l];
-                    if (L.type == 1)
-                        sky_light_sample(S.sky, L.power, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset,
-                                         &so, &sd, &smax, &psc);
-                    else
-                        rect_light_sample(L, S.lights_eval[l].col, S.overall_power, Pp, Nr, lr.x, lr.y,
-                                          R.sp.shadow_offset, &so, &sd, &smax, &psc, &scale);
-                }
-                F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
-                F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-                F.psc[slot] = make_float4(psc.x, psc.y, psc.z, scale);
-                F.rnd[slot] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
+                if (!GB_SPLIT_NEE) nee_at_hit(F, R, slot, Pp, Nr);
                 F.hit_p[slot] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
                 F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id));
             }
@@ -828,6 +886,19 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
     };
     ray_loop<false, INSTR, MODE>(count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[3], nvis); add_stats(&F.stats[4], ntri); }
+}
+
+// Light samples of every hit of the iteration (shadow queue), when they are
+// not taken inside k_extend (GB_SPLIT_NEE).
+__global__ void __launch_bounds__(kBlock) k_nee(Frame F) {
+    const uint32_t* cs = ctr_set(F, *F.iter);
+    const uint32_t count = cs[2];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const uint32_t slot = F.q[2][i];
+        const SceneRec& R = F.scenes[F.ps[slot]];
+        nee_at_hit(F, R, slot, ld3(F.hit_p[slot]), ld3(F.hit_n[slot]));
+    }
 }
 
 // Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
@@ -914,7 +985,7 @@ __device__ __noinline__ void texture_hit(const Frame& F, const SceneRec& R, uint
 // writes the vertex record of the path-replay adjoint.  Every path leaves
 // with pb's bounce field = the number of vertices it shaded.
 template <int MODE, bool TEX>
-__global__ void __launch_bounds__(kBlock) k_shade(Frame F, RenderParams P) {
+__global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     uint32_t* cn = ctr_set(F, it + 1);
@@ -1399,6 +1470,10 @@ template <bool INSTR, int MODE>
 void launch_extend_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static Grid g = persistent_grid(k_extend<INSTR, MODE>);
     k_extend<INSTR, MODE><<<traversal_grid(g, P.blocks_per_sm), kBlock, 0, st>>>(F, P);
+    if (GB_SPLIT_NEE) {
+        static int gn = persistent_blocks(k_nee);
+        k_nee<<<gn, kBlock, 0, st>>>(F);
+    }
 }
 
 template <bool INSTR, int MODE>
@@ -1435,10 +1510,16 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
     return cudaGetLastError();
 }
 
+// Grid of the streaming per-path kernels: one thread per slot
+// (GB_WIDE_STREAM_GRIDS, the default), or persistent.
+inline int stream_grid(int persistent, int nslots) {
+    return GB_WIDE_STREAM_GRIDS ? std::max(1, blocks_for(nslots)) : persistent;
+}
+
 template <int MODE, bool TEX>
 void launch_shade_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g = persistent_blocks(k_shade<MODE, TEX>);
-    k_shade<MODE, TEX><<<g, kBlock, 0, st>>>(F, P);
+    k_shade<MODE, TEX><<<stream_grid(g, F.nslots), kBlock, 0, st>>>(F, P);
 }
 
 // The texture path is compiled into its own variant so that frames without
@@ -1491,7 +1572,7 @@ cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, do
 
 cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static int g0 = persistent_blocks(k_regen);
-    k_regen<<<g0, kBlock, 0, st>>>(F, P);
+    k_regen<<<stream_grid(g0, F.nslots), kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
 }
 
