@@ -215,15 +215,9 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nsc
         cudaStreamSynchronize(ctx->stream);
         free_all(ctx->slot_allocs);
         ctx->slot_cap = 0;
-        size_t v4 = sizeof(float4) * (size_t)nslots;
-        float4** bufs[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
-        for (float4** b : bufs)
-            if ((e = dalloc(ctx->slot_allocs, (void**)b, v4)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->slot_allocs, (void**)&F.rdiff, 3 * v4)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->slot_allocs, (void**)&F.rng, sizeof(MrgState) * (size_t)nslots)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->slot_allocs, (void**)&F.pix, 4 * (size_t)nslots)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->slot_allocs, (void**)&F.pb, 4 * (size_t)nslots)) != cudaSuccess) return e;
-        if ((e = dalloc(ctx->slot_allocs, (void**)&F.ps, 4 * (size_t)nslots)) != cudaSuccess) return e;
+        unsigned char* recs = nullptr;
+        if ((e = dalloc(ctx->slot_allocs, (void**)&recs, kSlotBytes * (size_t)nslots)) != cudaSuccess) return e;
+        bind_slots(F, recs);
         for (int k = 0; k < 4; ++k)
             if ((e = dalloc(ctx->slot_allocs, (void**)&F.q[k], 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.ctr, 4 * 32)) != cudaSuccess) return e;
@@ -875,10 +869,9 @@ std::vector<uint64_t> graph_key(const gb_ctx* ctx, const RenderParams& P, int ns
     k.push_back(((uint64_t)(uint32_t)F.ntot << 32) | (uint32_t)F.nslots);
     k.push_back(((uint64_t)(uint32_t)F.nscenes << 32) | (uint32_t)nstart);
     k.push_back(((uint64_t)(uint32_t)max_iters << 32) | (ctx->instrument ? 1u : 0u));
-    const void* ptrs[] = {F.scenes, F.ray_o, F.ray_d, F.tp, F.accum, F.sh_o, F.sh_d, F.psc, F.rnd, F.hit_p,
-                          F.hit_n, F.rng, F.pix, F.ps, F.pb, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
+    const void* ptrs[] = {F.scenes, F.slots, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
                           F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr,
-                          F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad, F.rdiff};
+                          F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad};
     for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
     k.push_back(((uint64_t)(uint32_t)F.grad_stride << 32) | (uint32_t)F.grad_replicas);
     static_assert(sizeof(RenderParams) % 4 == 0, "RenderParams is made of 32-bit words");

@@ -414,6 +414,11 @@ __device__ __forceinline__ void st_mrg(MrgState* base, size_t i, const MrgState&
     q[1] = make_uint2(m.s1[2], m.s2[0]);
     q[2] = make_uint2(m.s2[1], m.s2[2]);
 }
+// the same for the stream of a slot record
+__device__ __forceinline__ MrgState ld_mrg(const SlotField<MrgState>& f, size_t slot) { return ld_mrg(&f[slot], 0); }
+__device__ __forceinline__ void st_mrg(const SlotField<MrgState>& f, size_t slot, const MrgState& m) {
+    st_mrg(&f[slot], 0, m);
+}
 __device__ __forceinline__ v3 draw3(MrgState* m) {
     curandStateMRG32k3a st = mrg_expand(*m);
     v3 r = draw3(&st);
@@ -478,7 +483,7 @@ __global__ void k_jitter_pool(Frame F, RenderParams P) {
 
 // Ray differentials of a slot, 12 floats in 3 planes of nslots float4.
 __device__ __forceinline__ RayDiff ld_rdiff(const Frame& F, uint32_t slot) {
-    const float4 a = F.rdiff[slot], b = F.rdiff[(size_t)F.nslots + slot], c = F.rdiff[2 * (size_t)F.nslots + slot];
+    const float4 a = F.rdiff[0][slot], b = F.rdiff[1][slot], c = F.rdiff[2][slot];
     RayDiff r;
     r.uo = mk(a.x, a.y, a.z);
     r.ud = mk(a.w, b.x, b.y);
@@ -487,9 +492,9 @@ __device__ __forceinline__ RayDiff ld_rdiff(const Frame& F, uint32_t slot) {
     return r;
 }
 __device__ __forceinline__ void st_rdiff(const Frame& F, uint32_t slot, const RayDiff& r) {
-    F.rdiff[slot] = make_float4(r.uo.x, r.uo.y, r.uo.z, r.ud.x);
-    F.rdiff[(size_t)F.nslots + slot] = make_float4(r.ud.y, r.ud.z, r.ro.x, r.ro.y);
-    F.rdiff[2 * (size_t)F.nslots + slot] = make_float4(r.ro.z, r.rd.x, r.rd.y, r.rd.z);
+    F.rdiff[0][slot] = make_float4(r.uo.x, r.uo.y, r.uo.z, r.ud.x);
+    F.rdiff[1][slot] = make_float4(r.ud.y, r.ud.z, r.ro.x, r.ro.y);
+    F.rdiff[2][slot] = make_float4(r.ro.z, r.rd.x, r.rd.y, r.rd.z);
 }
 
 __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t l) {
@@ -926,7 +931,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
             uint32_t slot = qsh[q];
             float smax = F.sh_o[slot].w;
             bool occl = smax < 0.0f || h.best_id != 0xffffffffu;
-            reinterpret_cast<float*>(F.sh_d + slot)[3] = occl ? 1.0f : 0.0f;
+            reinterpret_cast<float*>(&F.sh_d[slot])[3] = occl ? 1.0f : 0.0f;
         }
     };
     ray_loop<true, INSTR, MODE>(count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);

@@ -63,28 +63,60 @@ constexpr int kMaxAdjBounces = 16;   // bounces the adjoint records per path
 
 constexpr int kMaxRounds = 64;  // path samples per chunk
 
-// Wavefront state: per path slot (SoA) and per global pixel.
+// Per-slot state of the wavefront: one 256-byte record per path slot.
+// Slots are visited in queue order, which is not slot order, so every field
+// access of a slot is a scattered access.  A record keeps what one stage
+// reads or writes together in one 128-byte line, so that a stage touches a
+// few whole 32-byte sectors of a slot instead of one partly used sector per
+// field:
+//   line 0 (path state: written by path start and by shading)
+//     0 ray_o, 16 ray_d, 32 tp, 48 accum, 64 pix, 68 ps, 72 pb,
+//     80 rdiff[0..2] (ray differentials, textured scenes)
+//   line 1 (hit record: written by the closest-hit kernel)
+//     128 hit_p, 144 hit_n, 160 sh_o, 176 sh_d, 192 psc, 208 rnd, 224 rng
+constexpr size_t kSlotBytes = 256;
+enum : size_t {
+    kSlotRayO = 0, kSlotRayD = 16, kSlotTp = 32, kSlotAccum = 48, kSlotPix = 64, kSlotPs = 68, kSlotPb = 72,
+    kSlotRdiff = 80, kSlotHitP = 128, kSlotHitN = 144, kSlotShO = 160, kSlotShD = 176, kSlotPsc = 192,
+    kSlotRnd = 208, kSlotRng = 224
+};
+static_assert(kSlotRdiff + 48 <= 128 && kSlotRng + 24 <= kSlotBytes, "slot record layout");
+
+// One field of the slot records: f[slot] is that field of record `slot`.
+template <class T>
+struct SlotField {
+    unsigned char* base = nullptr;  // the field in record 0
+#ifdef __CUDACC__
+    __host__ __device__
+#endif
+    inline T& operator[](size_t slot) const {
+        return *reinterpret_cast<T*>(base + slot * kSlotBytes);
+    }
+};
+
+// Wavefront state: per path slot (records above) and per global pixel.
 struct Frame {
     int ntot;          // pixels of all scenes
     int nslots;        // path slots in flight
     const SceneRec* scenes;  // device array
     int nscenes;
-    // per slot
-    float4* ray_o;     // origin xyz, t_max
-    float4* ray_d;     // direction xyz
-    float4* tp;        // throughput
-    float4* accum;     // col_accum of the slot's path
-    float4* sh_o;      // shadow origin xyz, max_t
-    float4* sh_d;      // shadow direction xyz (to_light), w = occluded
-    float4* psc;       // potential_sample_contribution
-    float4* rnd;       // path draw of this bounce
-    float4* hit_p;     // hit point xyz | material index bits
-    float4* hit_n;     // interpolated (unnormalised) normal | hit triangle id bits
-    float4* rdiff;     // ray differentials of textured scenes: 3 planes of nslots (RayDiff packed)
-    MrgState* rng;     // light/path stream of the slot's path
-    uint32_t* pix;     // global pixel of the slot's path
-    uint32_t* ps;      // scene of the slot's path
-    uint32_t* pb;      // path index << 10 | bounce
+    // per slot: nslots records of kSlotBytes at `slots`, viewed field by field
+    unsigned char* slots;
+    SlotField<float4> ray_o;     // origin xyz, t_max
+    SlotField<float4> ray_d;     // direction xyz
+    SlotField<float4> tp;        // throughput
+    SlotField<float4> accum;     // col_accum of the slot's path
+    SlotField<float4> sh_o;      // shadow origin xyz, max_t
+    SlotField<float4> sh_d;      // shadow direction xyz (to_light), w = occluded
+    SlotField<float4> psc;       // potential_sample_contribution
+    SlotField<float4> rnd;       // path draw of this bounce
+    SlotField<float4> hit_p;     // hit point xyz | material index bits
+    SlotField<float4> hit_n;     // interpolated (unnormalised) normal | hit triangle id bits
+    SlotField<float4> rdiff[3];  // ray differentials of textured scenes (RayDiff packed)
+    SlotField<MrgState> rng;     // light/path stream of the slot's path
+    SlotField<uint32_t> pix;     // global pixel of the slot's path
+    SlotField<uint32_t> ps;      // scene of the slot's path
+    SlotField<uint32_t> pb;      // path index << 10 | bounce
     uint32_t* q[4];    // queues: extension (ping/pong), shadow, ended paths; nslots entries each
     // per global pixel
     float4* out;       // output_color (moving average)
@@ -110,6 +142,27 @@ struct Frame {
     int grad_stride;   // floats per replica
     int grad_replicas;
 };
+
+// Points the slot fields of F at the records at `slots` (kSlotBytes-aligned).
+inline void bind_slots(Frame& F, unsigned char* slots) {
+    F.slots = slots;
+    auto at = [slots](size_t off) { return slots ? slots + off : nullptr; };
+    F.ray_o.base = at(kSlotRayO);
+    F.ray_d.base = at(kSlotRayD);
+    F.tp.base = at(kSlotTp);
+    F.accum.base = at(kSlotAccum);
+    F.pix.base = at(kSlotPix);
+    F.ps.base = at(kSlotPs);
+    F.pb.base = at(kSlotPb);
+    for (int k = 0; k < 3; ++k) F.rdiff[k].base = at(kSlotRdiff + 16 * (size_t)k);
+    F.hit_p.base = at(kSlotHitP);
+    F.hit_n.base = at(kSlotHitN);
+    F.sh_o.base = at(kSlotShO);
+    F.sh_d.base = at(kSlotShD);
+    F.psc.base = at(kSlotPsc);
+    F.rnd.base = at(kSlotRnd);
+    F.rng.base = at(kSlotRng);
+}
 
 // Launch-wide parameters of one chunk.
 struct RenderParams {

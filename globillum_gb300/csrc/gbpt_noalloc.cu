@@ -51,12 +51,13 @@ constexpr size_t kCtr = align_up(4 * 32);
 constexpr size_t kStats = align_up(8 * 8);
 constexpr size_t kStatus = align_up(4);
 constexpr size_t kRec = align_up(sizeof(SceneRec));
-// One slot per pixel and one path sample per pass: 10 float4 slot planes,
-// slot RNG, pixel / scene / path words, 4 queues; per pixel the image, the
+constexpr size_t kSlots = kSlotBytes * (size_t)kNoAllocMaxPixels;  // slot records
+// One slot per pixel and one path sample per pass: the slot records and
+// 4 queues; per pixel the image, the
 // initial RNG states, the two stream cursors, the scene word, one sample and
 // one jitter value; counters, path counter, iteration, stats, status and the
 // scene record.
-constexpr size_t kScratchBytes = 10 * kV4 + kRng + 3 * kU32 + 4 * kU32 + kV4 + 3 * kRng + kU32 + 2 * kV4 + kCtr +
+constexpr size_t kScratchBytes = kSlots + 4 * kU32 + kV4 + 3 * kRng + kU32 + 2 * kV4 + kCtr +
                                  kCtr + kCtr + kStats + kStatus + kRec;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -83,12 +84,7 @@ Frame carve(unsigned char* base, int n, SceneRec** rec) {
     F.nslots = n;
     F.nscenes = 1;
     size_t off = 0;
-    float4** planes[] = {&F.ray_o, &F.ray_d, &F.tp, &F.accum, &F.sh_o, &F.sh_d, &F.psc, &F.rnd, &F.hit_p, &F.hit_n};
-    for (float4** p : planes) { *p = (float4*)(base + off); off += kV4; }
-    F.rng = (MrgState*)(base + off); off += kRng;
-    F.pix = (uint32_t*)(base + off); off += kU32;
-    F.pb = (uint32_t*)(base + off); off += kU32;
-    F.ps = (uint32_t*)(base + off); off += kU32;
+    bind_slots(F, base + off); off += kSlots;
     for (int k = 0; k < 4; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
     F.out = (float4*)(base + off); off += kV4;
     F.pristine = (MrgState*)(base + off); off += kRng;

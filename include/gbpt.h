@@ -474,7 +474,7 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
  * The scene is created beforehand (gb_scene_create allocates); this call
  * renders the same frame as gb_render into the caller's device buffer
  * `out_rgb` (w*h*3 floats) on `stream` (NULL = legacy default stream), with
- * its wavefront state in one fixed file-scope device array (about 22 MB,
+ * its wavefront state in one fixed file-scope device array (about 25 MB,
  * held by every GPU that loads the library until exit) instead of cudaMalloc.
  * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID.
  * The first call on a device looks the array up (cudaGetSymbolAddress) with
