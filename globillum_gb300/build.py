@@ -71,7 +71,7 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     # the library records the build-time defines it was made with
     # experimental compile options (GBPT_<name> in the environment -> -DGB_<name>)
     knobs = ("TRAV_MIN_BLOCKS", "SMEM_STACK", "PREFETCH", "SPLIT_NEE", "SHADE_MIN_BLOCKS", "STREAM_MIN_BLOCKS",
-             "WIDE_STREAM_GRIDS")
+             "WIDE_STREAM_GRIDS", "SHADOW_SPLIT")
     flags = " ".join(f"GB_{k}={os.environ.get('GBPT_' + k, '')}" for k in knobs)
     stamp = LIB.with_suffix(".flags")
     if not stamp.exists() or stamp.read_text() != flags:
@@ -94,10 +94,11 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
         if verbose_ptxas:
             c.insert(1, "-Xptxas=-v")
         cmds.append(c)
+    defines = [f"-DGB_{k}={int(os.environ['GBPT_' + k])}" for k in knobs if os.environ.get("GBPT_" + k)]
     for s in cpp:
         o = BUILD / (s.stem + ".o")
         objs.append(o)
-        cmds.append(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + _cuda_include(),
+        cmds.append(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", *defines, "-I" + _cuda_include(),
                      "-c", str(s), "-o", str(o)])
     _run_parallel(cmds)
     tmp = LIB.with_suffix(".so.tmp")

@@ -215,9 +215,11 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nsc
         cudaStreamSynchronize(ctx->stream);
         free_all(ctx->slot_allocs);
         ctx->slot_cap = 0;
-        unsigned char* recs = nullptr;
+        unsigned char *recs = nullptr, *shadow = nullptr;
         if ((e = dalloc(ctx->slot_allocs, (void**)&recs, kSlotBytes * (size_t)nslots)) != cudaSuccess) return e;
-        bind_slots(F, recs);
+        if (GB_SHADOW_SPLIT && (e = dalloc(ctx->slot_allocs, (void**)&shadow, 32 * (size_t)nslots)) != cudaSuccess)
+            return e;
+        bind_slots(F, recs, shadow);
         for (int k = 0; k < 4; ++k)
             if ((e = dalloc(ctx->slot_allocs, (void**)&F.q[k], 4 * (size_t)nslots)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->slot_allocs, (void**)&F.ctr, 4 * 32)) != cudaSuccess) return e;
@@ -869,7 +871,7 @@ std::vector<uint64_t> graph_key(const gb_ctx* ctx, const RenderParams& P, int ns
     k.push_back(((uint64_t)(uint32_t)F.ntot << 32) | (uint32_t)F.nslots);
     k.push_back(((uint64_t)(uint32_t)F.nscenes << 32) | (uint32_t)nstart);
     k.push_back(((uint64_t)(uint32_t)max_iters << 32) | (ctx->instrument ? 1u : 0u));
-    const void* ptrs[] = {F.scenes, F.slots, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
+    const void* ptrs[] = {F.scenes, F.slots, F.shadow, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
                           F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr,
                           F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad};
     for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);

@@ -75,6 +75,12 @@ constexpr int kMaxRounds = 64;  // path samples per chunk
 //   line 1 (hit record: written by the closest-hit kernel)
 //     128 hit_p, 144 hit_n, 160 sh_o, 176 sh_d, 192 psc, 208 rnd, 224 rng
 constexpr size_t kSlotBytes = 256;
+// GB_SHADOW_SPLIT: shadow rays (sh_o, sh_d) in their own 32-byte-per-slot
+// array instead of the hit line
+#ifndef GB_SHADOW_SPLIT
+#define GB_SHADOW_SPLIT 0
+#endif
+constexpr size_t kShadowStride = GB_SHADOW_SPLIT ? 32 : kSlotBytes;
 enum : size_t {
     kSlotRayO = 0, kSlotRayD = 16, kSlotTp = 32, kSlotAccum = 48, kSlotPix = 64, kSlotPs = 68, kSlotPb = 72,
     kSlotRdiff = 80, kSlotHitP = 128, kSlotHitN = 144, kSlotShO = 160, kSlotShD = 176, kSlotPsc = 192,
@@ -83,14 +89,14 @@ enum : size_t {
 static_assert(kSlotRdiff + 48 <= 128 && kSlotRng + 24 <= kSlotBytes, "slot record layout");
 
 // One field of the slot records: f[slot] is that field of record `slot`.
-template <class T>
+template <class T, size_t Stride = kSlotBytes>
 struct SlotField {
     unsigned char* base = nullptr;  // the field in record 0
 #ifdef __CUDACC__
     __host__ __device__
 #endif
     inline T& operator[](size_t slot) const {
-        return *reinterpret_cast<T*>(base + slot * kSlotBytes);
+        return *reinterpret_cast<T*>(base + slot * Stride);
     }
 };
 
@@ -106,8 +112,9 @@ struct Frame {
     SlotField<float4> ray_d;     // direction xyz
     SlotField<float4> tp;        // throughput
     SlotField<float4> accum;     // col_accum of the slot's path
-    SlotField<float4> sh_o;      // shadow origin xyz, max_t
-    SlotField<float4> sh_d;      // shadow direction xyz (to_light), w = occluded
+    SlotField<float4, kShadowStride> sh_o;  // shadow origin xyz, max_t
+    SlotField<float4, kShadowStride> sh_d;  // shadow direction xyz (to_light), w = occluded
+    unsigned char* shadow;       // the shadow-ray array (GB_SHADOW_SPLIT), else null
     SlotField<float4> psc;       // potential_sample_contribution
     SlotField<float4> rnd;       // path draw of this bounce
     SlotField<float4> hit_p;     // hit point xyz | material index bits
@@ -143,8 +150,9 @@ struct Frame {
     int grad_replicas;
 };
 
-// Points the slot fields of F at the records at `slots` (kSlotBytes-aligned).
-inline void bind_slots(Frame& F, unsigned char* slots) {
+// Points the slot fields of F at the records at `slots` (kSlotBytes-aligned)
+// and, with GB_SHADOW_SPLIT, the shadow rays at `shadow` (nslots * 32 bytes).
+inline void bind_slots(Frame& F, unsigned char* slots, unsigned char* shadow) {
     F.slots = slots;
     auto at = [slots](size_t off) { return slots ? slots + off : nullptr; };
     F.ray_o.base = at(kSlotRayO);
@@ -157,8 +165,9 @@ inline void bind_slots(Frame& F, unsigned char* slots) {
     for (int k = 0; k < 3; ++k) F.rdiff[k].base = at(kSlotRdiff + 16 * (size_t)k);
     F.hit_p.base = at(kSlotHitP);
     F.hit_n.base = at(kSlotHitN);
-    F.sh_o.base = at(kSlotShO);
-    F.sh_d.base = at(kSlotShD);
+    F.shadow = GB_SHADOW_SPLIT ? shadow : nullptr;
+    F.sh_o.base = GB_SHADOW_SPLIT ? shadow : at(kSlotShO);
+    F.sh_d.base = GB_SHADOW_SPLIT ? (shadow ? shadow + 16 : nullptr) : at(kSlotShD);
     F.psc.base = at(kSlotPsc);
     F.rnd.base = at(kSlotRnd);
     F.rng.base = at(kSlotRng);

@@ -52,12 +52,13 @@ constexpr size_t kStats = align_up(8 * 8);
 constexpr size_t kStatus = align_up(4);
 constexpr size_t kRec = align_up(sizeof(SceneRec));
 constexpr size_t kSlots = kSlotBytes * (size_t)kNoAllocMaxPixels;  // slot records
+constexpr size_t kShadow = GB_SHADOW_SPLIT ? 32 * (size_t)kNoAllocMaxPixels : 0;  // shadow rays
 // One slot per pixel and one path sample per pass: the slot records and
 // 4 queues; per pixel the image, the
 // initial RNG states, the two stream cursors, the scene word, one sample and
 // one jitter value; counters, path counter, iteration, stats, status and the
 // scene record.
-constexpr size_t kScratchBytes = kSlots + 4 * kU32 + kV4 + 3 * kRng + kU32 + 2 * kV4 + kCtr +
+constexpr size_t kScratchBytes = kSlots + kShadow + 4 * kU32 + kV4 + 3 * kRng + kU32 + 2 * kV4 + kCtr +
                                  kCtr + kCtr + kStats + kStatus + kRec;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -84,7 +85,7 @@ Frame carve(unsigned char* base, int n, SceneRec** rec) {
     F.nslots = n;
     F.nscenes = 1;
     size_t off = 0;
-    bind_slots(F, base + off); off += kSlots;
+    bind_slots(F, base + off, base + off + kSlots); off += kSlots + kShadow;
     for (int k = 0; k < 4; ++k) { F.q[k] = (uint32_t*)(base + off); off += kU32; }
     F.out = (float4*)(base + off); off += kV4;
     F.pristine = (MrgState*)(base + off); off += kRng;
