@@ -1688,6 +1688,23 @@ int gb_mrg_pool(gb_ctx* ctx, int npix, uint32_t seed, int first_update, int num_
     return GB_OK;
 }
 
+int gb_mrg_states(gb_ctx* ctx, uint32_t seed, const uint32_t* subsequences, int n, int method, uint32_t* out) {
+    if (!ctx || n <= 0 || !subsequences || !out || (method != 0 && method != 1))
+        return fail(ctx, GB_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    void* d = nullptr;
+    CK(cudaMalloc(&d, 7 * 4 * (size_t)n));
+    uint32_t* dsub = (uint32_t*)d;
+    uint32_t* dout = dsub + n;
+    cudaError_t e = cudaMemcpyAsync(dsub, subsequences, 4 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = k_launch_mrg_states(seed, dsub, n, method, dout, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, 6 * 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mrg states");
+    return GB_OK;
+}
+
 }  // extern "C"
 
 namespace gb {

@@ -254,36 +254,11 @@ static inline CameraRec make_camera(const gb_camera& c, int w, int h) {
     return r;
 }
 
-// A1^k and A2^k of the MRG32k3a recurrence (mrg_jump): square-and-multiply
-// of 3x3 matrices mod m.
-static inline void mrg_matmul(const uint32_t* A, const uint32_t* B, uint32_t* C, uint32_t c, uint32_t m) {
-    uint32_t r[9];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            uint64_t acc = 0;
-            for (int k = 0; k < 3; ++k) acc += mrg_reduce((uint64_t)A[3 * i + k] * B[3 * k + j], c, m);
-            r[3 * i + j] = mrg_reduce(acc, c, m);
-        }
-    std::memcpy(C, r, sizeof(r));
-}
-
-static inline void mrg_power(const uint32_t* A, uint64_t k, uint32_t* out, uint32_t c, uint32_t m) {
-    uint32_t base[9], acc[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    std::memcpy(base, A, sizeof(base));
-    while (k) {
-        if (k & 1) mrg_matmul(acc, base, acc, c, m);
-        mrg_matmul(base, base, base, c, m);
-        k >>= 1;
-    }
-    std::memcpy(out, acc, sizeof(acc));
-}
-
-// Jump matrices for `steps` MRG32k3a steps.
+// Jump matrices for `steps` MRG32k3a steps (mrg_power of the one-step
+// matrices, gbpt_math.h).
 static inline void mrg_jump_matrices(uint64_t steps, uint32_t J1[9], uint32_t J2[9]) {
-    const uint32_t A1[9] = {0, 1, 0, 0, 0, 1, kMrgM1 - 810728u, 1403580u, 0};
-    const uint32_t A2[9] = {0, 1, 0, 0, 0, 1, kMrgM2 - 1370589u, 0, 527612u};
-    mrg_power(A1, steps, J1, 209u, kMrgM1);
-    mrg_power(A2, steps, J2, 22853u, kMrgM2);
+    mrg_power(kMrgA1, steps, J1, 209u, kMrgM1);
+    mrg_power(kMrgA2, steps, J2, 22853u, kMrgM2);
 }
 
 static inline ShadeParams make_shade_params(const gb_render_desc& d) {

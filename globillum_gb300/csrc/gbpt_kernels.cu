@@ -426,15 +426,46 @@ __device__ __forceinline__ v3 draw3(MrgState* m) {
     return r;
 }
 
+// The state curand_init(seed, sub, 0) leaves: curand_init of subsequence 0
+// (no skip-ahead) advanced by sub * 2^76 steps with the table's jumps, one
+// 3x3 matrix product per component for each set bit of sub, in exact
+// integer arithmetic mod m1 / m2.
+__device__ __forceinline__ MrgState mrg_stream(const MrgSubseqTable& T, uint32_t seed, uint32_t sub) {
+    curandStateMRG32k3a s;
+    curand_init((unsigned long long)seed, 0ull, 0ull, &s);
+    MrgState m = mrg_pack(s);
+    for (int k = 0; sub != 0u; ++k, sub >>= 1)
+        if (sub & 1u) {
+            mrg_apply(m.s1, T.j1[k], 209u, kMrgM1);
+            mrg_apply(m.s2, T.j2[k], 22853u, kMrgM2);
+        }
+    return m;
+}
+
 // curand states right after curand_init(seed, pixel, 0) (util-kernels.cu:277-285)
 // for every pixel of every scene of the frame (pixel = index within its scene).
-__global__ void k_rng_init_frame(Frame F) {
+__global__ void k_rng_init_frame(Frame F, const MrgSubseqTable T) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= F.ntot) return;
     const SceneRec& R = F.scenes[F.pscene[g]];
-    curandStateMRG32k3a s;
-    curand_init((unsigned long long)R.seed, (unsigned long long)(g - (int)R.pixel_base), 0ull, &s);
-    st_mrg(F.pristine, (size_t)g, mrg_pack(s));
+    st_mrg(F.pristine, (size_t)g, mrg_stream(T, R.seed, (uint32_t)(g - (int)R.pixel_base)));
+}
+
+// States of curand_init(seed, sub[i], 0): method 0 by curand_init itself,
+// 1 by mrg_stream.
+__global__ void k_mrg_states(const MrgSubseqTable T, uint32_t seed, const uint32_t* sub, int n, int method,
+                             uint32_t* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    MrgState m;
+    if (method == 0) {
+        curandStateMRG32k3a s;
+        curand_init((unsigned long long)seed, (unsigned long long)sub[i], 0ull, &s);
+        m = mrg_pack(s);
+    } else {
+        m = mrg_stream(T, seed, sub[i]);
+    }
+    for (int k = 0; k < 3; ++k) { out[6 * i + k] = m.s1[k]; out[6 * i + 3 + k] = m.s2[k]; }
 }
 
 // Scene of every global pixel.
@@ -1136,7 +1167,7 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
 // camera ray's for the first sample, (0, 0, 0) afterwards.
 __global__ void __launch_bounds__(kBlock) k_direct(DevScene S, CameraRec cam, int w, int h, int samples,
                                                    uint32_t seed, float shadow_offset, v3 background, float* out,
-                                                   uint32_t* status) {
+                                                   uint32_t* status, const MrgSubseqTable T) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= w * h) return;
     v3 o, d;
@@ -1162,8 +1193,7 @@ __global__ void __launch_bounds__(kBlock) k_direct(DevScene S, CameraRec cam, in
             mcol = mcol * tex_sample_bilin_lod(S.tex[dtex], ts, tt, diff);
         }
     }
-    curandStateMRG32k3a st;
-    curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &st);
+    curandStateMRG32k3a st = mrg_expand(mrg_stream(T, seed, (uint32_t)g));
     v3 rnd = draw3(&st);
     v3 buf_dir = d;
     v3 acc = mk(0.0f, 0.0f, 0.0f);
@@ -1210,15 +1240,14 @@ __global__ void __launch_bounds__(kBlock) k_direct(DevScene S, CameraRec cam, in
 // so the jitter and light draws are one stream read twice.
 __global__ void __launch_bounds__(kBlock) k_direct_hybrid(DevScene S, CameraRec cam, int w, int h, int cam_samples,
                                                           int light_samples, uint32_t seed, float shadow_offset,
-                                                          v3 background, float* out, uint32_t* status) {
+                                                          v3 background, float* out, uint32_t* status,
+                                                          const MrgSubseqTable T) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= w * h) return;
     const int px = g % w, py = g / w;
-    curandStateMRG32k3a js, ls, lens;
-    curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &js);
-    curand_init((unsigned long long)seed, (unsigned long long)g, 0ull, &ls);
+    curandStateMRG32k3a js = mrg_expand(mrg_stream(T, seed, (uint32_t)g)), ls = js, lens;
     const bool aperture = cam.aperture != 0.0f;
-    if (aperture) curand_init((unsigned long long)seed, (unsigned long long)((g + 17) % (w * h)), 0ull, &lens);
+    if (aperture) lens = mrg_expand(mrg_stream(T, seed, (uint32_t)((g + 17) % (w * h))));
     const int L = light_samples;
     v3 acc = mk(0.0f, 0.0f, 0.0f);
     for (int c = 0; c < cam_samples; ++c) {
@@ -1460,9 +1489,19 @@ cudaError_t k_launch_trace(const DevScene& S, int n, const float* orig, const fl
     return cudaGetLastError();
 }
 
+// The subsequence jumps, computed once per process.
+const MrgSubseqTable& subseq_table() {
+    static const MrgSubseqTable T = [] {
+        MrgSubseqTable t;
+        mrg_subsequence_table(&t);
+        return t;
+    }();
+    return T;
+}
+
 cudaError_t k_launch_frame_init(const Frame& F, bool rng, cudaStream_t st) {
     k_fill_pscene<<<blocks_for(F.ntot), kBlock, 0, st>>>(F);
-    if (rng) k_rng_init_frame<<<blocks_for(F.ntot), kBlock, 0, st>>>(F);
+    if (rng) k_rng_init_frame<<<blocks_for(F.ntot), kBlock, 0, st>>>(F, subseq_table());
     return cudaGetLastError();
 }
 
@@ -1550,7 +1589,8 @@ cudaError_t k_launch_adjoint(const Frame& F, const RenderParams& P, cudaStream_t
 cudaError_t k_launch_direct(const DevScene& S, const CameraRec& cam, int w, int h, int samples, uint32_t seed,
                             float shadow_offset, v3 background, float* out, uint32_t* status, cudaStream_t st) {
     if (w * h <= 0) return cudaSuccess;
-    k_direct<<<blocks_for(w * h), kBlock, 0, st>>>(S, cam, w, h, samples, seed, shadow_offset, background, out, status);
+    k_direct<<<blocks_for(w * h), kBlock, 0, st>>>(S, cam, w, h, samples, seed, shadow_offset, background, out, status,
+                                                   subseq_table());
     return cudaGetLastError();
 }
 
@@ -1559,7 +1599,7 @@ cudaError_t k_launch_direct_hybrid(const DevScene& S, const CameraRec& cam, int 
                                    uint32_t* status, cudaStream_t st) {
     if (w * h <= 0) return cudaSuccess;
     k_direct_hybrid<<<blocks_for(w * h), kBlock, 0, st>>>(S, cam, w, h, cam_samples, light_samples, seed,
-                                                          shadow_offset, background, out, status);
+                                                          shadow_offset, background, out, status, subseq_table());
     return cudaGetLastError();
 }
 
@@ -1599,6 +1639,13 @@ cudaError_t k_launch_combine(const Frame& F, const RenderParams& P, cudaStream_t
 
 cudaError_t k_launch_pack_rgb(const float4* src, int n, float* dst, cudaStream_t st) {
     k_pack_rgb<<<blocks_for(n), kBlock, 0, st>>>(src, n, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_mrg_states(uint32_t seed, const uint32_t* sub, int n, int method, uint32_t* out,
+                                cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_mrg_states<<<blocks_for(n), kBlock, 0, st>>>(subseq_table(), seed, sub, n, method, out);
     return cudaGetLastError();
 }
 

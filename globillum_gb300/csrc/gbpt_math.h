@@ -235,6 +235,60 @@ GB_HD void mrg_apply(uint32_t s[3], const uint32_t* J, uint32_t c, uint32_t m) {
     s[0] = r[0]; s[1] = r[1]; s[2] = r[2];
 }
 
+// One step of the two component recurrences as 3x3 matrices on the state
+// vectors (L'Ecuyer 1999: x_n = (1403580 x_{n-2} - 810728 x_{n-3}) mod m1,
+// y_n = (527612 y_{n-1} - 1370589 y_{n-3}) mod m2), in the state order
+// s[0] oldest .. s[2] newest.
+constexpr uint32_t kMrgA1[9] = {0, 1, 0, 0, 0, 1, kMrgM1 - 810728u, 1403580u, 0};
+constexpr uint32_t kMrgA2[9] = {0, 1, 0, 0, 0, 1, kMrgM2 - 1370589u, 0, 527612u};
+
+// C = A B mod m (3x3); C may alias A or B.
+GB_HD void mrg_matmul(const uint32_t* A, const uint32_t* B, uint32_t* C, uint32_t c, uint32_t m) {
+    uint32_t r[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            uint64_t acc = 0;
+            for (int k = 0; k < 3; ++k) acc += mrg_reduce((uint64_t)A[3 * i + k] * B[3 * k + j], c, m);
+            r[3 * i + j] = mrg_reduce(acc, c, m);
+        }
+    for (int i = 0; i < 9; ++i) C[i] = r[i];
+}
+
+// out = A^k mod m by square-and-multiply.
+GB_HD void mrg_power(const uint32_t* A, uint64_t k, uint32_t* out, uint32_t c, uint32_t m) {
+    uint32_t base[9], acc[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int i = 0; i < 9; ++i) base[i] = A[i];
+    while (k) {
+        if (k & 1) mrg_matmul(acc, base, acc, c, m);
+        mrg_matmul(base, base, base, c, m);
+        k >>= 1;
+    }
+    for (int i = 0; i < 9; ++i) out[i] = acc[i];
+}
+
+// Jumps between the subsequences of curand_init(seed, subsequence, 0):
+// subsequence i starts i * 2^76 steps after subsequence 0 (cuRAND's
+// documented MRG32k3a subsequence spacing).  j1[k], j2[k] = A1^(2^(76+k)),
+// A2^(2^(76+k)), so subsequence i is reached by applying the matrices of
+// the set bits of i.
+struct MrgSubseqTable {
+    uint32_t j1[32][9], j2[32][9];
+};
+
+static inline void mrg_subsequence_table(MrgSubseqTable* T) {
+    uint32_t a1[9], a2[9];
+    for (int i = 0; i < 9; ++i) { a1[i] = kMrgA1[i]; a2[i] = kMrgA2[i]; }
+    for (int s = 0; s < 76; ++s) {  // A^(2^76)
+        mrg_matmul(a1, a1, a1, 209u, kMrgM1);
+        mrg_matmul(a2, a2, a2, 22853u, kMrgM2);
+    }
+    for (int k = 0; k < 32; ++k) {
+        for (int i = 0; i < 9; ++i) { T->j1[k][i] = a1[i]; T->j2[k][i] = a2[i]; }
+        mrg_matmul(a1, a1, a1, 209u, kMrgM1);
+        mrg_matmul(a2, a2, a2, 22853u, kMrgM2);
+    }
+}
+
 // Advances a state (s1, s2) by the steps J1 = A1^k, J2 = A2^k stand for.
 GB_HD void mrg_jump(uint32_t s1[3], uint32_t s2[3], const uint32_t* J1, const uint32_t* J2) {
     mrg_apply(s1, J1, 209u, kMrgM1);

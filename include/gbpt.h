@@ -407,6 +407,13 @@ int gb_compute_path_contribution_and_bounce(gb_ctx* ctx, gb_scene* scene, int w,
  * (util-kernels.cu:287-302) leaves in the pool at update first_update+u
  * (curand_init(seed, i, 0), 3 curand_uniform per update).  Host `out`. */
 int gb_mrg_pool(gb_ctx* ctx, int npix, uint32_t seed, int first_update, int num_updates, float* out);
+/* The MRG32k3a states curand_init(seed, subsequences[i], 0) leaves, as
+ * out[6 i .. 6 i + 5] = s1[0..2], s2[0..2].  method 0: curand_init itself
+ * (the reference's seeding call, util-kernels.cu:284); method 1: the
+ * library's own jump-ahead, which the frame, gpu_area_lights and
+ * hybrid_area_lights kernels use to start their pixel streams.  Host
+ * buffers. */
+int gb_mrg_states(gb_ctx* ctx, uint32_t seed, const uint32_t* subsequences, int n, int method, uint32_t* out);
 
 /* ------------------------------------------------------------- statistics */
 typedef struct {

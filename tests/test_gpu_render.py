@@ -115,6 +115,21 @@ def test_mrg_pool_streams(gpu_ctx):
     assert not np.array_equal(a[0, 0], a[0, 1])
 
 
+def test_mrg_stream_jump_matches_curand_init(gpu_ctx):
+    """The library's stream starts (subsequence i = i * 2^76 steps, by jump
+    matrices) equal curand_init(seed, i, 0): small indices, every single bit,
+    every all-ones prefix and random 32-bit indices, for several seeds."""
+    rng = np.random.default_rng(5)
+    sub = np.concatenate([np.arange(4096, dtype=np.uint64), np.uint64(1) << np.arange(32, dtype=np.uint64),
+                          (np.uint64(1) << np.arange(1, 33, dtype=np.uint64)) - np.uint64(1),
+                          rng.integers(0, 2**32, 20000, dtype=np.uint64)]).astype(np.uint32)
+    for seed in (0, 1, 0x9E3779B9):
+        a = gpu_ctx.mrg_states(sub, seed=seed, method=0)
+        b = gpu_ctx.mrg_states(sub, seed=seed, method=1)
+        assert np.array_equal(a, b), seed
+    assert not np.array_equal(a[0], a[1])
+
+
 def test_ingested_obj_scene_frame(gpu_ctx):
     """A scene gathered by gb_asset (OBJ + MTL + .pbrdf + light script),
     created straight from gb_asset_get_desc's description, renders the
