@@ -56,7 +56,7 @@ constexpr int kIterLimit = 1 << 22;
 #define GB_SPLIT_NEE 0
 #endif
 #ifndef GB_SHADE_MIN_BLOCKS
-#define GB_SHADE_MIN_BLOCKS 1
+#define GB_SHADE_MIN_BLOCKS 4  // resident k_shade blocks per SM (register budget 128)
 #endif
 #ifndef GB_STREAM_MIN_BLOCKS
 #define GB_STREAM_MIN_BLOCKS 1
@@ -414,10 +414,13 @@ __device__ __forceinline__ void st_mrg(MrgState* base, size_t i, const MrgState&
     q[1] = make_uint2(m.s1[2], m.s2[0]);
     q[2] = make_uint2(m.s2[1], m.s2[2]);
 }
-// the same for the stream of a slot record
+// the same for the stream of a slot record, stored as its whole 32-byte
+// sector (the state and 8 zero bytes)
 __device__ __forceinline__ MrgState ld_mrg(const SlotField<MrgState>& f, size_t slot) { return ld_mrg(&f[slot], 0); }
 __device__ __forceinline__ void st_mrg(const SlotField<MrgState>& f, size_t slot, const MrgState& m) {
-    st_mrg(&f[slot], 0, m);
+    uint4* q = reinterpret_cast<uint4*>(&f[slot]);
+    q[0] = make_uint4(m.s1[0], m.s1[1], m.s1[2], m.s2[0]);
+    q[1] = make_uint4(m.s2[1], m.s2[2], 0u, 0u);
 }
 __device__ __forceinline__ v3 draw3(MrgState* m) {
     curandStateMRG32k3a st = mrg_expand(*m);
@@ -554,14 +557,13 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
     v3 o, d;
     camera_ray(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w), j.x, j.y, lx, ly, &o, &d);
     F.ray_o[slot] = make_float4(o.x, o.y, o.z, FLT_MAX);
-    F.ray_d[slot] = make_float4(d.x, d.y, d.z, 0.0f);
+    F.ray_d[slot] = make_float4(d.x, d.y, d.z, __uint_as_float(((uint32_t)P.p0 + (uint32_t)lo) << 10));  // w: pb
     F.tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     if (P.mode == MODE_FROZEN) F.tp0[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     F.accum[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    F.pix[slot] = gpix;
-    F.ps[slot] = sc;
-    F.pb[slot] = ((uint32_t)P.p0 + (uint32_t)lo) << 10;
+    F.pixw[slot] = make_uint4(gpix, sc, 0u, 0u);
     if (R.S.texcoord) st_rdiff(F, slot, camera_diff(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w)));
+    else F.rdiff[0][slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // completes the sector of pix / ps
 }
 
 // Counter set of iteration `it`: [0] queue count, [1] extension head,
@@ -903,6 +905,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                 float4 tp4 = F.tp[slot];
                 float4 acc = F.accum[slot];
                 v3 add = miss_contribution(ld3(tp4), ld3(F.ray_d[slot]), R.sp, &R.S.sky);
+                F.tp[slot] = tp4;  // with accum, the whole sector
                 F.accum[slot] = make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f);
                 ended = true;
             } else {
@@ -1077,11 +1080,14 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
             cont = o.alive && bounce + 1 < R.L;
             ended = !cont;
             F.accum[slot] = acc;
-            F.pb[slot] = pbv + 1u;
+            const float pbw = __uint_as_float(pbv + 1u);  // ray_d.w
             if (cont) {
                 F.tp[slot] = make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f);
                 F.ray_o[slot] = make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX);
-                F.ray_d[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, 0.0f);
+                F.ray_d[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, pbw);
+            } else {
+                F.tp[slot] = tp4;
+                F.ray_d[slot] = make_float4(rd.x, rd.y, rd.z, pbw);
             }
         }
         push(cont, slot, qout, cn);

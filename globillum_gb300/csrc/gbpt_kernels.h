@@ -68,12 +68,15 @@ constexpr int kMaxRounds = 64;  // path samples per chunk
 // access of a slot is a scattered access.  A record keeps what one stage
 // reads or writes together in one 128-byte line, so that a stage touches a
 // few whole 32-byte sectors of a slot instead of one partly used sector per
-// field:
+// field, and the kernels write whole sectors (a partly written sector costs
+// DRAM a read-modify-write when it leaves the L2):
 //   line 0 (path state: written by path start and by shading)
-//     0 ray_o, 16 ray_d, 32 tp, 48 accum, 64 pix, 68 ps, 72 pb,
-//     80 rdiff[0..2] (ray differentials, textured scenes)
+//     0 ray_o, 16 ray_d (w: pb), 32 tp, 48 accum, 64 pix, 68 ps, 72 zero,
+//     80 rdiff[0..2] (ray differentials of textured scenes; rdiff[0] is
+//     zeroed at path start otherwise)
 //   line 1 (hit record: written by the closest-hit kernel)
-//     128 hit_p, 144 hit_n, 160 sh_o, 176 sh_d, 192 psc, 208 rnd, 224 rng
+//     128 hit_p, 144 hit_n, 160 sh_o, 176 sh_d, 192 psc, 208 rnd,
+//     224 rng (+ 8 zero bytes)
 constexpr size_t kSlotBytes = 256;
 // GB_SHADOW_SPLIT: shadow rays (sh_o, sh_d) in their own 32-byte-per-slot
 // array instead of the hit line
@@ -82,7 +85,7 @@ constexpr size_t kSlotBytes = 256;
 #endif
 constexpr size_t kShadowStride = GB_SHADOW_SPLIT ? 32 : kSlotBytes;
 enum : size_t {
-    kSlotRayO = 0, kSlotRayD = 16, kSlotTp = 32, kSlotAccum = 48, kSlotPix = 64, kSlotPs = 68, kSlotPb = 72,
+    kSlotRayO = 0, kSlotRayD = 16, kSlotPb = 28, kSlotTp = 32, kSlotAccum = 48, kSlotPix = 64, kSlotPs = 68,
     kSlotRdiff = 80, kSlotHitP = 128, kSlotHitN = 144, kSlotShO = 160, kSlotShD = 176, kSlotPsc = 192,
     kSlotRnd = 208, kSlotRng = 224
 };
@@ -123,7 +126,8 @@ struct Frame {
     SlotField<MrgState> rng;     // light/path stream of the slot's path
     SlotField<uint32_t> pix;     // global pixel of the slot's path
     SlotField<uint32_t> ps;      // scene of the slot's path
-    SlotField<uint32_t> pb;      // path index << 10 | bounce
+    SlotField<uint32_t> pb;      // path index << 10 | bounce (the bits of ray_d.w)
+    SlotField<uint4> pixw;       // (pix, ps, 0, 0) as one 16-byte word
     uint32_t* q[4];    // queues: extension (ping/pong), shadow, ended paths; nslots entries each
     // per global pixel
     float4* out;       // output_color (moving average)
@@ -162,6 +166,7 @@ inline void bind_slots(Frame& F, unsigned char* slots, unsigned char* shadow) {
     F.pix.base = at(kSlotPix);
     F.ps.base = at(kSlotPs);
     F.pb.base = at(kSlotPb);
+    F.pixw.base = at(kSlotPix);
     for (int k = 0; k < 3; ++k) F.rdiff[k].base = at(kSlotRdiff + 16 * (size_t)k);
     F.hit_p.base = at(kSlotHitP);
     F.hit_n.base = at(kSlotHitN);
