@@ -56,7 +56,7 @@ constexpr int kIterLimit = 1 << 22;
 #define GB_SPLIT_NEE 0
 #endif
 #ifndef GB_SHADE_MIN_BLOCKS
-#define GB_SHADE_MIN_BLOCKS 4  // resident k_shade blocks per SM (register budget 128)
+#define GB_SHADE_MIN_BLOCKS 5  // resident k_shade blocks per SM (register budget 102)
 #endif
 #ifndef GB_STREAM_MIN_BLOCKS
 #define GB_STREAM_MIN_BLOCKS 1
