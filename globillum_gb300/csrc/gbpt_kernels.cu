@@ -843,7 +843,13 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
 // The light sample of a hit (generate_arealight_sample,
 // arealight-sampler-cpu.cpp:25-143) on the path's light draw: shadow ray,
 // potential_sample_contribution and the path draw of this bounce.
-__device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, uint32_t slot, v3 Pp, v3 Nr) {
+// skip_dark: a sample whose potential contribution is exactly zero (the
+// surface or the light faces away) gets no shadow ray (max_t = -1, read as
+// occluded).  Its visibility cannot change the path: shading adds
+// bl * (tp * psc) = +-0 when unoccluded (or nothing, when that is NaN), and
+// the accumulation is never -0, so the sum is the same bits either way.
+__device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, uint32_t slot, v3 Pp, v3 Nr,
+                                           bool skip_dark) {
     const DevScene& S = R.S;
     MrgState st = ld_mrg(F.rng, slot);
     v3 rnd = draw3(&st);
@@ -866,6 +872,7 @@ __device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, ui
             rect_light_sample(L, S.lights_eval[l].col, S.overall_power, Pp, Nr, lr.x, lr.y, R.sp.shadow_offset,
                               &so, &sd, &smax, &psc, &scale);
     }
+    if (skip_dark && psc.x == 0.0f && psc.y == 0.0f && psc.z == 0.0f) smax = -1.0f;
     F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
     F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
     F.psc[slot] = make_float4(psc.x, psc.y, psc.z, scale);
@@ -915,7 +922,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                 float4 na = __ldg(sh + 3), nb = __ldg(sh + 4), nc = __ldg(sh + 5);
                 v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
                 v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
-                if (!GB_SPLIT_NEE) nee_at_hit(F, R, slot, Pp, Nr);
+                if (!GB_SPLIT_NEE) nee_at_hit(F, R, slot, Pp, Nr, P.mode != MODE_ADJOINT);
                 F.hit_p[slot] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
                 F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id));
             }
@@ -929,14 +936,14 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
 
 // Light samples of every hit of the iteration (shadow queue), when they are
 // not taken inside k_extend (GB_SPLIT_NEE).
-__global__ void __launch_bounds__(kBlock) k_nee(Frame F) {
+__global__ void __launch_bounds__(kBlock) k_nee(Frame F, int mode) {
     const uint32_t* cs = ctr_set(F, *F.iter);
     const uint32_t count = cs[2];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
         const uint32_t slot = F.q[2][i];
         const SceneRec& R = F.scenes[F.ps[slot]];
-        nee_at_hit(F, R, slot, ld3(F.hit_p[slot]), ld3(F.hit_n[slot]));
+        nee_at_hit(F, R, slot, ld3(F.hit_p[slot]), ld3(F.hit_n[slot]), mode != MODE_ADJOINT);
     }
 }
 
@@ -947,7 +954,6 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
     uint32_t* cs = ctr_set(F, it);
     const uint32_t count = cs[2];
     const uint32_t* qsh = F.q[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&F.stats[2], (unsigned long long)count);
     uint32_t nvis = 0, ntri = 0;
     auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
                      const float4** shade) {
@@ -958,7 +964,9 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
         *tris = R.S.tris;
         *shade = R.S.shade;
         *o = ld3(so); *d = ld3(sd); *tmax = so.w;
-        return so.w >= 0.0f;
+        const bool traced = so.w >= 0.0f;
+        if (traced) add_stats_lane(&F.stats[2]);  // shadow rays traced
+        return traced;
     };
     auto finish = [&](bool fin, uint32_t q, const Trav& h) {
         if (fin) {
@@ -1522,7 +1530,7 @@ void launch_extend_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
     k_extend<INSTR, MODE><<<traversal_grid(g, P.blocks_per_sm), kBlock, 0, st>>>(F, P);
     if (GB_SPLIT_NEE) {
         static int gn = persistent_blocks(k_nee);
-        k_nee<<<gn, kBlock, 0, st>>>(F);
+        k_nee<<<gn, kBlock, 0, st>>>(F, P.mode);
     }
 }
 
