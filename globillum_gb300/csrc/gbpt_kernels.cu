@@ -572,8 +572,15 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
 // are the same every time (graph-capturable).
 __device__ __forceinline__ uint32_t* ctr_set(const Frame& F, int it) { return F.ctr + 8 * (it % 3); }
 
-// Slots whose path ended go to the free queue; k_regen stores their
-// samples and starts the next paths.
+// The sample of a path that ended (new_path's input to the moving average):
+// path p's colour at sample index round_start[p - p0] + pixel.
+__device__ __forceinline__ void store_sample(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t pbv,
+                                             float4 acc) {
+    F.samples[P.round_start[(pbv >> 10) - (uint32_t)P.p0] + F.pix[slot]] = acc;
+}
+
+// Slots whose path ended go to the free queue; k_regen starts the next
+// paths on them.
 __device__ __forceinline__ void end_paths(const Frame& F, bool ended, uint32_t slot, uint32_t* cn) {
     push(ended, slot, F.q[3], cn + 4);
 }
@@ -591,15 +598,13 @@ __global__ void __launch_bounds__(kBlock, GB_STREAM_MIN_BLOCKS) k_regen(Frame F,
     uint32_t* qout = F.q[(it + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
     // free-queue entry qi takes path l0 + qi and next-queue entry next0 + qi:
-    // no counter round trip; k_step advances both counters afterwards
-    for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < count; qi += stride) {
+    // no counter round trip; k_step advances both counters afterwards.  The
+    // ended paths' samples were stored where they ended (store_sample).
+    const uint32_t nstart = min(count, avail);
+    for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nstart; qi += stride) {
         const uint32_t slot = F.q[3][qi];
-        const uint32_t p = F.pb[slot] >> 10;
-        F.samples[P.round_start[p - (uint32_t)P.p0] + F.pix[slot]] = F.accum[slot];
-        if (qi < avail) {
-            start_path(F, P, slot, l0 + qi);
-            qout[next0 + qi] = slot;
-        }
+        start_path(F, P, slot, l0 + qi);
+        qout[next0 + qi] = slot;
     }
 }
 
@@ -912,8 +917,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                 float4 tp4 = F.tp[slot];
                 float4 acc = F.accum[slot];
                 v3 add = miss_contribution(ld3(tp4), ld3(F.ray_d[slot]), R.sp, &R.S.sky);
-                F.tp[slot] = tp4;  // with accum, the whole sector
-                F.accum[slot] = make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f);
+                store_sample(F, P, slot, pbv, make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f));
                 ended = true;
             } else {
                 const DevScene& S = R.S;
@@ -1087,15 +1091,15 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
             acc = make_float4(acc.x + o.accum_add.x, acc.y + o.accum_add.y, acc.z + o.accum_add.z, 0.0f);
             cont = o.alive && bounce + 1 < R.L;
             ended = !cont;
-            F.accum[slot] = acc;
             const float pbw = __uint_as_float(pbv + 1u);  // ray_d.w
             if (cont) {
                 F.tp[slot] = make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f);
+                F.accum[slot] = acc;
                 F.ray_o[slot] = make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX);
                 F.ray_d[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, pbw);
             } else {
-                F.tp[slot] = tp4;
-                F.ray_d[slot] = make_float4(rd.x, rd.y, rd.z, pbw);
+                store_sample(F, P, slot, pbv, acc);
+                if (MODE == MODE_ADJOINT) F.ray_d[slot] = make_float4(rd.x, rd.y, rd.z, pbw);  // bounces for k_adjoint
             }
         }
         push(cont, slot, qout, cn);
