@@ -61,6 +61,9 @@ constexpr int kIterLimit = 1 << 22;
 #ifndef GB_STREAM_MIN_BLOCKS
 #define GB_STREAM_MIN_BLOCKS 1
 #endif
+#ifndef GB_FUSED_RESTART
+#define GB_FUSED_RESTART 1  // paths ended by a miss restart in k_shadow's warps
+#endif
 #ifndef GB_WIDE_STREAM_GRIDS
 #define GB_WIDE_STREAM_GRIDS 1
 #endif
@@ -591,20 +594,59 @@ __device__ __forceinline__ void end_paths(const Frame& F, bool ended, uint32_t s
 __global__ void __launch_bounds__(kBlock, GB_STREAM_MIN_BLOCKS) k_regen(Frame F, RenderParams P) {
     const int it = *F.iter;
     const uint32_t* cn = ctr_set(F, it + 1);
-    const uint32_t count = cn[4];   // ended paths of this iteration (free queue)
+    // free-queue entries before cn[5] were restarted by k_shadow (cn[7]
+    // paths started); the rest are the paths k_shade ended (all of them
+    // when k_shadow restarted none)
+    const uint32_t first = cn[5];
+    const uint32_t count = cn[4] - first;
     const uint32_t next0 = cn[0];   // paths already queued for the next iteration
-    const uint32_t l0 = *F.path_ctr;
+    const uint32_t l0 = *F.path_ctr + cn[7];
     const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
     uint32_t* qout = F.q[(it + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
-    // free-queue entry qi takes path l0 + qi and next-queue entry next0 + qi:
-    // no counter round trip; k_step advances both counters afterwards.  The
-    // ended paths' samples were stored where they ended (store_sample).
+    // free-queue entry first + qi takes path l0 + qi and next-queue entry
+    // next0 + qi: no counter round trip; k_step advances both counters
+    // afterwards.  The ended paths' samples were stored where they ended
+    // (store_sample).
     const uint32_t nstart = min(count, avail);
     for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nstart; qi += stride) {
-        const uint32_t slot = F.q[3][qi];
+        const uint32_t slot = F.q[3][first + qi];
         start_path(F, P, slot, l0 + qi);
         qout[next0 + qi] = slot;
+    }
+}
+
+// Restart of the paths k_extend ended (misses), run by the warps of
+// k_shadow once the shadow queue has no rays left for them, so that it
+// fills the tail of the any-hit launch.  Free-queue entry qi < nA takes
+// path l0 + qi and next-queue entry qi; k_shade appends the continuing
+// paths after them, k_regen restarts the paths k_shade ends.  Not in the
+// adjoint mode, whose sweep reads the ended paths' records first.
+__device__ __forceinline__ void restart_misses(const Frame& F, const RenderParams& P) {
+    const int it = *F.iter;
+    uint32_t* cn = ctr_set(F, it + 1);
+    const uint32_t count = cn[4];  // misses of k_extend (k_shade has not run)
+    const uint32_t l0 = *F.path_ctr;
+    const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
+    const uint32_t nA = min(count, avail);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cn[0] = nA;     // next-queue entries taken (k_shade appends after them)
+        cn[5] = count;  // free-queue entries consumed
+        cn[7] = nA;     // paths started
+    }
+    uint32_t* qout = F.q[(it + 1) & 1];
+    const uint32_t lane = lane_id();
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0u) base = atomicAdd(&cn[6], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= nA) break;
+        const uint32_t qi = base + lane;
+        if (qi < nA) {
+            const uint32_t slot = F.q[3][qi];
+            start_path(F, P, slot, l0 + qi);
+            qout[qi] = slot;
+        }
     }
 }
 
@@ -630,7 +672,7 @@ __global__ void k_step(Frame F, RenderParams P, unsigned long long cond, int has
     const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
     const uint32_t started = min(cn[4], avail);
     *F.path_ctr = l0 + started;
-    cn[0] += started;
+    cn[0] += started - cn[7];  // k_shadow's restarts (cn[7]) are counted already
     F.stats[0] += (unsigned long long)started;
     uint32_t* c2 = ctr_set(F, it + 2);
     for (int k = 0; k < 8; ++k) c2[k] = 0u;
@@ -982,6 +1024,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
     };
     ray_loop<true, INSTR, MODE>(count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
+    if (GB_FUSED_RESTART && P.mode != MODE_ADJOINT) restart_misses(F, P);
 }
 
 // Material record of index mi; the texture fields (last float4) only when
