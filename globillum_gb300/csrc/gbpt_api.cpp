@@ -1046,9 +1046,9 @@ int finish_frame(gb_ctx* ctx) {
     ctx->stats.closest_tri_tests = st[4];
     ctx->stats.shadow_node_visits = st[5];
     ctx->stats.shadow_tri_tests = st[6];
-    // every slot-pool iteration (counted by k_step in st[7]) is 5 launches,
-    // 6 with the adjoint sweep
-    ctx->stats.kernel_launches = ctx->launches + (ctx->mode == MODE_ADJOINT ? 6 : 5) * st[7];
+    // every slot-pool iteration (counted by k_step in st[7]) is 4 launches
+    // (extend, shadow, shade, step), 6 with the adjoint sweep
+    ctx->stats.kernel_launches = ctx->launches + (uint64_t)k_launches_per_iteration(ctx->mode) * st[7];
     ctx->stats.paths_done = ctx->paths_done;
     for (int k = 0; k < 6; ++k) { ctx->stats.stage_ms[k] = 0.0; ctx->stats.stage_launches[k] = 0; }
     for (size_t i = 0; i < ctx->ev_used; ++i) {

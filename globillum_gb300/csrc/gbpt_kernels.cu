@@ -347,6 +347,18 @@ __device__ __forceinline__ void push(bool pred, uint32_t id, uint32_t* q, uint32
     if (pred) q[base + (uint32_t)__popc(mask & ((1u << lane_id()) - 1u))] = id;
 }
 
+// Warp-aggregated counter increment: the lane's index among the warp's
+// increments, counted from the counter's value (0 where pred is false).
+__device__ __forceinline__ uint32_t warp_inc(bool pred, uint32_t* c) {
+    uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0u) return 0u;
+    uint32_t leader = (uint32_t)__ffs(mask) - 1u;
+    uint32_t base = 0u;
+    if (lane_id() == leader) base = atomicAdd(c, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, (int)leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane_id()) - 1u));
+}
+
 __device__ __forceinline__ void add_stats(unsigned long long* s, uint32_t v) {
     uint32_t w = __reduce_add_sync(0xffffffffu, v);
     if (lane_id() == 0u && w) atomicAdd(s, (unsigned long long)w);
@@ -670,9 +682,12 @@ __global__ void k_step(Frame F, RenderParams P, unsigned long long cond, int has
     uint32_t* cn = ctr_set(F, it + 1);
     const uint32_t l0 = *F.path_ctr;
     const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
-    const uint32_t started = min(cn[4], avail);
+    // restarts in k_shadow and k_shade (cn[7] attempts, already queued), or
+    // in k_regen (the free queue, queued at cn[0] + qi)
+    const bool fused = GB_FUSED_RESTART && P.mode != MODE_ADJOINT;
+    const uint32_t started = fused ? min(cn[7], avail) : min(cn[4], avail);
     *F.path_ctr = l0 + started;
-    cn[0] += started - cn[7];  // k_shadow's restarts (cn[7]) are counted already
+    if (!fused) cn[0] += started;
     F.stats[0] += (unsigned long long)started;
     uint32_t* c2 = ctr_set(F, it + 2);
     for (int k = 0; k < 8; ++k) c2[k] = 0u;
@@ -1087,6 +1102,8 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
     const uint32_t* qsh = F.q[2];
     uint32_t* qout = F.q[(it + 1) & 1];
     const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t l0 = *F.path_ctr;
+    const uint32_t avail = l0 < P.chunk_paths ? P.chunk_paths - l0 : 0u;
     for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < count; i0 += stride) {
         uint32_t qi = i0 + lane_id();
         bool valid = qi < count;
@@ -1145,8 +1162,17 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
                 if (MODE == MODE_ADJOINT) F.ray_d[slot] = make_float4(rd.x, rd.y, rd.z, pbw);  // bounces for k_adjoint
             }
         }
-        push(cont, slot, qout, cn);
-        end_paths(F, ended, slot, cn);
+        if (GB_FUSED_RESTART && MODE != MODE_ADJOINT) {
+            // a path that shading ends restarts on its slot at once: path
+            // l0 + j, j counted on from k_shadow's restarts (cn[7])
+            const uint32_t j = warp_inc(ended, &cn[7]);
+            const bool restart = ended && j < avail;
+            if (restart) start_path(F, P, slot, l0 + j);
+            push(cont || restart, slot, qout, cn);
+        } else {
+            push(cont, slot, qout, cn);
+            end_paths(F, ended, slot, cn);
+        }
     }
 }
 
@@ -1676,7 +1702,13 @@ cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, do
     return cudaGetLastError();
 }
 
+int k_launches_per_iteration(int mode) {
+    if (mode == MODE_ADJOINT) return 6;   // extend, shadow, shade, adjoint, regen, step
+    return GB_FUSED_RESTART ? 4 : 5;      // restarts inside shadow and shade
+}
+
 cudaError_t k_launch_regen(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    if (GB_FUSED_RESTART && P.mode != MODE_ADJOINT) return cudaSuccess;  // restarted in k_shadow / k_shade
     static int g0 = persistent_blocks(k_regen);
     k_regen<<<stream_grid(g0, F.nslots), kBlock, 0, st>>>(F, P);
     return cudaGetLastError();
