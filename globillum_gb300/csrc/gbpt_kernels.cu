@@ -109,6 +109,36 @@ __device__ __forceinline__ RayInv make_ray(v3 o, v3 d) {
     return r;
 }
 
+// Read-only 16-byte loads of the tree with cache hints: triangles without L1
+// allocation (GB_TRI_NOALLOC), nodes with a 128-byte L2 fetch (GB_NODE_L2_128);
+// plain __ldg otherwise.
+#ifndef GB_TRI_NOALLOC
+#define GB_TRI_NOALLOC 0
+#endif
+#ifndef GB_NODE_L2_128
+#define GB_NODE_L2_128 0
+#endif
+__device__ __forceinline__ float4 ld_tri(const float4* p) {
+#if GB_TRI_NOALLOC
+    float4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(__cvta_generic_to_global(p)));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+__device__ __forceinline__ float4 ld_node(const float4* p) {
+#if GB_NODE_L2_128
+    float4 v;
+    asm("ld.global.nc.L2::128B.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(__cvta_generic_to_global(p)));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+
 // Packed FP32 (two lanes per 64-bit register) and 3-input min/max of sm_100+.
 __device__ __forceinline__ uint64_t pack2(float a, float b) {
     uint64_t r;
@@ -164,7 +194,7 @@ __device__ __forceinline__ uint32_t xor_permute8(uint32_t m, uint32_t x) {
 __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes, uint32_t ni, const RayInv& r,
                                                float bound, uint2* ng, uint2* tg) {
     const float4* n = nodes + 5 * (size_t)ni;
-    float4 n0 = __ldg(n + 0), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3), n4 = __ldg(n + 4);
+    float4 n0 = ld_node(n + 0), n1 = ld_node(n + 1), n2 = ld_node(n + 2), n3 = ld_node(n + 3), n4 = ld_node(n + 4);
     uint32_t ew = __float_as_uint(n0.w);
     float sx = __uint_as_float((ew & 0xffu) << 23);
     float sy = __uint_as_float(((ew >> 8) & 0xffu) << 23);
@@ -262,7 +292,7 @@ __device__ __forceinline__ bool tri_step(const float4* __restrict__ tris, const 
     int b = __ffs(s.tg.y) - 1;
     s.tg.y &= s.tg.y - 1u;
     const float4* tp = tris + 3 * (size_t)(s.tg.x + (uint32_t)b);
-    float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
+    float4 a0 = ld_tri(tp + 0), a1 = ld_tri(tp + 1), a2 = ld_tri(tp + 2);
     if (INSTR) ++*ntri;
     float t, u, v;
     if (intersect_tri(r.o, r.d, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= tmax) {
@@ -752,7 +782,7 @@ __device__ __forceinline__ bool coop_triangles(bool act, const float4* tris, con
             const uint32_t bit = __fns(om, 0u, (int)(g - oe) + 1);
             if (bit < 32u && ((om >> bit) & 1u)) {
                 const float4* tp = otris + 3 * (size_t)(ob + bit);
-                float4 a0 = __ldg(tp + 0), a1 = __ldg(tp + 1), a2 = __ldg(tp + 2);
+                float4 a0 = ld_tri(tp + 0), a1 = ld_tri(tp + 1), a2 = ld_tri(tp + 2);
                 if (INSTR) ++*ntri;
                 float t, u, v;
                 if (intersect_tri(ro, rd, ld3(a0), ld3(a1), ld3(a2), &t, &u, &v) && t <= otmax)
