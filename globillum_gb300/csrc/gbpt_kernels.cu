@@ -112,6 +112,9 @@ __device__ __forceinline__ RayInv make_ray(v3 o, v3 d) {
 // Read-only 16-byte loads of the tree with cache hints: triangles without L1
 // allocation (GB_TRI_NOALLOC), nodes with a 128-byte L2 fetch (GB_NODE_L2_128);
 // plain __ldg otherwise.
+#ifndef GB_SHADOW_REFILL
+#define GB_SHADOW_REFILL 12  // refill threshold of the any-hit kernel (0: the frame's refill)
+#endif
 #ifndef GB_TRI_NOALLOC
 #define GB_TRI_NOALLOC 0
 #endif
@@ -1067,7 +1070,8 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
             reinterpret_cast<float*>(&F.sh_d[slot])[3] = occl ? 1.0f : 0.0f;
         }
     };
-    ray_loop<true, INSTR, MODE>(count, cs + 3, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    ray_loop<true, INSTR, MODE>(count, cs + 3, GB_SHADOW_REFILL > 0 ? GB_SHADOW_REFILL : P.refill, F.status, fetch,
+                                finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
     if (GB_FUSED_RESTART && P.mode != MODE_ADJOINT) restart_misses(F, P);
 }
