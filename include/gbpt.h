@@ -432,7 +432,8 @@ typedef struct {
 } gb_stats;
 
 /* Knobs of the wavefront (chosen by the autotuner); 0 keeps a value:
- *   refill    idle lanes (1..32) at which a traversal warp fetches new rays
+ *   refill    idle lanes (1..32) at which a closest-hit traversal warp
+ *             fetches new rays (any-hit warps refill at 12)
  *   slots     paths in flight (queue capacity), default 2^20
  *   sample_mb budget of the per-path sample buffer, which bounds how many
  *             path samples per pixel one pass of the slot pool covers */
