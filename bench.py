@@ -585,7 +585,8 @@ def run_gbpt(args, rank, world):
                                   "shadow_node_visits": ist["shadow_node_visits"] / max(1, ist["shadow_rays"]),
                                   "shadow_tri_tests": ist["shadow_tri_tests"] / max(1, ist["shadow_rays"])},
             "stage_ms_per_frame": {"path_start": stage_ms[0], "closest_hit+light_sample": ext_ms,
-                                   "any_hit": stage_ms[2], "shade": stage_ms[3], "path_end+restart": stage_ms[4],
+                                   "any_hit+restart_of_misses": stage_ms[2], "shade+restart": stage_ms[3],
+                                   "iteration_end": stage_ms[4],
                                    "moving_average": stage_ms[5], "frame_ms_with_stage_events": stage_frame_ms},
             "stage_launches_per_frame": [int(x) for x in stage_n],
             "roofline": {"bound": "hbm", "kernel": "k_extend (closest-hit traversal + light sample)",
