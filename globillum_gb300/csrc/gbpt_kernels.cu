@@ -614,6 +614,12 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
     else F.rdiff[0][slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // completes the sector of pix / ps
 }
 
+// The scene record of a slot's path; a frame of one scene needs no load of
+// the slot's scene word.
+__device__ __forceinline__ const SceneRec& scene_of(const Frame& F, uint32_t slot) {
+    return F.scenes[F.nscenes == 1 ? 0u : F.ps[slot]];
+}
+
 // Counter set of iteration `it`: [0] queue count, [1] extension head,
 // [2] shadow count, [3] shadow head, [4] ended paths (free queue count).
 // The iteration index lives in F.iter (device), so an iteration's launches
@@ -987,7 +993,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                      const float4** shade) {
         uint32_t slot = qin[q];
         float4 ro = F.ray_o[slot], rd = F.ray_d[slot];
-        const SceneRec& R = F.scenes[F.ps[slot]];
+        const SceneRec& R = scene_of(F, slot);
         *nodes = R.S.nodes;
         *tris = R.S.tris;
         *shade = R.S.shade;
@@ -1000,7 +1006,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
         if (fin) {
             slot = qin[q];
             hit = h.best_id != 0xffffffffu;
-            const SceneRec& R = F.scenes[F.ps[slot]];
+            const SceneRec& R = scene_of(F, slot);
             uint32_t pbv = F.pb[slot];
             if ((pbv & 1023u) > 0u) add_stats_lane(&F.stats[1]);
             if (!hit) {
@@ -1036,7 +1042,7 @@ __global__ void __launch_bounds__(kBlock) k_nee(Frame F, int mode) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
         const uint32_t slot = F.q[2][i];
-        const SceneRec& R = F.scenes[F.ps[slot]];
+        const SceneRec& R = scene_of(F, slot);
         nee_at_hit(F, R, slot, ld3(F.hit_p[slot]), ld3(F.hit_n[slot]), mode != MODE_ADJOINT);
     }
 }
@@ -1053,7 +1059,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, 
                      const float4** shade) {
         uint32_t slot = qsh[q];
         float4 so = F.sh_o[slot], sd = F.sh_d[slot];
-        const SceneRec& R = F.scenes[F.ps[slot]];
+        const SceneRec& R = scene_of(F, slot);
         *nodes = R.S.nodes;
         *tris = R.S.tris;
         *shade = R.S.shade;
@@ -1145,7 +1151,7 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
         bool cont = false, ended = false;
         if (valid) {
             slot = qsh[qi];
-            const SceneRec& R = F.scenes[F.ps[slot]];
+            const SceneRec& R = scene_of(F, slot);
             float4 sd = F.sh_d[slot];
             float4 hp = F.hit_p[slot], hn = F.hit_n[slot];
             uint32_t mi = __float_as_uint(hp.w);
@@ -1228,7 +1234,7 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
         const int K = (int)(F.pb[slot] & 1023u);
         const float4 g4 = F.dimg[F.pix[slot]];
         if (K == 0 || (g4.x == 0.0f && g4.y == 0.0f && g4.z == 0.0f)) continue;
-        const SceneRec& R = F.scenes[F.ps[slot]];
+        const SceneRec& R = scene_of(F, slot);
         const v3 g = ld3(g4);
         float* gm_base = grad + R.grad_base;
         float* gl_base = gm_base + (size_t)kMatGradFloats * (size_t)R.n_mats;
