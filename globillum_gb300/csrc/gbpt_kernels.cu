@@ -587,7 +587,7 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
         else hi = mid - 1;
     }
     const uint32_t gpix = l - P.round_start[lo];
-    const uint32_t sc = F.pscene[gpix];
+    const uint32_t sc = F.nscenes == 1 ? 0u : F.pscene[gpix];
     const SceneRec& R = F.scenes[sc];
     const uint32_t lp = gpix - R.pixel_base;
     const float4* jp = F.jpool + P.round_start[lo];
