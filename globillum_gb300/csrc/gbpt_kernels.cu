@@ -112,6 +112,9 @@ __device__ __forceinline__ RayInv make_ray(v3 o, v3 d) {
 // Read-only 16-byte loads of the tree with cache hints: triangles without L1
 // allocation (GB_TRI_NOALLOC), nodes with a 128-byte L2 fetch (GB_NODE_L2_128);
 // plain __ldg otherwise.
+#ifndef GB_SHADOW_MIN_BLOCKS
+#define GB_SHADOW_MIN_BLOCKS GB_TRAV_MIN_BLOCKS  // resident any-hit blocks per SM (register budget)
+#endif
 #ifndef GB_SHADOW_REFILL
 #define GB_SHADOW_REFILL 12  // refill threshold of the any-hit kernel (0: the frame's refill)
 #endif
@@ -1049,7 +1052,7 @@ __global__ void __launch_bounds__(kBlock) k_nee(Frame F, int mode) {
 
 // Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
 template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_shadow(Frame F, RenderParams P) {
+__global__ void __launch_bounds__(kBlock, GB_SHADOW_MIN_BLOCKS) k_shadow(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     const uint32_t count = cs[2];
