@@ -65,7 +65,7 @@ constexpr int kIterLimit = 1 << 22;
 #define GB_FUSED_RESTART 1  // paths ended by a miss restart in k_shadow's warps
 #endif
 #ifndef GB_WIDE_STREAM_GRIDS
-#define GB_WIDE_STREAM_GRIDS 1
+#define GB_WIDE_STREAM_GRIDS 0
 #endif
 constexpr int kSmemStack = GB_SMEM_STACK;
 
@@ -1684,8 +1684,8 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
     return cudaGetLastError();
 }
 
-// Grid of the streaming per-path kernels: one thread per slot
-// (GB_WIDE_STREAM_GRIDS, the default), or persistent.
+// Grid of the streaming per-path kernels: persistent (the default), or one
+// thread per slot (GB_WIDE_STREAM_GRIDS).
 inline int stream_grid(int persistent, int nslots) {
     return GB_WIDE_STREAM_GRIDS ? std::max(1, blocks_for(nslots)) : persistent;
 }
