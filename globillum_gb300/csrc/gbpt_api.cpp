@@ -1674,13 +1674,18 @@ int gb_compute_path_contribution_and_bounce(gb_ctx* ctx, gb_scene* scene, int w,
 }
 
 int gb_mrg_pool(gb_ctx* ctx, int npix, uint32_t seed, int first_update, int num_updates, float* out) {
-    if (!ctx || npix <= 0 || first_update < 0 || num_updates <= 0 || !out)
+    return gb_mrg_pool_range(ctx, 0, npix, seed, first_update, num_updates, out);
+}
+
+int gb_mrg_pool_range(gb_ctx* ctx, int pixel0, int npix, uint32_t seed, int first_update, int num_updates,
+                      float* out) {
+    if (!ctx || pixel0 < 0 || npix <= 0 || npix > INT32_MAX - pixel0 || first_update < 0 || num_updates <= 0 || !out)
         return fail(ctx, GB_ERR_INVALID, "bad arguments");
     CK(cudaSetDevice(ctx->device));
     size_t bytes = sizeof(float) * 3 * (size_t)npix * (size_t)num_updates;
     void* d = nullptr;
     CK(cudaMalloc(&d, bytes));
-    cudaError_t e = k_launch_mrg_pool(npix, seed, first_update, num_updates, (float*)d, ctx->stream);
+    cudaError_t e = k_launch_mrg_pool(pixel0, npix, seed, first_update, num_updates, (float*)d, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     cudaFree(d);

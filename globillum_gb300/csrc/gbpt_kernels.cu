@@ -1483,11 +1483,11 @@ __global__ void k_pack_rgb(const float4* __restrict__ src, int n, float* dst) {
     dst[3 * i] = v.x; dst[3 * i + 1] = v.y; dst[3 * i + 2] = v.z;
 }
 
-__global__ void k_mrg_pool(int npix, uint32_t seed, int first_update, int num_updates, float* out) {
+__global__ void k_mrg_pool(int pixel0, int npix, uint32_t seed, int first_update, int num_updates, float* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npix) return;
     curandStateMRG32k3a s;
-    curand_init((unsigned long long)seed, (unsigned long long)i, 0ull, &s);
+    curand_init((unsigned long long)seed, (unsigned long long)(uint32_t)(pixel0 + i), 0ull, &s);
     for (int u = 0; u < first_update; ++u) (void)draw3(&s);
     for (int u = 0; u < num_updates; ++u) {
         v3 r = draw3(&s);
@@ -1785,9 +1785,9 @@ cudaError_t k_launch_mrg_states(uint32_t seed, const uint32_t* sub, int n, int m
     return cudaGetLastError();
 }
 
-cudaError_t k_launch_mrg_pool(int npix, uint32_t seed, int first_update, int num_updates, float* out,
+cudaError_t k_launch_mrg_pool(int pixel0, int npix, uint32_t seed, int first_update, int num_updates, float* out,
                               cudaStream_t st) {
-    k_mrg_pool<<<blocks_for(npix), kBlock, 0, st>>>(npix, seed, first_update, num_updates, out);
+    k_mrg_pool<<<blocks_for(npix), kBlock, 0, st>>>(pixel0, npix, seed, first_update, num_updates, out);
     return cudaGetLastError();
 }
 

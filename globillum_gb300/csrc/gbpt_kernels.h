@@ -217,7 +217,7 @@ cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, do
 int k_launches_per_iteration(int mode);
 cudaError_t k_launch_mrg_states(uint32_t seed, const uint32_t* sub, int n, int method, uint32_t* out,
                                 cudaStream_t st);
-cudaError_t k_launch_mrg_pool(int npix, uint32_t seed, int first_update, int num_updates, float* out,
+cudaError_t k_launch_mrg_pool(int pixel0, int npix, uint32_t seed, int first_update, int num_updates, float* out,
                               cudaStream_t st);
 cudaError_t k_launch_nee_stage(const DevScene& S, int n, float shadow_offset, const float* rnd, const float4* hits,
                                float* ray_orig, float* ray_dir, float* max_t, float* psc, cudaStream_t st);

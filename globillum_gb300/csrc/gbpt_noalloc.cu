@@ -18,8 +18,13 @@
 // each other's frames: serialise them.
 //
 // Set-up: the first call on a device, with that device current, looks up the
-// array's device address (cudaGetSymbolAddress) and caches it; make that
-// first call before any stream capture on the device.
+// array's device address (cudaGetSymbolAddress) and caches it.  The call
+// synchronises its stream and reads counters back to the host on every pass,
+// so it must never be called while its stream is capturing (it returns
+// GB_ERR_INVALID then).  It makes the scene's device current for its work
+// and gives the caller's current device back before it returns.  Errors are
+// recorded in the scene's context (gb_last_error): do not run other calls on
+// that context from another thread at the same time.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -109,10 +114,32 @@ int fail(const gb_scene* s, int code, const char* msg) {
     return code;
 }
 
+// The caller's current device, made current again when the call returns.
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() {
+        if (cudaGetDevice(&prev) != cudaSuccess) { cudaGetLastError(); prev = -1; }
+    }
+    ~DeviceRestore() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+int render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* d, float* out_rgb,
+                   void* stream);
+
 }  // namespace
 
 extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* d,
                                  float* out_rgb, void* stream) {
+    DeviceRestore restore;
+    return render_noalloc(scene, cam, d, out_rgb, stream);
+}
+
+namespace {
+
+int render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* d, float* out_rgb,
+                   void* stream) {
     if (!scene || !cam || !d || !out_rgb) return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: null argument");
     if (d->width <= 0 || d->height <= 0 || d->spp <= 0 || d->max_bounces <= 0)
         return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: bad resolution / spp / bounces");
@@ -135,6 +162,13 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
         return fail(scene, GB_ERR_CUDA, "gb_render_noalloc: cudaGetSymbolAddress of the scratch array failed");
     }
     cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(scene, GB_ERR_CUDA, "gb_render_noalloc: cudaStreamIsCapturing failed");
+    }
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(scene, GB_ERR_INVALID, "gb_render_noalloc: the stream is capturing (the call synchronises it)");
     const int n = d->width * d->height;
     SceneRec* d_rec = nullptr;
     Frame F = carve(base, n, &d_rec);
@@ -165,26 +199,31 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
     if (e == cudaSuccess) e = k_launch_frame_init(F, true, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)n, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(F.jcursor, F.pristine, sizeof(MrgState) * (size_t)n, cudaMemcpyDeviceToDevice, st);
-    // one path sample of every pixel per pass; the host checks the queue
-    // count every 8 iterations (a path has at most max_bounces segments)
-    const int max_iters = n * (d->max_bounces + 1) + 8;
+    // one path sample of every pixel per pass, one slot per pixel: a path
+    // has at most max_bounces segments, so the queue is empty after
+    // max_bounces + 1 iterations; the host checks the queue count every 8
+    // iterations and the device flags a queue still non-empty after
+    // max_bounces + 2 iterations (ST_ITER_LIMIT)
+    const int max_iters = d->max_bounces + 2;
+    uint32_t left = 0;
     for (int p = 0; p < d->spp && e == cudaSuccess; ++p) {
         P.p0 = p;
         e = cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, st);
         if (e == cudaSuccess) e = k_launch_jitter_pool(F, P, st);
         if (e == cudaSuccess) e = k_launch_start(F, P, n, st);
-        uint32_t left = 1;
-        for (int it = 0; e == cudaSuccess && left != 0u && it <= d->max_bounces + 1; ++it) {
+        left = 1;
+        for (int it = 0; e == cudaSuccess && left != 0u && it < max_iters; ++it) {
             e = k_launch_extend(F, P, false, st);
             if (e == cudaSuccess) e = k_launch_shadow(F, P, false, st);
             if (e == cudaSuccess) e = k_launch_shade(F, P, st);
             if (e == cudaSuccess) e = k_launch_regen(F, P, st);
             if (e == cudaSuccess) e = k_launch_step(F, P, 0, false, max_iters, st);
-            if (e == cudaSuccess && (it % 8 == 7 || it == d->max_bounces)) {
+            if (e == cudaSuccess && (it % 8 == 7 || it == d->max_bounces || it == max_iters - 1)) {
                 e = cudaMemcpyAsync(&left, F.ctr + 8 * ((it + 1) % 3), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             }
         }
+        if (e == cudaSuccess && left != 0u) break;  // paths still queued: reported below
         if (e == cudaSuccess) e = k_launch_combine(F, P, st);
     }
     if (e == cudaSuccess) e = k_launch_pack_rgb(F.out, n, out_rgb, st);
@@ -195,6 +234,8 @@ extern "C" int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, co
         cudaGetLastError();
         return fail(scene, GB_ERR_CUDA, cudaGetErrorString(e));
     }
-    if (status) return fail(scene, GB_ERR_TRAVERSAL, "gb_render_noalloc: traversal bound exceeded");
+    if (status || left != 0u) return fail(scene, GB_ERR_TRAVERSAL, "gb_render_noalloc: traversal bound exceeded");
     return GB_OK;
 }
+
+}  // namespace

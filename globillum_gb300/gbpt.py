@@ -130,7 +130,7 @@ EXPORTS = [
     "gb_ctx_create", "gb_ctx_destroy", "gb_last_error", "gb_ctx_set_stream", "gb_scene_create", "gb_scene_destroy",
     "gb_scene_get_info", "gb_render", "gb_render_begin", "gb_render_step", "gb_render_paths_done", "gb_render_read",
     "gb_trace_closest", "gb_trace_any", "gb_generate_arealight_sample", "gb_compute_path_contribution_and_bounce",
-    "gb_mrg_pool", "gb_mrg_states", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
+    "gb_mrg_pool", "gb_mrg_pool_range", "gb_mrg_states", "gb_get_stats", "gb_render_instrumented", "gb_layout_sizes", "gb_ctx_set_stage_timing",
     "gb_render_noalloc", "gb_ctx_set_tuning", "gb_ctx_get_tuning", "gb_set_fault_injection", "gb_render_batch",
     "gb_autotune", "gb_scene_param_count", "gb_scene_get_params", "gb_scene_set_params", "gb_forward",
     "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
@@ -177,6 +177,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_compute_path_contribution_and_bounce.argtypes = [vp, vp, ip, ip, C.POINTER(RenderDesc), vp, vp, vp, vp,
                                                             vp, vp, vp, vp, vp, vp, ip, ip]
     lib.gb_mrg_pool.argtypes = [vp, ip, C.c_uint32, ip, ip, vp]
+    lib.gb_mrg_pool_range.argtypes = [vp, ip, ip, C.c_uint32, ip, ip, vp]
     lib.gb_mrg_states.argtypes = [vp, C.c_uint32, vp, ip, ip, vp]
     lib.gb_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.gb_layout_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -394,9 +395,11 @@ class Context:
         self.check(self.lib.gb_mrg_states(self.h, seed, _ptr(sub), sub.size, method, _ptr(out)))
         return out
 
-    def mrg_pool(self, npix: int, num_updates: int, first_update: int = 0, seed: int = 0) -> np.ndarray:
+    def mrg_pool(self, npix: int, num_updates: int, first_update: int = 0, seed: int = 0,
+                 pixel0: int = 0) -> np.ndarray:
+        """(num_updates, npix, 3) pool values of pixels pixel0 .. pixel0 + npix - 1."""
         out = np.empty((num_updates, npix, 3), dtype=np.float32)
-        self.check(self.lib.gb_mrg_pool(self.h, npix, seed, first_update, num_updates, _ptr(out)))
+        self.check(self.lib.gb_mrg_pool_range(self.h, pixel0, npix, seed, first_update, num_updates, _ptr(out)))
         return out
 
 

@@ -407,6 +407,12 @@ int gb_compute_path_contribution_and_bounce(gb_ctx* ctx, gb_scene* scene, int w,
  * (util-kernels.cu:287-302) leaves in the pool at update first_update+u
  * (curand_init(seed, i, 0), 3 curand_uniform per update).  Host `out`. */
 int gb_mrg_pool(gb_ctx* ctx, int npix, uint32_t seed, int first_update, int num_updates, float* out);
+/* The same for pixels pixel0 .. pixel0 + npix - 1 (a band of rows of a
+ * frame): out[(u*npix + i)*3 + k] is draw 3*(first_update+u)+k of pixel
+ * pixel0 + i's stream, the pool slice the reference's bouncer downloads for
+ * those pixels (hybrid-pt.h:232-233).  Host `out`. */
+int gb_mrg_pool_range(gb_ctx* ctx, int pixel0, int npix, uint32_t seed, int first_update, int num_updates,
+                      float* out);
 /* The MRG32k3a states curand_init(seed, subsequences[i], 0) leaves, as
  * out[6 i .. 6 i + 5] = s1[0..2], s2[0..2].  method 0: curand_init itself
  * (the reference's seeding call, util-kernels.cu:284); method 1: the
@@ -484,12 +490,16 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
  * `out_rgb` (w*h*3 floats) on `stream` (NULL = legacy default stream), with
  * its wavefront state in one fixed file-scope device array (about 25 MB,
  * held by every GPU that loads the library until exit) instead of cudaMalloc.
- * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID.
+ * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID;
+ * scenes with texture coordinates return GB_ERR_UNSUPPORTED (use gb_render).
  * The first call on a device looks the array up (cudaGetSymbolAddress) with
- * that device current; make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race; serialise them.  Returns
- * after the frame is finished; errors are reported through the scene's
- * context (gb_last_error). */
+ * the scene's device current; the caller's current device is restored
+ * before the call returns.  Every call synchronises `stream` and reads
+ * counters back to the host, so it must never be called while `stream` is
+ * capturing (GB_ERR_INVALID).  All calls share the array: calls that overlap
+ * on the GPU race; serialise them.  Returns after the frame is finished;
+ * errors are reported through the scene's context (gb_last_error), so do
+ * not run other calls on that context from another thread meanwhile. */
 int gb_render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_desc* desc,
                       float* out_rgb, void* stream);
 

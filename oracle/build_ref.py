@@ -20,8 +20,17 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_SRC = Path(os.environ.get("GBPT_REFERENCE_SRC", "/root/reference/src"))
+# The reference tree this recipe compiles from and the CPU tests read assets
+# from: GB_REFERENCE_TREE when set, else the build container's mount.  The
+# GPU machine has no reference tree; everything here is then a no-op.
+REF_TREE = Path(os.environ.get("GB_REFERENCE_TREE") or "/root/reference")
+REF_SRC = REF_TREE / "src"
 OUT = HERE / "_ref" / "libgiref.so"
+
+
+def reference_tree() -> Path | None:
+    """The reference tree when it is present, else None."""
+    return REF_TREE if (REF_SRC / "arealight-sampler-cpu.cpp").exists() else None
 
 
 def _cuda_include() -> str:
@@ -31,7 +40,7 @@ def _cuda_include() -> str:
 
 
 def build_ref(force: bool = False) -> Path | None:
-    if not (REF_SRC / "arealight-sampler-cpu.cpp").exists():
+    if reference_tree() is None:
         return None
     srcs = [REF_SRC / "arealight-sampler-cpu.cpp", HERE / "ref_glue.cpp"]
     deps = srcs + list((HERE / "ref_shim").rglob("*.h"))

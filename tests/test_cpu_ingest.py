@@ -5,13 +5,14 @@ rectangular-light forms of scene scripts.  Fixtures: tests/golden/assets
 (written for these tests); the reference's bundled OBJ assets are loaded
 too when its tree is available."""
 import ctypes as C
-import os
 from pathlib import Path
 
 import numpy as np
 import pytest
 
 from globillum_gb300 import gbpt
+
+ROOT = Path(__file__).resolve().parent.parent
 
 ASSETS = Path(__file__).resolve().parent / "golden" / "assets"
 
@@ -101,10 +102,18 @@ def test_ingest_errors(tmp_path, lib_path):
     a.close()
 
 
-REF = Path(os.environ.get("GB_REFERENCE_TREE", "/root/reference"))
+def _reference_tree():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gbpt_build_ref", ROOT / "oracle" / "build_ref.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.reference_tree()
 
 
-@pytest.mark.skipif(not (REF / "boxes.obj").exists(), reason="reference tree not available")
+REF = _reference_tree()
+
+
+@pytest.mark.skipif(REF is None or not (REF / "boxes.obj").exists(), reason="reference tree not available")
 def test_reference_bundled_assets(lib_path):
     """The reference's own OBJ assets and material files load; every face
     of them is a triangle, so the triangle counts equal the face counts."""
