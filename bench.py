@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--sah-bins", type=int, default=0, help="binned-SAH bins per axis of the host builder (0 = 32)")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the mixed batch leg (0 = skip it)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the path-replay adjoint leg")
-    ap.add_argument("--rmse-spp", type=int, default=1024, help="spp of the converged reference image (0 = skip)")
+    ap.add_argument("--no-c0", dest="c0", action="store_false", help="skip the Cornell (256^2, 16 spp) leg")
+    ap.add_argument("--rmse-spp", type=int, default=1, help="0 = skip the RMSE against the fp64 reference images")
     ap.add_argument("--inverse-iters", type=int, default=200, help="Adam iterations of the inverse leg (0 = skip)")
     return ap.parse_args()
 
@@ -145,29 +146,44 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_sample(sc, min_seconds: float, max_frames: int = 64, orc=None):
+def frame_pools(sc, ctx=None):
+    """The per-pixel MRG32k3a pools of the workload's first path sample
+    (updates 0 .. L-1 of curand_init(seed, pixel, 0), hybrid-pt.cpp:83-95),
+    made by curand on the GPU as the reference makes them
+    (util-kernels.cu:305-333), so that a CPU frame renders the same paths as
+    the GPU's first sample.  Without a context: seeded uniform pools."""
+    r = sc.render
+    n = r["width"] * r["height"]
+    if ctx is None:
+        return np.random.default_rng(11).uniform(1e-7, 1.0, size=(r["max_bounces"], n, 3)).astype(np.float32), \
+            "seeded uniform pools"
+    return ctx.mrg_pool(n, r["max_bounces"], seed=r["seed"]), "the GPU frame's MRG32k3a pools (path sample 0)"
+
+
+def cpu_sample(sc, min_seconds: float, max_frames: int = 64, orc=None, pool=None, serial_nee: bool = False):
     """Times the oracle (CPU restatement of the hybrid path, all host threads)
     on whole frames of the workload at 1 spp until `min_seconds` have passed;
-    returns (Mpaths/s, seconds, frames, cores).  The BVH build is excluded."""
+    returns (Mpaths/s, seconds, frames, cores, last image).  serial_nee: the
+    reference as it is, whose light-sample loop runs on one thread (the
+    misspelt `#pragma omp prallel`, arealight-sampler-cpu.cpp:148).  The BVH
+    build is excluded."""
     from oracle import oracle
     rd = dict(sc.render, spp=1)
-    n = rd["width"] * rd["height"]
     own = orc is None
     if own:
         orc = oracle.OracleScene(sc, use_bvh=True)
-    total, frames = 0.0, 0
+    if pool is None:
+        pool = frame_pools(sc)[0]
+    n = rd["width"] * rd["height"]
+    total, frames, img = 0.0, 0, None
     while frames < max_frames and (total < min_seconds or frames == 0):
-        # the pool values do not change the amount of work on average; seeded
-        # uniform pools keep this leg off the GPU
-        pool = np.random.default_rng(11 + frames).uniform(1e-7, 1.0, size=(rd["max_bounces"], n, 3)).astype(
-            np.float32)
         t0 = time.perf_counter()
-        orc.render(sc.camera, rd, pool)
+        img = orc.render(sc.camera, rd, pool, serial_nee=serial_nee)
         total += time.perf_counter() - t0
         frames += 1
     if own:
         orc.close()
-    return n * frames / total / 1e6, total, frames, oracle.threads()
+    return n * frames / total / 1e6, total, frames, oracle.threads(), img
 
 
 def run_reference(args, rank, world):
@@ -176,21 +192,108 @@ def run_reference(args, rank, world):
     from oracle import oracle
     sc = workload(args.workload, args.spp)
     orc = oracle.OracleScene(sc, use_bvh=True)
+    ctx = None
+    try:  # the pools come from curand on the GPU, as in the reference (util-kernels.cu:305-333)
+        import torch
+        if torch.cuda.is_available():
+            from globillum_gb300 import build, gbpt
+            if not build.LIB.exists():
+                build.build_lib()
+            ctx = gbpt.Context(0)
+    except Exception:
+        ctx = None
+    pool, pool_kind = frame_pools(sc, ctx)
+    if ctx is not None:
+        ctx.close()
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, frames, cores = cpu_sample(sc, 0.0, max_frames=1, orc=orc)
+        v, dt, frames, cores, _ = cpu_sample(sc, 0.0, max_frames=1, orc=orc, pool=pool)
         if i >= args.warmup:
             vals.append((v, dt))
     ms = float(np.sum([x[1] for x in vals])) * 1e3 / len(vals)
     v = sc.render["width"] * sc.render["height"] * len(vals) / (ms * len(vals) / 1e3) / 1e6
+    # the reference as it is: light samples on one thread (arealight-sampler-cpu.cpp:148)
+    v_asis, dt_asis, _, _, _ = cpu_sample(sc, 0.0, max_frames=1, orc=orc, pool=pool, serial_nee=True)
+    orc.close()
     sample = f"one whole {sc.render['width']}x{sc.render['height']} frame at 1 spp per step (bounded sample of " \
-             f"the {sc.render['spp']}-spp frame), seeded uniform pools"
+             f"the {sc.render['spp']}-spp frame), {pool_kind}; light-sample loop on all threads"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(sc, {"sample": sample}),
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+            "reference_as_is": {"value": v_asis, "unit": METRIC, "cores": cores, "seconds": dt_asis,
+                                "note": "the light-sample loop on one thread, as the misspelt pragma of "
+                                        "arealight-sampler-cpu.cpp:148 leaves it; shading on all threads"},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+FP64_REFS = ROOT / "tests" / "golden" / "fp64_refs.npz"
+
+
+def fp64_rmse(img, key: str, spp: int) -> dict:
+    """RMSE of a frame (numpy, rows x w x 3) over the rows of the converged
+    reference image `key` in tests/golden/fp64_refs.npz (the oracle's
+    independent double-precision restatement of the hybrid path, thousands of
+    spp, written by tests/golden/make_fp64_refs.py), with the RMSE an
+    unbiased spp-sample frame would show (the reference's per-pixel variance)
+    and the image-mean difference in standard errors."""
+    g = np.load(FP64_REFS)
+    r0, r1 = (int(v) for v in g[key + "_rows"])
+    ref = g[key].astype(np.float64)
+    x = np.asarray(img, np.float64)[r0:r1]
+    n_ref, var = int(g[key + "_spp"]), float(g[key + "_var"].mean())
+    noise = float(np.sqrt(var * (1.0 / spp + 1.0 / n_ref)))
+    return {"value": float(np.sqrt(np.mean((x - ref) ** 2))), "noise_predicted": noise,
+            "bias_z": float((x.mean() - ref.mean()) / (noise / np.sqrt(x.size))),
+            "reference": f"fp64 oracle, {n_ref} spp (rows {r0}-{r1 - 1})", "image_spp": spp}
+
+
+def c0_leg(ctx, args, torch, flush, with_cpu: bool):
+    """The CPU-runnable configuration: the 48-triangle Cornell room, 256x256,
+    16 spp, 5 bounces, Halton light samples, MRG32k3a path samples.  GPU
+    frame device-timed (L2 flushed), its RMSE against the fp64 reference of
+    the whole frame; on the host, the oracle at the same spp on the same
+    pools (as the reference and OpenMP-fixed), whose image is compared with
+    the GPU's."""
+    from globillum_gb300 import scenes
+    sc = scenes.cornell()
+    r = sc.render
+    W, H, spp = r["width"], r["height"], r["spp"]
+    scene = ctx.scene(sc)
+    out = torch.empty((H, W, 3), device="cuda", dtype=torch.float32)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(1, args.warmup)):
+        scene.render_device(sc.camera, r, out.data_ptr())
+    ts = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        scene.render_device(sc.camera, r, out.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    img = out.cpu().numpy()
+    ms = float(np.median(ts))
+    res = {"workload": {"scene": sc.name, "triangles": sc.num_triangles, "width": W, "height": H, "spp": spp,
+                        "max_bounces": r["max_bounces"], "light_samples": "Halton"},
+           "value": W * H * spp / ms / 1e3, "unit": METRIC, "ms_per_frame": ms,
+           "rmse": fp64_rmse(img, "c0", spp)}
+    if with_cpu:
+        from oracle import oracle
+        orc = oracle.OracleScene(sc, use_bvh=True)
+        pool = ctx.mrg_pool(W * H, spp * r["max_bounces"], seed=r["seed"])
+        for serial, name in ((False, "cpu_openmp_fixed"), (True, "cpu_reference_as_is")):
+            t0 = time.perf_counter()
+            cimg = orc.render(sc.camera, r, pool, serial_nee=serial)
+            dt = time.perf_counter() - t0
+            res[name] = {"value": W * H * spp / dt / 1e6, "unit": METRIC, "seconds": dt, "cores": oracle.threads(),
+                         "image_equals_gpu": bool(np.array_equal(cimg, img))}
+        res["rmse"]["cpu_frame"] = fp64_rmse(cimg, "c0", spp)["value"]
+        orc.close()
+    scene.close()
+    return res
 
 
 def batch_leg(ctx, args, torch, flush, dist):
@@ -213,7 +316,7 @@ def batch_leg(ctx, args, torch, flush, dist):
             for sc in mixed]
     ptrs = [o.data_ptr() for o in outs]
     t0 = time.perf_counter()
-    tuning, tune_ms = ctx.autotune(jobs, proxy_spp=4, repeats=1)
+    tuning, tune_ms = ctx.autotune(jobs, proxy_spp=4, repeats=3)
     tune_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
 
@@ -244,6 +347,9 @@ def batch_leg(ctx, args, torch, flush, dist):
     plain_ms = timed(plain)
     plain_imgs = [o.clone() for o in outs]
     batch_ms = timed(batched)
+    big = int(np.argmax([sc.num_triangles for sc in mixed]))
+    rmse_big = (fp64_rmse(outs[big].cpu().numpy(), "c2", mixed[big].render["spp"])
+                if big == 2 and args.rmse_spp > 0 else None)
     launches = ctx.stats()["kernel_launches"]
     same = all(torch.equal(a, b) for a, b in zip(plain_imgs, outs))
     tot_b, ms_b = replicas.aggregate(paths * args.steps, batch_ms, dist, "cuda")
@@ -255,6 +361,7 @@ def batch_leg(ctx, args, torch, flush, dist):
     return {"value": vb, "unit": METRIC, "plain_value": vp, "batched_over_plain": vb / vp,
             "ms_per_step": ms_b / args.steps, "plain_ms_per_step": ms_p / args.steps,
             "images_identical": bool(same), "paths_per_step": paths, "launches_per_step": int(launches),
+            "rmse_largest_scene": rmse_big,
             "workload": {"scenes": len(mixed), "triangles_total": int(sum(tris)), "triangles_min": int(min(tris)),
                          "triangles_max": int(max(tris)), "resolutions": [64, 128, 256, 512], "spp": [4, 16, 64],
                          "max_bounces": 6, "generate_s": gen_s, "bvh_build_and_upload_s": build_s},
@@ -300,6 +407,7 @@ def adjoint_leg(ctx, scene, sc, args, torch, flush, orc):
         return float(np.median(ts))
 
     fwd_ms = timed(lambda: scene.render_device(sc.camera, rd, img.data_ptr()))
+    rmse_fwd = fp64_rmse(img.cpu().numpy(), "c3", rd["spp"]) if args.rmse_spp > 0 else None
     dimg = (2.0 * (img - target)).contiguous()
     grad_box = {}
 
@@ -344,6 +452,7 @@ def adjoint_leg(ctx, scene, sc, args, torch, flush, orc):
     out = {"workload": {"scene": sc.name, "width": W, "height": H, "spp": rd["spp"], "max_bounces": rd["max_bounces"],
                         "params": int(x0.size), "loss": "L2 to a target from materials seeded 97"},
            "forward_ms": fwd_ms, "backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms, "loss": loss0,
+           "rmse_forward_frame": rmse_fwd,
            "adjoint_record_bytes": int(80 * rd["max_bounces"] * min(W * H, 1 << 20)),
            "finite_differences": {"h": h, "params": int(sel.size), "median_rel_err": float(np.median(rel_fd)),
                                   "max_rel_err": float(rel_fd.max()),
@@ -603,19 +712,13 @@ def run_gbpt(args, rank, world):
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": W * H * 3 * 4},
             "gpu_launches": int(launches)}
-    if args.rmse_spp > 0:
-        # converged image of the same frame (same estimator and streams, 16x the
-        # samples); the timed frame's RMSE against it.  Batched and CPU images are
-        # bit-identical to this frame's, so their RMSE is the same.
-        ref_img = torch.empty_like(out)
-        scene.render_device(sc.camera, dict(r, spp=args.rmse_spp), ref_img.data_ptr())
+    if args.rmse_spp > 0 and args.workload == "icospheres-1m" and spp == 64:
+        # the timed frame against the converged fp64 reference of its rows
+        # 352-367 (an independent double-precision restatement, its own random
+        # numbers); batched and CPU frames are bit-identical to this frame's
         scene.render_device(sc.camera, r, out.data_ptr())
         torch.cuda.synchronize()
-        diff = (out.double() - ref_img.double())
-        line["rmse"] = {"value": float(diff.pow(2).mean().sqrt().item()), "reference_spp": args.rmse_spp,
-                        "reference_mean": float(ref_img.double().mean().item()),
-                        "image_spp": spp, "arithmetic": "fp32, IEEE-exact per path (bit-identical to the oracle)"}
-        del ref_img
+        line["rmse"] = fp64_rmse(out.cpu().numpy(), "c1", spp)
     if args.batch_scenes > 0:
         line["batched"] = batch_leg(ctx, args, torch, flush, dist)
     orc = None
@@ -626,11 +729,37 @@ def run_gbpt(args, rank, world):
         line["adjoint"] = adjoint_leg(ctx, scene, sc, args, torch, flush, orc)
     if args.inverse_iters > 0:
         line["inverse"] = inverse_leg(ctx, args, torch, dist)
+    if args.c0:
+        line["c0"] = c0_leg(ctx, args, torch, flush, orc is not None)
     if orc is not None:
-        v, dt, frames, cores = cpu_sample(sc, args.cpu_seconds, orc=orc)
+        pool, pool_kind = frame_pools(sc, ctx)
+        v, dt, frames, cores, cimg = cpu_sample(sc, args.cpu_seconds, orc=orc, pool=pool)
+        v1, dt1, _, _, _ = cpu_sample(sc, 0.0, max_frames=1, orc=orc, pool=pool, serial_nee=True)
+        scene.render_device(sc.camera, dict(r, spp=1), out.data_ptr())
+        same1 = bool(np.array_equal(cimg, out.cpu().numpy()))
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
                                 "sample": f"{frames} whole {W}x{H} frames at 1 spp ({dt:.1f} s of CPU time, "
-                                          f"BVH build excluded)"}
+                                          f"BVH build excluded), {pool_kind}",
+                                "image_equals_gpu_1spp_frame": same1,
+                                "reference_as_is": {"value": v1, "unit": METRIC, "seconds": dt1,
+                                                    "note": "light-sample loop on one thread "
+                                                            "(arealight-sampler-cpu.cpp:148)"}}
+        if "rmse" in line:
+            # the CPU frame of the timed configuration over the reference rows:
+            # the oracle at 64 spp on the GPU frame's own pools
+            g = np.load(FP64_REFS)
+            r0, r1 = (int(x) for x in g["c1_rows"])
+            bpool = ctx.mrg_pool((r1 - r0) * W, spp * r["max_bounces"], seed=r["seed"], pixel0=r0 * W)
+            t0 = time.perf_counter()
+            band = orc.render(sc.camera, r, bpool, r0, r1)
+            band_s = time.perf_counter() - t0
+            scene.render_device(sc.camera, r, out.data_ptr())
+            gpu_band = out.cpu().numpy()[r0:r1]
+            full = np.zeros((H, W, 3), np.float32)
+            full[r0:r1] = band
+            line["rmse"]["cpu_frame"] = fp64_rmse(full, "c1", spp)["value"]
+            line["rmse"]["cpu_frame_equals_gpu"] = bool(np.array_equal(band, gpu_band))
+            line["rmse"]["cpu_frame_seconds"] = band_s
         orc.close()
     scene.close()
     ctx.close()

@@ -22,6 +22,7 @@ LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libgbpt.so"
 HEADLESS = LIBDIR / "gi_headless"
 ORACLE_SRC = ROOT / "oracle" / "gbpt_oracle.cpp"
+ORACLE_F64_SRC = ROOT / "oracle" / "fp64_render.cpp"
 ORACLE_LIB = ROOT / "oracle" / "_build" / "libgbpt_oracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -123,14 +124,16 @@ def build_headless(force: bool = False) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    """Compiles the CPU oracle (test infrastructure) into oracle/_build."""
+    """Compiles the CPU oracle (test infrastructure) into oracle/_build: the
+    float restatement of the hybrid path and the independent double-precision
+    one (fp64_render.cpp)."""
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    deps = [ORACLE_SRC, CSRC / "gbpt_math.h", CSRC / "gbpt_host.h", ROOT / "include" / "gbpt.h"]
+    deps = [ORACLE_SRC, ORACLE_F64_SRC, CSRC / "gbpt_math.h", CSRC / "gbpt_host.h", ROOT / "include" / "gbpt.h"]
     if not force and not _stale(ORACLE_LIB, deps):
         return ORACLE_LIB
     tmp = ORACLE_LIB.with_suffix(".so.tmp")
     _run_parallel([["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-                    str(ORACLE_SRC), "-o", str(tmp)]])
+                    str(ORACLE_SRC), str(ORACLE_F64_SRC), "-o", str(tmp)]])
     os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 

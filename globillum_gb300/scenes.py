@@ -111,6 +111,42 @@ def cornell(width: int = 256, height: int = 256, spp: int = 16, max_bounces: int
                      name="cornell-48tri")
 
 
+def principled_room(width: int = 48, height: int = 48, spp: int = 16, max_bounces: int = 6,
+                    rr_start: int = 2) -> SceneData:
+    """The Cornell room with one principled material per part, so that every
+    lobe of principledMaterial.h is reached: a rough metal floor, a
+    sheen/subsurface ceiling, a clearcoated back wall, an anisotropic metal
+    left wall, a Lambert right wall, a glass short box (opacity < 1) and a
+    near-mirror tall box; Russian roulette from `rr_start`.  The glass box
+    floats 0.01 above the floor: rays inside it reach its bottom face, which
+    would otherwise be coplanar with the floor, and which of two coplanar
+    faces a float triangle test reports first is a matter of rounding."""
+    sc = cornell(width=width, height=height, spp=spp, max_bounces=max_bounces)
+    pos = sc.positions.copy()
+    glass_box = sc.material_index == 5
+    pos[glass_box, 1::3] += np.float32(0.01)
+    params = [
+        {"color": (0.8, 0.6, 0.3), "metallic": 1.0, "roughness": 0.35},
+        {"color": (0.7, 0.7, 0.6), "roughness": 0.6, "sheen": 0.8, "sheen_tint": 0.5, "subsurface": 0.5},
+        {"color": (0.3, 0.5, 0.7), "roughness": 0.4, "clearcoat": 1.0, "clearcoat_gloss": 0.7, "specular": 0.5,
+         "specular_tint": 0.3},
+        {"color": (0.6, 0.7, 0.8), "metallic": 1.0, "roughness": 0.5, "anisotropic": 0.7},
+        None,
+        {"color": (0.9, 0.9, 0.9), "roughness": 0.2, "opacity": 0.5},
+        {"color": (0.9, 0.8, 0.7), "metallic": 1.0, "roughness": 0.06},
+    ]
+    mats, plist = [], []
+    for m, p in zip(sc.materials, params):
+        if p is None:
+            mats.append(dict(m))
+        else:
+            mats.append({"diffuse": p["color"], "principled": len(plist)})
+            plist.append(p)
+    render = dict(sc.render, rng_mode=0, rr_start=rr_start)
+    return SceneData(pos, sc.normals, sc.material_index, mats, plist, sc.lights, sc.camera, render,
+                     name="principled-room-48tri")
+
+
 # ------------------------------------------------------------- icospheres --
 
 def icosphere(level: int = 3):

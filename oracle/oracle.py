@@ -48,6 +48,12 @@ def load() -> C.CDLL:
         lib.orc_mrg_jump.argtypes = [C.c_ulonglong, vp, vp]
         lib.orc_atan2_acos.argtypes = [ip, vp, vp, vp, vp]
         lib.orc_dist1d.argtypes = [ip, vp, ip, vp, vp, vp]
+        lib.orc64_scene_create.restype = vp
+        lib.orc64_scene_create.argtypes = [vp]
+        lib.orc64_scene_destroy.argtypes = [vp]
+        lib.orc64_scene_destroy.restype = None
+        lib.orc64_render.argtypes = [vp, vp, vp, ip, ip, ip, C.c_ulonglong, vp, vp]
+        lib.orc64_trace_closest.argtypes = [vp, ip, vp, vp, vp, vp, vp]
         lib.orc_threads.restype = ip
         lib.orc_set_threads.argtypes = [ip]
         lib.orc_set_threads.restype = None
@@ -186,6 +192,54 @@ class OracleScene:
             _p(np.ascontiguousarray(rnd, np.float32)), _p(t), _p(a), _p(np.ascontiguousarray(to_light, np.float32)),
             _p(np.ascontiguousarray(psc, np.float32)), path, bounce, 0)
         return ro, rd, mt, t, a
+
+
+class F64Scene:
+    """The independent double-precision restatement (oracle/fp64_render.cpp):
+    its own BVH, its own random numbers, every formula re-derived in double.
+    Renders converged reference images; rect lights, untextured materials."""
+
+    def __init__(self, scene):
+        self.lib = load()
+        desc, self._keep = _gbpt.make_scene_desc(scene)
+        self.h = self.lib.orc64_scene_create(C.byref(desc))
+        if not self.h:
+            raise ValueError("fp64 scene creation failed (sky light, texture or bad description)")
+
+    def close(self):
+        if self.h:
+            self.lib.orc64_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, cam: dict, rdesc: dict, spp: int, seed: int = 1, row0: int = 0, row1: int | None = None,
+               with_var: bool = False):
+        """Mean radiance (rows, w, 3) float64 over `spp` path samples of rows
+        [row0, row1); with_var also returns each pixel's one-sample variance."""
+        rd = _gbpt.make_render_desc(rdesc)
+        cm = _gbpt.make_camera(cam)
+        row1 = rd.height if row1 is None else row1
+        mean = np.empty((row1 - row0, rd.width, 3), np.float64)
+        var = np.empty_like(mean) if with_var else None
+        rc = self.lib.orc64_render(self.h, C.byref(cm), C.byref(rd), row0, row1, int(spp), int(seed), _p(mean),
+                                   _p(var))
+        if rc != 0:
+            raise ValueError(f"orc64_render failed ({rc})")
+        return (mean, var) if with_var else mean
+
+    def trace_closest(self, o, d, tmax):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        tmax = np.ascontiguousarray(tmax, np.float32)
+        ids = np.empty(tmax.shape[0], np.int32)
+        t = np.empty(tmax.shape[0], np.float64)
+        self.lib.orc64_trace_closest(self.h, tmax.shape[0], _p(o), _p(d), _p(tmax), _p(ids), _p(t))
+        return ids, t
 
 
 def halton_pool(n: int) -> np.ndarray:

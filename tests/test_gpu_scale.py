@@ -30,6 +30,31 @@ def _compare(img, ref, what):
     assert not bad.any(), f"{what}: {bad.any(axis=2).sum()} pixels differ, max abs diff {diff.max():.3g}"
 
 
+def _fp64_refs():
+    from pathlib import Path
+    p = Path(__file__).resolve().parent / "golden" / "fp64_refs.npz"
+    return dict(np.load(p))
+
+
+def _against_fp64(img, key, spp):
+    """A GPU frame (the fixture's rows) against the converged fp64 image of
+    the oracle's independent double-precision restatement: the mean within
+    4 standard errors (no bias) and the RMSE the noise of spp + the
+    reference's samples predicts (var = one-sample variance)."""
+    g = _fp64_refs()
+    ref = g[key].astype(np.float64)
+    n_ref, var = int(g[key + "_spp"]), float(g[key + "_var"].mean())
+    x = img.astype(np.float64)
+    assert x.shape == ref.shape
+    se = np.sqrt(var * (1.0 / spp + 1.0 / n_ref) / x.size)
+    z = (x.mean() - ref.mean()) / se
+    rmse = float(np.sqrt(np.mean((x - ref) ** 2)))
+    expected = float(np.sqrt(var * (1.0 / spp + 1.0 / n_ref)))
+    assert abs(z) < 4.0, f"{key}: GPU mean {x.mean():.5f}, fp64 {ref.mean():.5f}, z = {z:.2f}"
+    assert 0.75 < rmse / expected < 1.33, f"{key}: RMSE {rmse:.5f}, noise predicts {expected:.5f}"
+    return rmse, expected
+
+
 def _check_hits(g, o, what):
     assert np.array_equal(g["ref"], o["ref"]), f"{what}: {(g['ref'] != o['ref']).sum()} triangle ids differ"
     hit = o["ref"] != 0xFFFFFFFF
@@ -179,6 +204,9 @@ def test_c1_band_64spp(gpu_ctx, c1):
     pool = gpu_ctx.mrg_pool((r1 - r0) * W, rd["spp"] * rd["max_bounces"], pixel0=r0 * W)
     ref = orc.render(sc.camera, rd, pool, r0, r1)
     _compare(img[r0:r1], ref, "C1 64 spp band")
+    g = _fp64_refs()
+    assert tuple(g["c1_rows"]) == (r0, r1)
+    _against_fp64(img[r0:r1], "c1", rd["spp"])
 
 
 @pytest.mark.parametrize("rng_mode", [gbpt.GB_RNG_HALTON_LIGHT, gbpt.GB_RNG_MRG32K3A_POOL])
@@ -198,6 +226,8 @@ def test_c0_cornell_full_size(gpu_ctx, rng_mode):
     ref = oracle.OracleScene(sc, use_bvh=False).render(sc.camera, rd, pool)
     _compare(img, ref, "C0")
     assert img.mean() > 0.05
+    if rng_mode == gbpt.GB_RNG_HALTON_LIGHT:  # the configuration's light draws
+        _against_fp64(img, "c0", rd["spp"])
 
 
 def test_c2_largest_member_in_batch(gpu_ctx):
@@ -224,3 +254,15 @@ def test_c2_largest_member_in_batch(gpu_ctx):
     pool = gpu_ctx.mrg_pool(rows * W, rd["spp"] * rd["max_bounces"], seed=rd["seed"], pixel0=r0 * W)
     ref = oracle.OracleScene(sc, use_bvh=True).render(sc.camera, rd, pool, r0, r0 + rows)
     _compare(imgs[0][r0:r0 + rows], ref, f"mixed-set scene {big} ({sizes[big]} triangles)")
+    assert tuple(_fp64_refs()["c2_rows"]) == (r0, r0 + rows)
+    _against_fp64(imgs[0][r0:r0 + rows], "c2", rd["spp"])
+
+
+def test_adjoint_configuration_frame_against_fp64(gpu_ctx, c1):
+    """The forward frame of the differentiation workload (the 1M-triangle
+    scene at 512x512, 16 spp, 4 bounces) against its fp64 reference band."""
+    sc, scene, _, _ = c1
+    rd = dict(sc.render, width=512, height=512, spp=16, max_bounces=4)
+    img = scene.render(sc.camera, rd)
+    r0, r1 = (int(v) for v in _fp64_refs()["c3_rows"])
+    _against_fp64(img[r0:r1], "c3", rd["spp"])
