@@ -454,24 +454,24 @@ __device__ __forceinline__ MrgState mrg_pack(const curandStateMRG32k3a& st) {
 // 24-byte states as three 8-byte accesses.
 __device__ __forceinline__ MrgState ld_mrg(const MrgState* base, size_t i) {
     const uint2* q = reinterpret_cast<const uint2*>(base + i);
-    uint2 a = q[0], b = q[1], c = q[2];
+    uint2 a = rec_ld(q), b = rec_ld(q + 1), c = rec_ld(q + 2);
     MrgState m;
     m.s1[0] = a.x; m.s1[1] = a.y; m.s1[2] = b.x; m.s2[0] = b.y; m.s2[1] = c.x; m.s2[2] = c.y;
     return m;
 }
 __device__ __forceinline__ void st_mrg(MrgState* base, size_t i, const MrgState& m) {
     uint2* q = reinterpret_cast<uint2*>(base + i);
-    q[0] = make_uint2(m.s1[0], m.s1[1]);
-    q[1] = make_uint2(m.s1[2], m.s2[0]);
-    q[2] = make_uint2(m.s2[1], m.s2[2]);
+    rec_st(q, make_uint2(m.s1[0], m.s1[1]));
+    rec_st(q + 1, make_uint2(m.s1[2], m.s2[0]));
+    rec_st(q + 2, make_uint2(m.s2[1], m.s2[2]));
 }
 // the same for the stream of a slot record, stored as its whole 32-byte
 // sector (the state and 8 zero bytes)
 __device__ __forceinline__ MrgState ld_mrg(const SlotField<MrgState>& f, size_t slot) { return ld_mrg(&f[slot], 0); }
 __device__ __forceinline__ void st_mrg(const SlotField<MrgState>& f, size_t slot, const MrgState& m) {
     uint4* q = reinterpret_cast<uint4*>(&f[slot]);
-    q[0] = make_uint4(m.s1[0], m.s1[1], m.s1[2], m.s2[0]);
-    q[1] = make_uint4(m.s2[1], m.s2[2], 0u, 0u);
+    rec_st(q, make_uint4(m.s1[0], m.s1[1], m.s1[2], m.s2[0]));
+    rec_st(q + 1, make_uint4(m.s2[1], m.s2[2], 0u, 0u));
 }
 __device__ __forceinline__ v3 draw3(MrgState* m) {
     curandStateMRG32k3a st = mrg_expand(*m);
@@ -594,10 +594,10 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
     const SceneRec& R = F.scenes[sc];
     const uint32_t lp = gpix - R.pixel_base;
     const float4* jp = F.jpool + P.round_start[lo];
-    float4 j = jp[gpix];
+    float4 j = rec_ld(&jp[gpix]);
     float lx = 0.0f, ly = 0.0f;
     if (R.cam.aperture != 0.0f) {
-        float4 lj = jp[R.pixel_base + (lp + 17u) % (uint32_t)R.n];
+        float4 lj = rec_ld(&jp[R.pixel_base + (lp + 17u) % (uint32_t)R.n]);
         lx = lj.z - 0.5f;
         ly = lj.y - 0.5f;
     }
@@ -607,12 +607,12 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
     st_mrg(F.cursor, gpix, bs);
     v3 o, d;
     camera_ray(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w), j.x, j.y, lx, ly, &o, &d);
-    F.ray_o[slot] = make_float4(o.x, o.y, o.z, FLT_MAX);
-    F.ray_d[slot] = make_float4(d.x, d.y, d.z, __uint_as_float(((uint32_t)P.p0 + (uint32_t)lo) << 10));  // w: pb
-    F.tp[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    F.ray_o.st(slot, make_float4(o.x, o.y, o.z, FLT_MAX));
+    F.ray_d.st(slot, make_float4(d.x, d.y, d.z, __uint_as_float(((uint32_t)P.p0 + (uint32_t)lo) << 10)));  // w: pb
+    F.tp.st(slot, make_float4(1.0f, 1.0f, 1.0f, 0.0f));
     if (P.mode == MODE_FROZEN) F.tp0[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    F.accum[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    F.pixw[slot] = make_uint4(gpix, sc, 0u, 0u);
+    F.accum.st(slot, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    F.pixw.st(slot, make_uint4(gpix, sc, 0u, 0u));
     if (R.S.texcoord) st_rdiff(F, slot, camera_diff(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w)));
     else F.rdiff[0][slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // completes the sector of pix / ps
 }
@@ -620,7 +620,7 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
 // The scene record of a slot's path; a frame of one scene needs no load of
 // the slot's scene word.
 __device__ __forceinline__ const SceneRec& scene_of(const Frame& F, uint32_t slot) {
-    return F.scenes[F.nscenes == 1 ? 0u : F.ps[slot]];
+    return F.scenes[F.nscenes == 1 ? 0u : F.ps.ld(slot)];
 }
 
 // Counter set of iteration `it`: [0] queue count, [1] extension head,
@@ -633,7 +633,7 @@ __device__ __forceinline__ uint32_t* ctr_set(const Frame& F, int it) { return F.
 // path p's colour at sample index round_start[p - p0] + pixel.
 __device__ __forceinline__ void store_sample(const Frame& F, const RenderParams& P, uint32_t slot, uint32_t pbv,
                                              float4 acc) {
-    F.samples[P.round_start[(pbv >> 10) - (uint32_t)P.p0] + F.pix[slot]] = acc;
+    rec_st(&F.samples[P.round_start[(pbv >> 10) - (uint32_t)P.p0] + F.pix.ld(slot)], acc);
 }
 
 // Slots whose path ended go to the free queue; k_regen starts the next
@@ -960,7 +960,7 @@ __device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, ui
     st_mrg(F.rng, slot, st);
     v3 lr = rnd;
     if (R.rng_mode == 1) {
-        int pid = (int)(F.pix[slot] - R.pixel_base) + 1;
+        int pid = (int)(F.pix.ld(slot) - R.pixel_base) + 1;
         float hy = halton(pid, 3);
         lr = mk(halton(pid, 2), hy, hy);
     }
@@ -977,10 +977,10 @@ __device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, ui
                               &so, &sd, &smax, &psc, &scale);
     }
     if (skip_dark && psc.x == 0.0f && psc.y == 0.0f && psc.z == 0.0f) smax = -1.0f;
-    F.sh_o[slot] = make_float4(so.x, so.y, so.z, smax);
-    F.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-    F.psc[slot] = make_float4(psc.x, psc.y, psc.z, scale);
-    F.rnd[slot] = make_float4(rnd.x, rnd.y, rnd.z, 0.0f);
+    F.sh_o.st(slot, make_float4(so.x, so.y, so.z, smax));
+    F.sh_d.st(slot, make_float4(sd.x, sd.y, sd.z, 0.0f));
+    F.psc.st(slot, make_float4(psc.x, psc.y, psc.z, scale));
+    F.rnd.st(slot, make_float4(rnd.x, rnd.y, rnd.z, 0.0f));
 }
 
 template <bool INSTR, int MODE>
@@ -995,7 +995,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
     auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
                      const float4** shade) {
         uint32_t slot = qin[q];
-        float4 ro = F.ray_o[slot], rd = F.ray_d[slot];
+        float4 ro = F.ray_o.ld(slot), rd = F.ray_d.ld(slot);
         const SceneRec& R = scene_of(F, slot);
         *nodes = R.S.nodes;
         *tris = R.S.tris;
@@ -1010,12 +1010,12 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
             slot = qin[q];
             hit = h.best_id != 0xffffffffu;
             const SceneRec& R = scene_of(F, slot);
-            uint32_t pbv = F.pb[slot];
+            uint32_t pbv = F.pb.ld(slot);
             if ((pbv & 1023u) > 0u) add_stats_lane(&F.stats[1]);
             if (!hit) {
-                float4 tp4 = F.tp[slot];
-                float4 acc = F.accum[slot];
-                v3 add = miss_contribution(ld3(tp4), ld3(F.ray_d[slot]), R.sp, &R.S.sky);
+                float4 tp4 = F.tp.ld(slot);
+                float4 acc = F.accum.ld(slot);
+                v3 add = miss_contribution(ld3(tp4), ld3(F.ray_d.ld(slot)), R.sp, &R.S.sky);
                 store_sample(F, P, slot, pbv, make_float4(acc.x + add.x, acc.y + add.y, acc.z + add.z, 0.0f));
                 ended = true;
             } else {
@@ -1026,8 +1026,8 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
                 v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
                 v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
                 if (!GB_SPLIT_NEE) nee_at_hit(F, R, slot, Pp, Nr, P.mode != MODE_ADJOINT);
-                F.hit_p[slot] = make_float4(Pp.x, Pp.y, Pp.z, a.w);
-                F.hit_n[slot] = make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id));
+                F.hit_p.st(slot, make_float4(Pp.x, Pp.y, Pp.z, a.w));
+                F.hit_n.st(slot, make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id)));
             }
         }
         push(fin && hit, slot, qsh, cs + 2);
@@ -1046,7 +1046,7 @@ __global__ void __launch_bounds__(kBlock) k_nee(Frame F, int mode) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
         const uint32_t slot = F.q[2][i];
         const SceneRec& R = scene_of(F, slot);
-        nee_at_hit(F, R, slot, ld3(F.hit_p[slot]), ld3(F.hit_n[slot]), mode != MODE_ADJOINT);
+        nee_at_hit(F, R, slot, ld3(F.hit_p.ld(slot)), ld3(F.hit_n.ld(slot)), mode != MODE_ADJOINT);
     }
 }
 
@@ -1061,7 +1061,7 @@ __global__ void __launch_bounds__(kBlock, GB_SHADOW_MIN_BLOCKS) k_shadow(Frame F
     auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
                      const float4** shade) {
         uint32_t slot = qsh[q];
-        float4 so = F.sh_o[slot], sd = F.sh_d[slot];
+        float4 so = F.sh_o.ld(slot), sd = F.sh_d.ld(slot);
         const SceneRec& R = scene_of(F, slot);
         *nodes = R.S.nodes;
         *tris = R.S.tris;
@@ -1074,9 +1074,9 @@ __global__ void __launch_bounds__(kBlock, GB_SHADOW_MIN_BLOCKS) k_shadow(Frame F
     auto finish = [&](bool fin, uint32_t q, const Trav& h) {
         if (fin) {
             uint32_t slot = qsh[q];
-            float smax = F.sh_o[slot].w;
+            float smax = F.sh_o.ld(slot).w;
             bool occl = smax < 0.0f || h.best_id != 0xffffffffu;
-            reinterpret_cast<float*>(&F.sh_d[slot])[3] = occl ? 1.0f : 0.0f;
+            rec_st(reinterpret_cast<float*>(&F.sh_d[slot]) + 3, occl ? 1.0f : 0.0f);
         }
     };
     ray_loop<true, INSTR, MODE>(count, cs + 3, GB_SHADOW_REFILL > 0 ? GB_SHADOW_REFILL : P.refill, F.status, fetch,
@@ -1105,7 +1105,7 @@ __device__ __forceinline__ MaterialRec load_material(const float* mats, uint32_t
 __device__ __forceinline__ int nee_light(const Frame& F, const SceneRec& R, uint32_t slot, v3 rnd) {
     if (R.S.n_lights <= 0) return 0;
     float lz = rnd.z;
-    if (R.rng_mode == 1) lz = halton((int)(F.pix[slot] - R.pixel_base) + 1, 3);
+    if (R.rng_mode == 1) lz = halton((int)(F.pix.ld(slot) - R.pixel_base) + 1, 3);
     return pick_light(R.S.lights, R.S.n_lights, R.S.overall_power, lz);
 }
 
@@ -1119,7 +1119,7 @@ __device__ __noinline__ void texture_hit(const Frame& F, const SceneRec& R, uint
     const float4* sh = R.S.shade + 6 * (size_t)tid;
     const v3 a = ld3(__ldg(sh)), b = ld3(__ldg(sh + 1)), c = ld3(__ldg(sh + 2));
     float t, bb = 0.0f, bg = 0.0f;
-    intersect_tri(ld3(F.ray_o[slot]), ld3(F.ray_d[slot]), a, b - a, c - a, &t, &bb, &bg);
+    intersect_tri(ld3(F.ray_o.ld(slot)), ld3(F.ray_d.ld(slot)), a, b - a, c - a, &t, &bb, &bg);
     const float* tcs = R.S.texcoord + 6 * (size_t)tid;
     float ts, tt;
     bary2(bb, bg, tcs, &ts, &tt);
@@ -1155,29 +1155,29 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
         if (valid) {
             slot = qsh[qi];
             const SceneRec& R = scene_of(F, slot);
-            float4 sd = F.sh_d[slot];
-            float4 hp = F.hit_p[slot], hn = F.hit_n[slot];
+            float4 sd = F.sh_d.ld(slot);
+            float4 hp = F.hit_p.ld(slot), hn = F.hit_n.ld(slot);
             uint32_t mi = __float_as_uint(hp.w);
             const bool textured = TEX && R.S.texcoord != nullptr;
             MaterialRec m = load_material(R.S.mats, mi, textured);
             if (textured) texture_hit(F, R, slot, hn, &m);
-            uint32_t pbv = F.pb[slot];
+            uint32_t pbv = F.pb.ld(slot);
             int bounce = (int)(pbv & 1023u);
             uint32_t path = pbv >> 10;
-            float4 rd = F.ray_d[slot], tp4 = F.tp[slot], rn = F.rnd[slot],
-                   ps = F.psc[slot];
-            float4 acc = F.accum[slot];
+            float4 rd = F.ray_d.ld(slot), tp4 = F.tp.ld(slot), rn = F.rnd.ld(slot),
+                   ps = F.psc.ld(slot);
+            float4 acc = F.accum.ld(slot);
             ShadeOut o;
             if (MODE == MODE_FROZEN) {
                 MaterialRec me = load_material(R.S.mats_eval, mi);
                 v3 t0 = ld3(F.tp0[slot]);
                 o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps), R.sp,
-                              F.pix[slot] - R.pixel_base, path, bounce, &me, &t0);
+                              F.pix.ld(slot) - R.pixel_base, path, bounce, &me, &t0);
                 F.tp0[slot] = make_float4(t0.x, t0.y, t0.z, 0.0f);
             } else if (MODE == MODE_ADJOINT) {
                 ShadeTrace tr;
                 o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps), R.sp,
-                              F.pix[slot] - R.pixel_base, path, bounce, nullptr, nullptr, &tr);
+                              F.pix.ld(slot) - R.pixel_base, path, bounce, nullptr, nullptr, &tr);
                 int light = nee_light(F, R, slot, ld3(rn));
                 uint32_t info = (uint32_t)light | ((uint32_t)tr.lobe << 16) | (tr.clamp_mask << 20) |
                                 (tr.nee ? (1u << 23) : 0u);
@@ -1189,20 +1189,20 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
                 rec[4 * (size_t)F.nslots] = make_float4(tr.ld.x, tr.ld.y, tr.ld.z, __uint_as_float(info));
             } else {
                 o = shade_hit(m, ld3(hp), ld3(hn), ld3(rd), ld3(tp4), ld3(rn), sd.w == 0.0f, ld3(sd), ld3(ps), R.sp,
-                              F.pix[slot] - R.pixel_base, path, bounce);
+                              F.pix.ld(slot) - R.pixel_base, path, bounce);
             }
             acc = make_float4(acc.x + o.accum_add.x, acc.y + o.accum_add.y, acc.z + o.accum_add.z, 0.0f);
             cont = o.alive && bounce + 1 < R.L;
             ended = !cont;
             const float pbw = __uint_as_float(pbv + 1u);  // ray_d.w
             if (cont) {
-                F.tp[slot] = make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f);
-                F.accum[slot] = acc;
-                F.ray_o[slot] = make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX);
-                F.ray_d[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, pbw);
+                F.tp.st(slot, make_float4(o.tp.x, o.tp.y, o.tp.z, 0.0f));
+                F.accum.st(slot, acc);
+                F.ray_o.st(slot, make_float4(o.org.x, o.org.y, o.org.z, FLT_MAX));
+                F.ray_d.st(slot, make_float4(o.dir.x, o.dir.y, o.dir.z, pbw));
             } else {
                 store_sample(F, P, slot, pbv, acc);
-                if (MODE == MODE_ADJOINT) F.ray_d[slot] = make_float4(rd.x, rd.y, rd.z, pbw);  // bounces for k_adjoint
+                if (MODE == MODE_ADJOINT) F.ray_d.st(slot, make_float4(rd.x, rd.y, rd.z, pbw));  // bounces for k_adjoint
             }
         }
         if (GB_FUSED_RESTART && MODE != MODE_ADJOINT) {
@@ -1234,8 +1234,8 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
     const size_t ns = (size_t)F.nslots;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t slot = F.q[3][i];
-        const int K = (int)(F.pb[slot] & 1023u);
-        const float4 g4 = F.dimg[F.pix[slot]];
+        const int K = (int)(F.pb.ld(slot) & 1023u);
+        const float4 g4 = F.dimg[F.pix.ld(slot)];
         if (K == 0 || (g4.x == 0.0f && g4.y == 0.0f && g4.z == 0.0f)) continue;
         const SceneRec& R = scene_of(F, slot);
         const v3 g = ld3(g4);

@@ -91,7 +91,36 @@ enum : size_t {
 };
 static_assert(kSlotRdiff + 48 <= 128 && kSlotRng + 24 <= kSlotBytes, "slot record layout");
 
-// One field of the slot records: f[slot] is that field of record `slot`.
+// Loads and stores of the per-iteration state stream (slot records, samples,
+// jitter pool, stream cursors) carry the cache-streaming hint (ld.cs /
+// st.cs: lines allocated evict-first in L1 and L2), so that the state
+// streaming through every iteration -- several times the L2 -- is evicted
+// before the scene's nodes and triangles.  GB_REC_EVICT_FIRST=0 makes them
+// plain accesses.
+#ifndef GB_REC_EVICT_FIRST
+#define GB_REC_EVICT_FIRST 1
+#endif
+#ifdef __CUDACC__
+template <class T>
+__device__ __forceinline__ T rec_ld(const T* p) {
+#if GB_REC_EVICT_FIRST
+    return __ldcs(p);
+#else
+    return *p;
+#endif
+}
+template <class T>
+__device__ __forceinline__ void rec_st(T* p, const T& v) {
+#if GB_REC_EVICT_FIRST
+    __stcs(p, v);
+#else
+    *p = v;
+#endif
+}
+#endif
+
+// One field of the slot records: f[slot] is that field of record `slot`;
+// f.ld(slot) / f.st(slot, v) are the stream accesses (rec_ld / rec_st).
 template <class T, size_t Stride = kSlotBytes>
 struct SlotField {
     unsigned char* base = nullptr;  // the field in record 0
@@ -101,6 +130,12 @@ struct SlotField {
     inline T& operator[](size_t slot) const {
         return *reinterpret_cast<T*>(base + slot * Stride);
     }
+#ifdef __CUDACC__
+    __device__ inline T ld(size_t slot) const { return rec_ld(reinterpret_cast<const T*>(base + slot * Stride)); }
+    __device__ inline void st(size_t slot, const T& v) const {
+        rec_st(reinterpret_cast<T*>(base + slot * Stride), v);
+    }
+#endif
 };
 
 // Wavefront state: per path slot (records above) and per global pixel.
