@@ -89,6 +89,8 @@ struct gb_ctx {
     int refill = 16;                    // idle lanes that trigger a warp refill
     int tri_mode = 0;                   // traversal triangle policy (see gb_tuning)
     int blocks_per_sm = 0;              // resident traversal blocks per SM (0 = occupancy limit)
+    int stack_depth = 32;               // traversal stack entries (24 or 32)
+    int block_threads = 128;            // threads per traversal block (64 or 128)
     int slots = 1 << 20;                // path slots in flight (upper bound)
     int sample_mb = 1024;               // sample buffer budget (chunk size)
     // queue-count snapshots: pinned ring + events (host stays a few iterations ahead)
@@ -964,6 +966,7 @@ int run_chunk(gb_ctx* ctx, int p0, int p1) {
     P.refill = ctx->refill;
     P.tri_mode = ctx->tri_mode;
     P.blocks_per_sm = ctx->blocks_per_sm;
+    P.trav_variant = (ctx->stack_depth == 24 ? 1 : 0) + (ctx->block_threads == 64 ? 2 : 0);
     P.mode = ctx->mode;
     P.textured = 0;
     for (const BatchScene& b : ctx->items)
@@ -1452,6 +1455,8 @@ int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, i
         {&gb_tuning::refill, {8, 16, 24, 32}},
         {&gb_tuning::tri_mode, {1, 2, 3, 4}},
         {&gb_tuning::blocks_per_sm, {1, 3, 4, 5, 6}},
+        {&gb_tuning::stack_depth, {24, 32}},
+        {&gb_tuning::block_threads, {64, 128}},
     };
     for (int pass = 0; pass < 2; ++pass) {
         bool changed = false;
@@ -1463,6 +1468,7 @@ int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, i
                 gb_ctx_set_tuning(ctx, &t);
                 double ms = 0.0;
                 rc = tune_trial(ctx, v, repeats, &ms);
+                if (rc == GB_ERR_TRAVERSAL) continue;  // e.g. a stack too shallow for a tree: not a candidate
                 if (rc != GB_OK) {
                     gb_ctx_set_tuning(ctx, &cur);
                     return rc;
@@ -1568,7 +1574,13 @@ int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* t) {
     if (t->graph < 0 || t->graph > 2) return fail(ctx, GB_ERR_INVALID, "graph must be 1 or 2 (0 keeps)");
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 65)
         return fail(ctx, GB_ERR_INVALID, "blocks_per_sm must be 1..65 (0 keeps)");
+    if (t->stack_depth != 0 && t->stack_depth != 24 && t->stack_depth != 32)
+        return fail(ctx, GB_ERR_INVALID, "stack_depth must be 24 or 32 (0 keeps)");
+    if (t->block_threads != 0 && t->block_threads != 64 && t->block_threads != 128)
+        return fail(ctx, GB_ERR_INVALID, "block_threads must be 64 or 128 (0 keeps)");
     if (t->blocks_per_sm) ctx->blocks_per_sm = t->blocks_per_sm - 1;
+    if (t->stack_depth) ctx->stack_depth = t->stack_depth;
+    if (t->block_threads) ctx->block_threads = t->block_threads;
     if (t->tri_mode) ctx->tri_mode = t->tri_mode - 1;
     if (t->graph) ctx->use_graph = t->graph == 2;
     if (t->refill) ctx->refill = t->refill;
@@ -1585,6 +1597,8 @@ int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* t) {
     t->tri_mode = ctx->tri_mode + 1;
     t->graph = ctx->use_graph ? 2 : 1;
     t->blocks_per_sm = ctx->blocks_per_sm + 1;
+    t->stack_depth = ctx->stack_depth;
+    t->block_threads = ctx->block_threads;
     return GB_OK;
 }
 

@@ -312,7 +312,7 @@ __device__ __forceinline__ bool tri_step(const float4* __restrict__ tris, const 
 // node_step (current triangle group empty): one node of the current node
 // group, or a stack pop.  Returns true when the ray is finished; the result
 // is the (t, id)-minimum in s (any-hit: best_id != none when found).
-template <bool INSTR>
+template <bool INSTR, int STACK = kStack>
 __device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, const RayInv& r, float tmax, Trav& s,
                                           const StackRef& stack, uint32_t* status, uint32_t* nvis) {
     if (s.ng.y > 0x00ffffffu) {
@@ -322,7 +322,7 @@ __device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, cons
         uint32_t imask = s.ng.y & 0xffu;
         uint32_t child = s.ng.x + (uint32_t)__popc(imask & ((1u << slot) - 1u));
         if (s.ng.y > 0x00ffffffu) {
-            if (s.sp >= kStack) { atomicOr(status, ST_STACK_OVERFLOW); return true; }
+            if (s.sp >= STACK) { atomicOr(status, ST_STACK_OVERFLOW); return true; }
             stack_put(stack, s.sp++, s.ng);
         }
         if (INSTR) ++*nvis;
@@ -339,13 +339,13 @@ __device__ __forceinline__ bool node_step(const float4* __restrict__ nodes, cons
 }
 
 // Whole traversal of one ray without warp cooperation.
-template <bool ANY, bool INSTR>
+template <bool ANY, bool INSTR, int STACK = kStack>
 __device__ __forceinline__ bool trav_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                           const RayInv& r, float tmax, Trav& s, const StackRef& stack, uint32_t* status,
                                           uint32_t* nvis, uint32_t* ntri) {
     while (s.tg.y != 0u)
         if (tri_step<ANY, INSTR>(tris, r, tmax, s, ntri)) return true;
-    return node_step<INSTR>(nodes, r, tmax, s, stack, status, nvis);
+    return node_step<INSTR, STACK>(nodes, r, tmax, s, stack, status, nvis);
 }
 
 struct TraceOut {
@@ -832,7 +832,7 @@ __device__ __forceinline__ bool coop_triangles(bool act, const float4* tris, con
 // wave is assigned by warp index (warp w takes entries [32w, 32w+32)); later
 // fetches take one atomic per warp on `head`.  Each lane carries the
 // geometry of its own scene.
-template <bool ANY, bool INSTR, int MODE, typename Fetch, typename Finish>
+template <bool ANY, bool INSTR, int MODE, int STACK, int BT, typename Fetch, typename Finish>
 __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int refill, uint32_t* status, Fetch fetch,
                                          Finish finish, uint32_t* nvis, uint32_t* ntri) {
     const uint32_t lane = lane_id();
@@ -845,13 +845,13 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
     RayInv r;
     float tmax = 0.0f;
     Trav s;
-    __shared__ uint2 s_stack[kSmemStack > 0 ? kSmemStack * kBlock : 1];
-    uint2 deep[kStack - kSmemStack];
-    const StackRef stack{s_stack + threadIdx.x, deep, kBlock};
+    __shared__ uint2 s_stack[kSmemStack > 0 ? kSmemStack * BT : 1];
+    uint2 deep[STACK - kSmemStack];
+    const StackRef stack{s_stack + threadIdx.x, deep, BT};
     const float4* nodes = nullptr;
     const float4* tris = nullptr;
     const float4* shade = nullptr;
-    __shared__ unsigned long long s_key[MODE == 3 ? kBlock : 1];
+    __shared__ unsigned long long s_key[MODE == 3 ? BT : 1];
     unsigned long long* skey = s_key + (MODE == 3 ? (threadIdx.x & ~31u) : 0u);
     while (true) {
         finish(fin, qi, s);
@@ -896,14 +896,14 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
                 bool hit = coop_triangles<ANY, INSTR>(act, tris, shade, r, tmax, s, skey, ntri);
                 if (ANY && act && hit) { act = false; fin = true; }
                 if (act) {
-                    bool done = node_step<INSTR>(nodes, r, tmax, s, stack, status, nvis);
+                    bool done = node_step<INSTR, STACK>(nodes, r, tmax, s, stack, status, nvis);
                     if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
                     if (done) { act = false; fin = true; }
                 }
             } else if (MODE == 0) {
                 // every pending triangle, then one node
                 if (act) {
-                    bool done = trav_step<ANY, INSTR>(nodes, tris, r, tmax, s, stack, status, nvis, ntri);
+                    bool done = trav_step<ANY, INSTR, STACK>(nodes, tris, r, tmax, s, stack, status, nvis, ntri);
                     if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
                     if (done) { act = false; fin = true; }
                 }
@@ -917,7 +917,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
                 const uint32_t mt = __ballot_sync(0xffffffffu, want_tri);
                 const uint32_t ma = __ballot_sync(0xffffffffu, act);
                 bool do_tri = want_tri;
-                if (want_tri && 5u * (uint32_t)__popc(mt) < (uint32_t)__popc(ma) && s.sp < kStack) {
+                if (want_tri && 5u * (uint32_t)__popc(mt) < (uint32_t)__popc(ma) && s.sp < STACK) {
                     stack_put(stack, s.sp++, s.tg);
                     s.tg.y = 0u;
                     do_tri = false;
@@ -929,7 +929,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
                         else
                             while (s.tg.y != 0u && !done) done = tri_step<ANY, INSTR>(tris, r, tmax, s, ntri);
                     } else {
-                        done = node_step<INSTR>(nodes, r, tmax, s, stack, status, nvis);
+                        done = node_step<INSTR, STACK>(nodes, r, tmax, s, stack, status, nvis);
                     }
                     if (!done && ++iters > kIterLimit) { atomicOr(status, ST_ITER_LIMIT); done = true; }
                     if (done) { act = false; fin = true; }
@@ -983,8 +983,10 @@ __device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, ui
     F.rnd.st(slot, make_float4(rnd.x, rnd.y, rnd.z, 0.0f));
 }
 
-template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, RenderParams P) {
+// STACK: traversal stack entries; BT: threads per block (the register
+// budget stays that of GB_TRAV_MIN_BLOCKS blocks of 128 threads).
+template <bool INSTR, int MODE, int STACK, int BT>
+__global__ void __launch_bounds__(BT, GB_TRAV_MIN_BLOCKS * 128 / BT) k_extend(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     uint32_t* cn = ctr_set(F, it + 1);
@@ -1033,7 +1035,7 @@ __global__ void __launch_bounds__(kBlock, GB_TRAV_MIN_BLOCKS) k_extend(Frame F, 
         push(fin && hit, slot, qsh, cs + 2);
         end_paths(F, ended, slot, cn);
     };
-    ray_loop<false, INSTR, MODE>(count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
+    ray_loop<false, INSTR, MODE, STACK, BT>(count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[3], nvis); add_stats(&F.stats[4], ntri); }
 }
 
@@ -1051,8 +1053,8 @@ __global__ void __launch_bounds__(kBlock) k_nee(Frame F, int mode) {
 }
 
 // Any-hit of the shadow queue; the result goes to sh_d.w (1 = occluded).
-template <bool INSTR, int MODE>
-__global__ void __launch_bounds__(kBlock, GB_SHADOW_MIN_BLOCKS) k_shadow(Frame F, RenderParams P) {
+template <bool INSTR, int MODE, int STACK, int BT>
+__global__ void __launch_bounds__(BT, GB_SHADOW_MIN_BLOCKS * 128 / BT) k_shadow(Frame F, RenderParams P) {
     const int it = *F.iter;
     uint32_t* cs = ctr_set(F, it);
     const uint32_t count = cs[2];
@@ -1079,8 +1081,8 @@ __global__ void __launch_bounds__(kBlock, GB_SHADOW_MIN_BLOCKS) k_shadow(Frame F
             rec_st(reinterpret_cast<float*>(&F.sh_d[slot]) + 3, occl ? 1.0f : 0.0f);
         }
     };
-    ray_loop<true, INSTR, MODE>(count, cs + 3, GB_SHADOW_REFILL > 0 ? GB_SHADOW_REFILL : P.refill, F.status, fetch,
-                                finish, &nvis, &ntri);
+    ray_loop<true, INSTR, MODE, STACK, BT>(count, cs + 3, GB_SHADOW_REFILL > 0 ? GB_SHADOW_REFILL : P.refill,
+                                           F.status, fetch, finish, &nvis, &ntri);
     if (INSTR) { add_stats(&F.stats[5], nvis); add_stats(&F.stats[6], ntri); }
     if (GB_FUSED_RESTART && P.mode != MODE_ADJOINT) restart_misses(F, P);
 }
@@ -1588,11 +1590,11 @@ struct Grid {
 };
 
 template <typename K>
-Grid persistent_grid(K kernel) {
+Grid persistent_grid(K kernel, int block = kBlock) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0);
     if (sms < 1) sms = 1;
     if (per < 1) per = 1;
     return Grid{sms, per};
@@ -1605,9 +1607,11 @@ int persistent_blocks(K kernel) {
 }
 
 // Grid of a persistent traversal kernel: every SM holds min(occupancy
-// limit, blocks_per_sm) blocks (all it can hold when blocks_per_sm is 0).
-inline int traversal_grid(const Grid& g, int blocks_per_sm) {
-    return g.sms * (blocks_per_sm > 0 ? std::min(g.per, blocks_per_sm) : g.per);
+// limit, blocks_per_sm) blocks (all it can hold when blocks_per_sm is 0);
+// blocks_per_sm counts 128-thread blocks, so blocks of bt threads scale it.
+inline int traversal_grid(const Grid& g, int blocks_per_sm, int bt = kBlock) {
+    const int want = blocks_per_sm > 0 ? std::max(1, blocks_per_sm * kBlock / bt) : g.per;
+    return g.sms * std::min(g.per, want);
 }
 
 }  // namespace
@@ -1640,20 +1644,38 @@ cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cu
     return cudaGetLastError();
 }
 
+template <bool INSTR, int MODE, int STACK, int BT>
+void launch_extend_v(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    static Grid g = persistent_grid(k_extend<INSTR, MODE, STACK, BT>, BT);
+    k_extend<INSTR, MODE, STACK, BT><<<traversal_grid(g, P.blocks_per_sm, BT), BT, 0, st>>>(F, P);
+}
+
+// The default triangle policy has variants for two stack depths and two
+// block shapes (RenderParams::trav_variant), the other policies one each.
 template <bool INSTR, int MODE>
 void launch_extend_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
-    static Grid g = persistent_grid(k_extend<INSTR, MODE>);
-    k_extend<INSTR, MODE><<<traversal_grid(g, P.blocks_per_sm), kBlock, 0, st>>>(F, P);
+    if (MODE == 0 && P.trav_variant == 1) launch_extend_v<INSTR, MODE, 24, 128>(F, P, st);
+    else if (MODE == 0 && P.trav_variant == 2) launch_extend_v<INSTR, MODE, 32, 64>(F, P, st);
+    else if (MODE == 0 && P.trav_variant == 3) launch_extend_v<INSTR, MODE, 24, 64>(F, P, st);
+    else launch_extend_v<INSTR, MODE, kStack, kBlock>(F, P, st);
     if (GB_SPLIT_NEE) {
         static int gn = persistent_blocks(k_nee);
         k_nee<<<gn, kBlock, 0, st>>>(F, P.mode);
     }
 }
 
+template <bool INSTR, int MODE, int STACK, int BT>
+void launch_shadow_v(const Frame& F, const RenderParams& P, cudaStream_t st) {
+    static Grid g = persistent_grid(k_shadow<INSTR, MODE, STACK, BT>, BT);
+    k_shadow<INSTR, MODE, STACK, BT><<<traversal_grid(g, P.blocks_per_sm, BT), BT, 0, st>>>(F, P);
+}
+
 template <bool INSTR, int MODE>
 void launch_shadow_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
-    static Grid g = persistent_grid(k_shadow<INSTR, MODE>);
-    k_shadow<INSTR, MODE><<<traversal_grid(g, P.blocks_per_sm), kBlock, 0, st>>>(F, P);
+    if (MODE == 0 && P.trav_variant == 1) launch_shadow_v<INSTR, MODE, 24, 128>(F, P, st);
+    else if (MODE == 0 && P.trav_variant == 2) launch_shadow_v<INSTR, MODE, 32, 64>(F, P, st);
+    else if (MODE == 0 && P.trav_variant == 3) launch_shadow_v<INSTR, MODE, 24, 64>(F, P, st);
+    else launch_shadow_v<INSTR, MODE, kStack, kBlock>(F, P, st);
 }
 
 cudaError_t k_launch_extend(const Frame& F, const RenderParams& P, bool instrument, cudaStream_t st) {

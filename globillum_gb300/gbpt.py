@@ -99,7 +99,7 @@ class RenderDesc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("refill", C.c_int), ("slots", C.c_int), ("sample_mb", C.c_int), ("tri_mode", C.c_int),
-                ("graph", C.c_int), ("blocks_per_sm", C.c_int)]
+                ("graph", C.c_int), ("blocks_per_sm", C.c_int), ("stack_depth", C.c_int), ("block_threads", C.c_int)]
 
 
 class BatchItem(C.Structure):
@@ -325,8 +325,8 @@ class Context:
         return d
 
     def set_tuning(self, refill: int = 0, slots: int = 0, sample_mb: int = 0, tri_mode: int = 0, graph: int = 0,
-                   blocks_per_sm: int = 0):
-        t = Tuning(refill, slots, sample_mb, tri_mode, graph, blocks_per_sm)
+                   blocks_per_sm: int = 0, stack_depth: int = 0, block_threads: int = 0):
+        t = Tuning(refill, slots, sample_mb, tri_mode, graph, blocks_per_sm, stack_depth, block_threads)
         self.check(self.lib.gb_ctx_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self) -> dict:

@@ -456,17 +456,24 @@ typedef struct {
                        chunk runs as one CUDA graph with a conditional while loop (default) */
     int blocks_per_sm; /* resident 128-thread blocks per SM of the persistent traversal
                           kernels + 1: 1 = as many as occupancy allows, k + 1 = at most k */
+    int stack_depth;   /* node-group stack entries of the traversal kernels: 24 or 32
+                          (default 32; the reference's tracers keep 32, tracers.cu:55).  A
+                          ray that needs more ends the render with GB_ERR_TRAVERSAL */
+    int block_threads; /* threads per block of the traversal kernels: 64 or 128 (default;
+                          the reference launches 16x16 blocks).  stack_depth and
+                          block_threads apply to triangle policy 1; the others run 32 / 128 */
 } gb_tuning;
 int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* tuning);
 int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* tuning);
 
 /* Autotuner of the wavefront knobs (gb_tuning: graph capture, slot-pool
  * capacity, refill threshold, triangle policy, resident traversal blocks per
- * SM) for a batch (or one scene, n = 1): coordinate descent from the
+ * SM, traversal stack depth and block shape) for a batch (or one scene, n = 1): coordinate descent from the
  * context's current tuning, two passes at most, each candidate timed as the
  * median device time of `repeats` frames after a warm-up frame.  With
  * proxy_spp > 0 every scene renders min(spp, proxy_spp) samples per trial
- * (a cheaper frame of the same layout).  Leaves the best tuning set on the
+ * (a cheaper frame of the same layout).  A candidate whose frame fails (a
+ * traversal stack too shallow for a tree) is skipped.  Leaves the best tuning set on the
  * context and returns it with its frame time; out_rgb of the items is not
  * used.  The reference has no tunable launch parameters; no counterpart. */
 int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, int repeats,

@@ -77,7 +77,8 @@ def test_struct_layouts_match_the_header(tmp_path):
              "gb_adjoint_item": gbpt.AdjointItem, "gb_build_options": gbpt.BuildOptions,
              "gb_texture": gbpt.Texture, "gb_bvh_stats": gbpt.BvhStats}
     c_fields = {"gb_batch_item": ["scene", "camera", "desc", "out_rgb"],
-                "gb_tuning": ["refill", "slots", "sample_mb", "tri_mode", "graph", "blocks_per_sm"],
+                "gb_tuning": ["refill", "slots", "sample_mb", "tri_mode", "graph", "blocks_per_sm", "stack_depth",
+                              "block_threads"],
                 "gb_render_desc": ["width", "height", "spp", "max_bounces", "rng_mode", "seed", "ray_offset",
                                    "shadow_offset", "background", "rr_start"],
                 "gb_scene_info": ["build_ms", "device_bytes", "overall_light_power", "builder", "build_passes"],

@@ -139,7 +139,8 @@ def test_autotune_keeps_images(gpu_ctx):
         best, ms = gpu_ctx.autotune(hj, proxy_spp=2, repeats=1)
         assert ms > 0.0
         assert best == gpu_ctx.get_tuning()
-        assert best["graph"] in (1, 2) and 1 <= best["tri_mode"] <= 3 and 1 <= best["refill"] <= 32
+        assert best["graph"] in (1, 2) and 1 <= best["tri_mode"] <= 4 and 1 <= best["refill"] <= 32
+        assert best["stack_depth"] in (24, 32) and best["block_threads"] in (64, 128)
         got = gpu_ctx.render_batch(hj, graph=None)
         for r, g in zip(ref, got):
             assert np.array_equal(r, g)

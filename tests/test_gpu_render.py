@@ -214,3 +214,28 @@ def test_triangle_policies_agree(gpu_ctx):
     for im in imgs[1:]:
         assert np.array_equal(imgs[0], im)
     s.close()
+
+
+def test_traversal_stack_and_block_variants_agree(gpu_ctx):
+    """The traversal kernels built for 24 or 32 stack entries and 64- or
+    128-thread blocks (gb_tuning stack_depth / block_threads) render the same
+    frame bit for bit, here on a tree of depth 10+ (a stack of 24 entries
+    suffices for it; a shallower tree never needs more than its depth
+    plus the postponed triangle groups)."""
+    sc = scenes.icospheres(n_spheres=300, level=3, box=50.0, width=96, height=54, spp=3, max_bounces=6, rr_start=3)
+    s = gpu_ctx.scene(sc)
+    old = gpu_ctx.get_tuning()
+    imgs = []
+    try:
+        for stack, block in ((32, 128), (24, 128), (32, 64), (24, 64)):
+            gpu_ctx.set_tuning(stack_depth=stack, block_threads=block)
+            t = gpu_ctx.get_tuning()
+            assert (t["stack_depth"], t["block_threads"]) == (stack, block)
+            imgs.append(s.render(sc.camera, sc.render))
+    finally:
+        gpu_ctx.set_tuning(stack_depth=old["stack_depth"], block_threads=old["block_threads"])
+    for im in imgs[1:]:
+        assert np.array_equal(imgs[0], im)
+    with pytest.raises(gbpt.GBError, match="stack_depth"):
+        gpu_ctx.set_tuning(stack_depth=16)
+    s.close()
