@@ -475,11 +475,12 @@ def inverse_leg(ctx, args, torch, dist):
     scene's 64 materials (base colour, roughness, metallic) are recovered
     from a target rendered with hidden seeded parameters: Adam (lr 1e-2) on
     the summed L2 image losses, starting from the scenes' own seeded
-    materials.  One iteration = parameters uploaded, one batched forward
-    frame (gb_render_batch) and one batched adjoint frame
-    (gb_backward_batch), each run as CUDA-graph chunks.  The same iteration
-    is also timed as 16 sequential plain runs (gb_render + gb_backward per
-    scene)."""
+    materials.  One iteration = one gb_fit_step: a single CUDA graph launch
+    that uploads the parameters, renders the batched forward frame, forms
+    the losses and image gradients on the device and runs the batched
+    adjoint; the host applies the parameter Jacobian and Adam.  The same
+    iteration is also timed as 16 sequential plain runs (gb_render +
+    gb_backward per scene, image gradients through the host)."""
     from globillum_gb300 import scenes
     n_sc = 16
     mixed = scenes.mixed_set(n_sc, seed=77, tri_range=(10_000, 200_000), resolutions=(256,), spp_choices=(8,),
@@ -524,17 +525,16 @@ def inverse_leg(ctx, args, torch, dist):
     visible = None
     losses = []
     t_iter = []
+    # one fitting step = one CUDA graph launch: parameter upload, batched
+    # forward frame, L2 loss and image gradient on the device, batched
+    # adjoint, gradient reduction (gb_fit_step)
+    ctx.fit_prepare(jobs, [t.data_ptr() for t in targets], ptrs)
     for it in range(args.inverse_iters):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for h, x in zip(handles, xs_t):
-            h.set_params(x.detach().numpy())
-        ctx.render_batch_device(jobs, ptrs, graph=True)
-        dimgs = [(2.0 * (o - t)).contiguous() for o, t in zip(outs, targets)]
-        g = ctx.backward_batch(jobs, [d.cpu().numpy() for d in dimgs], graph=True)
-        torch.cuda.synchronize()
+        g, lv = ctx.fit_step([x.detach().numpy() for x in xs_t])
         t_iter.append(time.perf_counter() - t0)
-        losses.append(float(sum(((o - t) ** 2).sum().item() for o, t in zip(outs, targets))))
+        losses.append(float(lv.sum()))
         if visible is None:
             # materials that influence their image: colour-gradient norm at the
             # start above 1 % of the scene's largest
@@ -579,7 +579,9 @@ def inverse_leg(ctx, args, torch, dist):
             "iteration_ms": it_s * 1e3, "sequential_iteration_ms": seq_s * 1e3,
             "batched_over_sequential": seq_s / it_s,
             "mpaths_per_s_fwd_plus_bwd": 2 * paths / it_s / 1e6,
-            "note": "wall-clock per iteration including parameter upload and host gradient copies"}
+            "graph_launches_per_iteration": 1,
+            "note": "wall-clock per iteration: one gb_fit_step (parameter records built on the host, one graph "
+                    "launch, parameter Jacobian on the host); Adam on the host"}
 
 
 def run_gbpt(args, rank, world):

@@ -44,12 +44,35 @@ struct BatchScene {
     const float* dimg = nullptr;
     float* grad_out = nullptr;
     uint32_t grad_base = 0;
+    // fitting step (gb_fit_*): target image (device), image output (device or
+    // null) and the scene's index in the caller's list
+    const float* target = nullptr;
+    float* image = nullptr;
+    int user = 0;
 };
 
 // An instantiated chunk graph and everything it was captured with.
 struct ChunkGraph {
     std::vector<uint64_t> key;
     cudaGraphExec_t exec;
+};
+
+// A prepared fitting step (gb_fit_prepare): the scenes in layout order, the
+// one graph of a step, and the pinned buffers it copies from and to.
+struct FitState {
+    bool ready = false;
+    std::vector<BatchScene> items;      // layout order
+    std::vector<gb_fit_item> user;      // as the caller gave them
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> key;          // device buffers the graph was captured with
+    SceneRec* h_recs = nullptr;         // scene records of the frame
+    float* h_mats = nullptr;            // material records of every scene
+    LightRec* h_lights = nullptr;       // light records of every scene
+    std::vector<size_t> mat_off, light_off;
+    double* h_out = nullptr;            // gradient sums (stride), then one loss per scene
+    double* d_loss = nullptr;
+    int stride = 0, replicas = 0;
+    size_t mats_total = 0, lights_total = 0;
 };
 
 struct gb_ctx {
@@ -106,6 +129,9 @@ struct gb_ctx {
     DevBuf scratch[4];
     float* d_rgb = nullptr;
     size_t rgb_cap = 0;
+    // fitting steps: the loop bodies of the step graph are captured on fit_aux
+    cudaStream_t fit_aux = nullptr;
+    FitState fit;
 };
 
 struct gb_scene {
@@ -352,6 +378,13 @@ void gb_ctx_destroy(gb_ctx* ctx) {
     free_all(ctx->pixel_allocs);
     free_all(ctx->sample_allocs);
     for (ChunkGraph& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    if (ctx->fit.exec) cudaGraphExecDestroy(ctx->fit.exec);
+    if (ctx->fit.h_recs) cudaFreeHost(ctx->fit.h_recs);
+    if (ctx->fit.h_mats) cudaFreeHost(ctx->fit.h_mats);
+    if (ctx->fit.h_lights) cudaFreeHost(ctx->fit.h_lights);
+    if (ctx->fit.h_out) cudaFreeHost(ctx->fit.h_out);
+    if (ctx->fit.d_loss) cudaFree(ctx->fit.d_loss);
+    if (ctx->fit_aux) cudaStreamDestroy(ctx->fit_aux);
     free_all(ctx->adj_allocs);
     if (ctx->d_scenes) cudaFree(ctx->d_scenes);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
@@ -723,6 +756,32 @@ int chunk_end(const gb_ctx* ctx, int p0, int end, long long* paths) {
     return p1;
 }
 
+// The device part of starting a frame, on stream `st`: counters, the scene
+// records (copied from `recs`, ctx->recs.size() of them), the layout's
+// initial RNG states when the layout changed, and both stream cursors of
+// every pixel reset to them.  Captured into the fitting graph as well.
+int enqueue_frame_setup(gb_ctx* ctx, cudaStream_t st, const SceneRec* recs, bool record_start) {
+    const Frame& F = ctx->F;
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * 8, st));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), st));
+    if (record_start) CK(cudaEventRecord(ctx->ev0, st));
+    CK(cudaMemcpyAsync(ctx->d_scenes, recs, sizeof(SceneRec) * ctx->recs.size(), cudaMemcpyHostToDevice, st));
+    // F.pscene and the initial RNG states depend on the pixel counts, their
+    // order and the seeds only
+    std::vector<uint64_t> key;
+    key.push_back((uint64_t)F.ntot);
+    for (const BatchScene& b : ctx->items) key.push_back(((uint64_t)b.desc.seed << 32) | (uint32_t)b.n);
+    if (key != ctx->pristine_key) {
+        CK(k_launch_frame_init(F, true, st));
+        ctx->launches += 2;
+        ctx->pristine_key = key;
+    }
+    // both streams of every pixel restart at curand_init(seed, pixel, 0)
+    CK(cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)F.ntot, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(F.jcursor, F.pristine, sizeof(MrgState) * (size_t)F.ntot, cudaMemcpyDeviceToDevice, st));
+    return GB_OK;
+}
+
 // Lays out the scenes of a render (one scene, or a batch) in HBM and starts
 // it: scene records, pixel ranges, RNG streams.
 int begin_frame(gb_ctx* ctx, std::vector<BatchScene>& items) {
@@ -784,24 +843,8 @@ int begin_frame(gb_ctx* ctx, std::vector<BatchScene>& items) {
     ctx->paths_done = 0;
     ctx->launches = 0;
     ctx->ev_used = 0;
-    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * 8, ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
-    CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_scenes, ctx->recs.data(), sizeof(SceneRec) * ctx->recs.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    // F.pscene and the initial RNG states depend on the pixel counts, their
-    // order and the seeds only
-    std::vector<uint64_t> key;
-    key.push_back((uint64_t)ntot);
-    for (const BatchScene& b : ctx->items) key.push_back(((uint64_t)b.desc.seed << 32) | (uint32_t)b.n);
-    if (key != ctx->pristine_key) {
-        CK(k_launch_frame_init(F, true, ctx->stream));
-        ctx->launches += 2;
-        ctx->pristine_key = key;
-    }
-    // both streams of every pixel restart at curand_init(seed, pixel, 0)
-    CK(cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(F.jcursor, F.pristine, sizeof(MrgState) * (size_t)ntot, cudaMemcpyDeviceToDevice, ctx->stream));
+    int rc = enqueue_frame_setup(ctx, ctx->stream, ctx->recs.data(), true);
+    if (rc != GB_OK) return rc;
     ctx->active = true;
     return GB_OK;
 }
@@ -939,6 +982,50 @@ int build_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_it
     return GB_OK;
 }
 
+// The same chunk appended to the capture in progress on stream `a`; the
+// loop body is captured on stream `b` while `a` keeps capturing.
+int append_chunk(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters, cudaStream_t a, cudaStream_t b) {
+    const Frame& F = ctx->F;
+    cudaError_t e = cudaMemsetAsync(F.ctr, 0, sizeof(uint32_t) * 24, a);
+    if (e == cudaSuccess) e = k_launch_jitter_pool(F, P, a);
+    if (e == cudaSuccess) e = k_launch_start(F, P, nstart, a);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(a, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    cudaGraphConditionalHandle h = 0;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np{};
+    cudaGraphNode_t loop = nullptr;
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&loop, cg, deps, nullptr, nd, &np);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(a, &loop, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) {
+        e = cudaStreamBeginCaptureToGraph(b, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            e = k_launch_extend(F, P, ctx->instrument, b);
+            if (e == cudaSuccess) e = k_launch_shadow(F, P, ctx->instrument, b);
+            if (e == cudaSuccess) e = k_launch_shade(F, P, b);
+            if (e == cudaSuccess && P.mode == MODE_ADJOINT) e = k_launch_adjoint(F, P, b);
+            if (e == cudaSuccess) e = k_launch_regen(F, P, b);
+            if (e == cudaSuccess) e = k_launch_step(F, P, (unsigned long long)h, true, max_iters, b);
+            cudaGraph_t body_out = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(b, &body_out);
+            if (e == cudaSuccess) e = e2;
+        }
+    }
+    if (e == cudaSuccess) e = k_launch_combine(F, P, a);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "step graph chunk");
+    return GB_OK;
+}
+
 int run_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iters) {
     std::vector<uint64_t> key = graph_key(ctx, P, nstart, max_iters);
     size_t hit = ctx->graphs.size();
@@ -960,8 +1047,9 @@ int run_chunk_graph(gb_ctx* ctx, const RenderParams& P, int nstart, int max_iter
     return GB_OK;
 }
 
-// Rounds [p0, p1) of every pixel that takes them, through the slot pool.
-int run_chunk(gb_ctx* ctx, int p0, int p1) {
+// Launch parameters of the chunk of rounds [p0, p1): sets the frame's slot
+// count and returns the paths started first and the iteration bound.
+void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out, int* max_iters_out) {
     RenderParams P{};
     P.refill = ctx->refill;
     P.tri_mode = ctx->tri_mode;
@@ -992,6 +1080,16 @@ int run_chunk(gb_ctx* ctx, int p0, int p1) {
     const long long L1 = ctx->max_L + 1;
     const int max_iters =
         (int)std::min<long long>(1ll << 30, 2 * ((acc * L1 + F.nslots - 1) / F.nslots + L1) + 16);
+    *out = P;
+    *nstart_out = nstart;
+    *max_iters_out = max_iters;
+}
+
+// Rounds [p0, p1) of every pixel that takes them, through the slot pool.
+int run_chunk(gb_ctx* ctx, int p0, int p1) {
+    RenderParams P{};
+    int nstart = 0, max_iters = 0;
+    make_chunk(ctx, p0, p1, &P, &nstart, &max_iters);
     if (ctx->use_graph && !ctx->stage_timing) return run_chunk_graph(ctx, P, nstart, max_iters);
     return run_chunk_loop(ctx, P, nstart, max_iters);
 }
@@ -1012,8 +1110,8 @@ int step_frame(gb_ctx* ctx, int paths) {
     return GB_OK;
 }
 
-// Packs the frame's colours into RGB triples (device scratch of 3 * ntot floats).
-int pack_frame(gb_ctx* ctx) {
+// The packed-colour scratch for the frame (3 * ntot floats).
+int ensure_rgb(gb_ctx* ctx) {
     const size_t bytes = sizeof(float) * 3 * (size_t)ctx->F.ntot;
     if (ctx->rgb_cap < bytes) {
         CK(cudaStreamSynchronize(ctx->stream));
@@ -1024,6 +1122,13 @@ int pack_frame(gb_ctx* ctx) {
         CK(dalloc(tmp, (void**)&ctx->d_rgb, bytes));
         ctx->rgb_cap = bytes;
     }
+    return GB_OK;
+}
+
+// Packs the frame's colours into RGB triples (device scratch of 3 * ntot floats).
+int pack_frame(gb_ctx* ctx) {
+    int rc = ensure_rgb(ctx);
+    if (rc != GB_OK) return rc;
     if (ctx->paths_done == 0) CK(cudaMemsetAsync(ctx->F.out, 0, sizeof(float4) * (size_t)ctx->F.ntot, ctx->stream));
     CK(k_launch_pack_rgb(ctx->F.out, ctx->F.ntot, ctx->d_rgb, ctx->stream));
     ctx->launches += 1;
@@ -1402,6 +1507,263 @@ int gb_backward(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam, const gb_ren
     it.dL_dimg = dL_dimg;
     it.dL_dparams = dL_dparams;
     return gb_backward_batch(ctx, 1, &it, dimg_is_device, -1);
+}
+
+namespace {
+
+// Device buffers and launch knobs a fitting graph was captured with; a
+// change (another render grew the frame, a new tuning) means a new graph.
+std::vector<uint64_t> fit_key(const gb_ctx* ctx) {
+    const Frame& F = ctx->F;
+    std::vector<uint64_t> k;
+    const void* ptrs[] = {ctx->d_scenes, F.slots, F.shadow, F.q[0], F.q[1], F.q[2], F.q[3], F.out, F.pristine,
+                          F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr, F.iter, F.stats,
+                          F.status, F.adj, F.dimg, F.grad, ctx->d_gsum, ctx->d_rgb, ctx->fit.d_loss};
+    for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
+    k.push_back(((uint64_t)ctx->slot_cap << 32) ^ (uint64_t)ctx->sample_cap);
+    k.push_back(((uint64_t)(uint32_t)ctx->slots << 32) | (uint32_t)ctx->sample_mb);
+    k.push_back(((uint64_t)(uint32_t)ctx->refill << 32) | (uint32_t)ctx->tri_mode);
+    k.push_back(((uint64_t)(uint32_t)ctx->blocks_per_sm << 32) | (uint32_t)(ctx->stack_depth * 1000 + ctx->block_threads));
+    for (const gb_fit_item& u : ctx->fit.user)
+        k.push_back((uint64_t)(uintptr_t)u.scene->S.mats ^ ((uint64_t)(uintptr_t)u.scene->S.lights << 1));
+    return k;
+}
+
+cudaError_t host_buf(void** p, size_t* cap, size_t bytes) {
+    if (bytes <= *cap && *p) return cudaSuccess;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaHostAlloc(p, std::max<size_t>(bytes, 16), cudaHostAllocDefault);
+    if (e == cudaSuccess) *cap = bytes;
+    return e;
+}
+
+// Lays the fitting frame out (an ordinary start of the forward frame: scene
+// order, buffers, the layout's initial RNG states), allocates everything a
+// step touches, and captures the step graph on the context's capture
+// streams.
+int fit_build(gb_ctx* ctx) {
+    FitState& f = ctx->fit;
+    f.ready = false;
+    if (f.exec) { cudaGraphExecDestroy(f.exec); f.exec = nullptr; }
+    std::vector<BatchScene> v(f.user.size());
+    uint32_t gtot = 0;
+    for (size_t i = 0; i < f.user.size(); ++i) {
+        const gb_fit_item& u = f.user[i];
+        v[i].scene = u.scene;
+        v[i].cam = u.camera;
+        v[i].desc = u.desc;
+        v[i].target = u.target;
+        v[i].image = u.image;
+        v[i].user = (int)i;
+        v[i].grad_base = gtot;
+        gtot += (uint32_t)grad_floats(u.scene);
+    }
+    CK(cudaSetDevice(ctx->device));
+    ctx->mode = MODE_FORWARD;
+    int rc = begin_frame(ctx, v);
+    ctx->active = false;
+    if (rc != GB_OK) return rc;
+    f.items = ctx->items;
+    Frame& F = ctx->F;
+    f.replicas = k_adjoint_grid();
+    f.stride = (int)std::max<uint32_t>(1, gtot);
+    const size_t ns = f.items.size();
+    cudaError_t e = ensure_buf(ctx, (void**)&F.adj, &ctx->adj_cap,
+                               sizeof(float4) * kAdjPlanes * (size_t)ctx->max_L * ctx->slot_cap);
+    if (e == cudaSuccess) e = ensure_buf(ctx, (void**)&F.dimg, &ctx->dimg_cap, sizeof(float4) * (size_t)F.ntot);
+    if (e == cudaSuccess)
+        e = ensure_buf(ctx, (void**)&F.grad, &ctx->grad_cap, sizeof(float) * (size_t)f.replicas * (size_t)f.stride);
+    if (e == cudaSuccess) e = ensure_buf(ctx, (void**)&ctx->d_gsum, &ctx->gsum_cap, sizeof(double) * (size_t)f.stride);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fitting buffers");
+    rc = ensure_rgb(ctx);
+    if (rc != GB_OK) return rc;
+    if (f.d_loss) { cudaFree(f.d_loss); f.d_loss = nullptr; }
+    std::vector<void*> tmp;
+    CK(dalloc(tmp, (void**)&f.d_loss, sizeof(double) * ns));
+    f.mat_off.assign(ns, 0);
+    f.light_off.assign(ns, 0);
+    f.mats_total = f.lights_total = 0;
+    for (size_t k = 0; k < ns; ++k) {
+        f.mat_off[k] = f.mats_total;
+        f.light_off[k] = f.lights_total;
+        f.mats_total += f.items[k].scene->mats.size() * kMaterialFloats;
+        f.lights_total += f.items[k].scene->lights.size();
+    }
+    size_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    if (f.h_recs) { cudaFreeHost(f.h_recs); f.h_recs = nullptr; }
+    if (f.h_mats) { cudaFreeHost(f.h_mats); f.h_mats = nullptr; }
+    if (f.h_lights) { cudaFreeHost(f.h_lights); f.h_lights = nullptr; }
+    if (f.h_out) { cudaFreeHost(f.h_out); f.h_out = nullptr; }
+    CK(host_buf((void**)&f.h_recs, &c0, sizeof(SceneRec) * ns));
+    CK(host_buf((void**)&f.h_mats, &c1, sizeof(float) * f.mats_total));
+    CK(host_buf((void**)&f.h_lights, &c2, sizeof(LightRec) * std::max<size_t>(1, f.lights_total)));
+    CK(host_buf((void**)&f.h_out, &c3, sizeof(double) * ((size_t)f.stride + ns)));
+    std::memcpy(f.h_recs, ctx->recs.data(), sizeof(SceneRec) * ns);
+    F.grad_stride = f.stride;
+    F.grad_replicas = f.replicas;
+    CK(cudaStreamSynchronize(ctx->stream));  // the layout's RNG states are in place
+    if (!ctx->fit_aux) CK(cudaStreamCreateWithFlags(&ctx->fit_aux, cudaStreamNonBlocking));
+    // capture: parameters -> forward frame -> loss and image gradient ->
+    // adjoint frame -> gradient reduction -> results to pinned memory
+    cudaStream_t a = ctx->aux, b = ctx->fit_aux;
+    e = cudaStreamBeginCapture(a, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "step graph capture");
+    rc = GB_OK;
+    for (size_t k = 0; k < ns && rc == GB_OK; ++k) {
+        gb_scene* sc = f.items[k].scene;
+        e = cudaMemcpyAsync((void*)sc->S.mats, f.h_mats + f.mat_off[k], sizeof(float) * sc->mats.size() * kMaterialFloats,
+                            cudaMemcpyHostToDevice, a);
+        if (e == cudaSuccess && !sc->lights.empty())
+            e = cudaMemcpyAsync((void*)sc->S.lights, f.h_lights + f.light_off[k], sizeof(LightRec) * sc->lights.size(),
+                                cudaMemcpyHostToDevice, a);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "step graph parameters");
+    }
+    if (rc == GB_OK) rc = enqueue_frame_setup(ctx, a, f.h_recs, false);
+    for (int pass = 0; pass < 2 && rc == GB_OK; ++pass) {
+        ctx->mode = pass == 0 ? MODE_FORWARD : MODE_ADJOINT;
+        if (pass == 1) {
+            // the adjoint replays the same paths: both streams of every pixel restart
+            e = cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)F.ntot, cudaMemcpyDeviceToDevice, a);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(F.jcursor, F.pristine, sizeof(MrgState) * (size_t)F.ntot, cudaMemcpyDeviceToDevice, a);
+            if (e == cudaSuccess) e = cudaMemsetAsync(F.grad, 0, sizeof(float) * (size_t)f.replicas * (size_t)f.stride, a);
+            if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "step graph adjoint set-up"); break; }
+        }
+        for (int p0 = 0; p0 < ctx->max_spp && rc == GB_OK;) {
+            long long cp = 0;
+            const int p1 = chunk_end(ctx, p0, ctx->max_spp, &cp);
+            RenderParams P{};
+            int nstart = 0, max_iters = 0;
+            make_chunk(ctx, p0, p1, &P, &nstart, &max_iters);
+            rc = append_chunk(ctx, P, nstart, max_iters, a, b);
+            p0 = p1;
+        }
+        if (rc != GB_OK) break;
+        if (pass == 0) {
+            e = k_launch_pack_rgb(F.out, F.ntot, ctx->d_rgb, a);
+            for (size_t k = 0; k < ns && e == cudaSuccess; ++k) {
+                const BatchScene& it = f.items[k];
+                const float* img = ctx->d_rgb + 3 * (size_t)it.base;
+                e = k_launch_l2_loss(img, it.target, it.n, 1.0f / (float)it.desc.spp, F.dimg + it.base, f.d_loss + k, a);
+                if (e == cudaSuccess && it.image)
+                    e = cudaMemcpyAsync(it.image, img, sizeof(float) * 3 * (size_t)it.n, cudaMemcpyDeviceToDevice, a);
+            }
+        } else {
+            e = k_launch_grad_reduce(F.grad, f.replicas, f.stride, ctx->d_gsum, a);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(f.h_out, ctx->d_gsum, sizeof(double) * (size_t)f.stride, cudaMemcpyDeviceToHost, a);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(f.h_out + f.stride, f.d_loss, sizeof(double) * ns, cudaMemcpyDeviceToHost, a);
+        }
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "step graph");
+    }
+    ctx->mode = MODE_FORWARD;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(a, &g);
+    if (rc == GB_OK && e != cudaSuccess) rc = cuda_fail(ctx, e, "step graph capture");
+    if (rc == GB_OK) {
+        e = cudaGraphInstantiate(&f.exec, g, 0);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "step graph instantiation");
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc != GB_OK) return rc;
+    f.key = fit_key(ctx);
+    f.ready = true;
+    return GB_OK;
+}
+
+}  // namespace
+
+int gb_fit_prepare(gb_ctx* ctx, int n, const gb_fit_item* items) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (n <= 0 || n > 1024 || !items) return fail(ctx, GB_ERR_INVALID, "a fitting step takes 1..1024 scenes");
+    for (int i = 0; i < n; ++i) {
+        const gb_fit_item& u = items[i];
+        if (!u.scene || !u.target) return fail(ctx, GB_ERR_INVALID, "null scene or target");
+        if (u.scene->ctx != ctx) return fail(ctx, GB_ERR_INVALID, "scene belongs to another context");
+        if (u.desc.max_bounces > kMaxAdjBounces)
+            return fail(ctx, GB_ERR_INVALID, "the adjoint records at most 16 bounces per path");
+        if (u.scene->S.sky.light >= 0)
+            return fail(ctx, GB_ERR_UNSUPPORTED, "the adjoint covers scenes with rectangular lights only");
+        if (u.scene->S.texcoord) return fail(ctx, GB_ERR_UNSUPPORTED, "the adjoint covers scenes without textures only");
+        for (int j = 0; j < i; ++j)
+            if (items[j].scene == u.scene) return fail(ctx, GB_ERR_INVALID, "a scene appears twice in a fitting step");
+        int rc = check_render_desc(ctx, &u.camera, &u.desc);
+        if (rc != GB_OK) return rc;
+    }
+    ctx->fit.user.assign(items, items + n);
+    return fit_build(ctx);
+}
+
+int gb_fit_step(gb_ctx* ctx, const float* const* params, float* const* dL_dparams, double* loss) {
+    if (!ctx) return GB_ERR_INVALID;
+    FitState& f = ctx->fit;
+    if (f.user.empty()) return fail(ctx, GB_ERR_INVALID, "no fitting step prepared");
+    if (!params || !dL_dparams) return fail(ctx, GB_ERR_INVALID, "null parameter or gradient list");
+    const size_t ns = f.user.size();
+    for (size_t i = 0; i < ns; ++i) {
+        if (!params[i] || !dL_dparams[i]) return fail(ctx, GB_ERR_INVALID, "null parameter or gradient vector");
+        if (!all_finite(params[i], param_count(f.user[i].scene))) return fail(ctx, GB_ERR_INVALID, "non-finite parameter");
+    }
+    CK(cudaSetDevice(ctx->device));
+    // parameters -> records (host, as gb_scene_set_params); a frame of
+    // another call may still read the scenes' records
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::vector<std::vector<float>> mrecs(ns);
+    std::vector<std::vector<LightRec>> lrecs(ns);
+    std::vector<std::vector<gb_material>> mats(ns);
+    std::vector<std::vector<gb_principled_params>> pars(ns);
+    std::vector<std::vector<gb_light>> lights(ns);
+    for (size_t i = 0; i < ns; ++i) {
+        gb_scene* sc = f.user[i].scene;
+        apply_params(sc, params[i], &mats[i], &pars[i], &lights[i]);
+        build_records(mats[i], pars[i], lights[i], &mrecs[i], &lrecs[i], &sc->mat_dtex);
+        for (const LightRec& l : lrecs[i])
+            if (!(l.power > 0.0f)) return fail(ctx, GB_ERR_INVALID, "light power must be positive");
+    }
+    for (size_t i = 0; i < ns; ++i) {
+        gb_scene* sc = f.user[i].scene;
+        sc->mats.swap(mats[i]);
+        sc->params.swap(pars[i]);
+        sc->lights.swap(lights[i]);
+        sc->S.overall_power = overall_power(lrecs[i].data(), (int)lrecs[i].size());
+        sc->info.overall_light_power = sc->S.overall_power;
+    }
+    if (!f.ready || fit_key(ctx) != f.key) {
+        int rc = fit_build(ctx);
+        if (rc != GB_OK) return rc;
+    }
+    for (size_t k = 0; k < f.items.size(); ++k) {
+        const BatchScene& it = f.items[k];
+        std::memcpy(f.h_mats + f.mat_off[k], mrecs[it.user].data(), sizeof(float) * mrecs[it.user].size());
+        if (!lrecs[it.user].empty())
+            std::memcpy(f.h_lights + f.light_off[k], lrecs[it.user].data(), sizeof(LightRec) * lrecs[it.user].size());
+        f.h_recs[k].S = it.scene->S;  // the light power sum follows the emissions
+    }
+    CK(cudaGraphLaunch(f.exec, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = check_status(ctx);
+    if (rc != GB_OK) return rc;
+    for (size_t k = 0; k < f.items.size(); ++k) {
+        const BatchScene& it = f.items[k];
+        const gb_scene* sc = it.scene;
+        const double* gm = f.h_out + it.grad_base;
+        float* go = dL_dparams[it.user];
+        for (size_t m = 0; m < sc->mats.size(); ++m) {
+            double out[kMatParams];
+            material_param_vjp(sc->mats[m], sc->params.empty() ? nullptr : sc->params.data(), gm + kMatGradFloats * m, out);
+            for (int j = 0; j < kMatParams; ++j) go[kMatParams * m + j] = (float)out[j];
+        }
+        const double* gl = gm + kMatGradFloats * sc->mats.size();
+        float* lo = go + kMatParams * sc->mats.size();
+        for (size_t l = 0; l < sc->lights.size(); ++l)
+            for (int c = 0; c < 3; ++c) lo[kLightParams * l + c] = (float)gl[3 * l + c];
+        if (loss) loss[it.user] = f.h_out[f.stride + k];
+    }
+    return GB_OK;
 }
 
 namespace {

@@ -1452,6 +1452,33 @@ __global__ void k_dimg_pack(const float* __restrict__ src, int n, float scale, f
     dst[i] = make_float4(src[3 * i] * scale, src[3 * i + 1] * scale, src[3 * i + 2] * scale, 0.0f);
 }
 
+// L2 image loss of one scene of a fitting step: loss = sum (x - t)^2 over
+// its n pixels (one block, double accumulation in a fixed order, so the sum
+// is the same every launch) and the adjoint's image gradient
+// dimg = 2 (x - t) * scale (scale = 1 / spp), the same float operations as
+// k_dimg_pack applied to 2 (x - t).
+__global__ void __launch_bounds__(1024) k_l2_loss(const float* __restrict__ img, const float* __restrict__ target,
+                                                  int n, float scale, float4* dimg, double* loss) {
+    __shared__ double part[1024];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float g[3];
+        for (int c = 0; c < 3; ++c) {
+            const float d = img[3 * (size_t)i + c] - target[3 * (size_t)i + c];
+            acc += (double)d * (double)d;
+            g[c] = (2.0f * d) * scale;
+        }
+        dimg[i] = make_float4(g[0], g[1], g[2], 0.0f);
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *loss = part[0];
+}
+
 // Sum of the gradient replicas, in double.
 __global__ void k_grad_reduce(const float* __restrict__ grad, int replicas, int stride, double* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1758,6 +1785,13 @@ cudaError_t k_launch_direct_hybrid(const DevScene& S, const CameraRec& cam, int 
 cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     k_dimg_pack<<<blocks_for(n), kBlock, 0, st>>>(src, n, scale, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t k_launch_l2_loss(const float* img, const float* target, int n, float scale, float4* dimg, double* loss,
+                             cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_l2_loss<<<1, 1024, 0, st>>>(img, target, n, scale, dimg, loss);
     return cudaGetLastError();
 }
 

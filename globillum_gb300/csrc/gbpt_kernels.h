@@ -250,6 +250,8 @@ cudaError_t k_launch_direct_hybrid(const DevScene& S, const CameraRec& cam, int 
 int k_adjoint_grid();
 cudaError_t k_launch_dimg_pack(const float* src, int n, float scale, float4* dst, cudaStream_t st);
 cudaError_t k_launch_grad_reduce(const float* grad, int replicas, int stride, double* out, cudaStream_t st);
+cudaError_t k_launch_l2_loss(const float* img, const float* target, int n, float scale, float4* dimg, double* loss,
+                             cudaStream_t st);
 // Kernel launches of one slot-pool iteration in a render mode.
 int k_launches_per_iteration(int mode);
 cudaError_t k_launch_mrg_states(uint32_t seed, const uint32_t* sub, int n, int method, uint32_t* out,

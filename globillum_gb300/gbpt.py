@@ -111,6 +111,11 @@ class AdjointItem(C.Structure):
                 ("dL_dparams", C.c_void_p)]
 
 
+class FitItem(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("desc", RenderDesc), ("target", C.c_void_p),
+                ("image", C.c_void_p)]
+
+
 class Hit(C.Structure):
     _fields_ = [("t", C.c_float), ("beta", C.c_float), ("gamma", C.c_float), ("ref", C.c_uint32)]
 
@@ -136,7 +141,7 @@ EXPORTS = [
     "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
     "gb_asset_add_obj", "gb_asset_add_lights", "gb_asset_add_light", "gb_asset_get_desc", "gb_asset_material_name",
     "gb_read_pbrdf", "gb_render_direct", "gb_scene_create_ex", "gb_scene_refit", "gb_render_hybrid_direct",
-    "gb_bvh_build_stats",
+    "gb_bvh_build_stats", "gb_fit_prepare", "gb_fit_step",
 ]
 
 _lib = None
@@ -194,6 +199,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_forward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, vp, ip]
     lib.gb_backward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, ip, vp]
     lib.gb_backward_batch.argtypes = [vp, ip, C.POINTER(AdjointItem), ip, ip]
+    lib.gb_fit_prepare.argtypes = [vp, ip, C.POINTER(FitItem)]
+    lib.gb_fit_step.argtypes = [vp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_double)]
     lib.gb_asset_create.argtypes = [C.POINTER(vp)]
     lib.gb_asset_destroy.argtypes = [vp]
     lib.gb_asset_destroy.restype = None
@@ -374,6 +381,29 @@ class Context:
         gflag = -1 if graph is None else (1 if graph else 0)
         self.check(self.lib.gb_backward_batch(self.h, len(jobs), items, 0, gflag))
         return outs
+
+    def fit_prepare(self, jobs: list, target_ptrs: list, image_ptrs: list | None = None) -> None:
+        """gb_fit_prepare over [(Scene, cam, rdesc), ...] with one device
+        target image (pointer) per job and optional device image outputs."""
+        items = (FitItem * max(1, len(jobs)))()
+        for i, (sc, cam, rdesc) in enumerate(jobs):
+            img = None if image_ptrs is None else image_ptrs[i]
+            items[i] = FitItem(sc.h, make_camera(cam), make_render_desc(rdesc), C.c_void_p(target_ptrs[i]),
+                               None if img is None else C.c_void_p(img))
+        self._fit_n = len(jobs)
+        self._fit_counts = [sc.param_count() for sc, _, _ in jobs]
+        self.check(self.lib.gb_fit_prepare(self.h, len(jobs), items))
+
+    def fit_step(self, params: list) -> tuple[list, np.ndarray]:
+        """gb_fit_step: one graph launch; returns (gradients, losses)."""
+        n = self._fit_n
+        xs = [np.ascontiguousarray(p, np.float32) for p in params]
+        gs = [np.empty(k, np.float32) for k in self._fit_counts]
+        xp = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+        gp = (C.c_void_p * n)(*[g.ctypes.data for g in gs])
+        loss = np.empty(n, np.float64)
+        self.check(self.lib.gb_fit_step(self.h, xp, gp, loss.ctypes.data_as(C.POINTER(C.c_double))))
+        return gs, loss
 
     def autotune(self, jobs: list, proxy_spp: int = 0, repeats: int = 2) -> tuple[dict, float]:
         """gb_autotune over the batch; returns (best tuning, its frame ms)

@@ -466,6 +466,39 @@ typedef struct {
 int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* tuning);
 int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* tuning);
 
+/* ------------------------------------------------ batched fitting steps */
+/* One scene of a fitting step: the frame it renders and the image it is
+ * fitted to. */
+typedef struct {
+    gb_scene* scene;
+    gb_camera camera;
+    gb_render_desc desc;
+    const float* target;    /* device, width*height*3 floats: the image to match */
+    float* image;           /* device, width*height*3 floats, or NULL: receives the frame */
+} gb_fit_item;
+
+/* Batched inverse rendering as one CUDA graph launch per step (no
+ * counterpart in the reference, which has no derivatives).  A step sets
+ * every scene's parameters, renders the scenes as one batched frame,
+ * computes each scene's L2 loss sum over pixels and channels of
+ * (image - target)^2 and its image gradient on the device, runs the
+ * path-replay adjoint of that gradient over the same batch (as
+ * gb_backward_batch) and reduces the parameter gradients: the parameter
+ * upload, both frames, the loss and the reduction are one captured graph,
+ * launched once per step; the image gradients never leave the device.
+ * gb_fit_prepare(ctx, n, items) lays the batch out and captures the graph
+ * (1..1024 scenes, each at most once; the restrictions of
+ * gb_backward_batch apply).  The targets and images must stay valid and the
+ * scenes must not be used by other calls while steps run.  Renders on the
+ * same context in between may grow its buffers; the next step then
+ * captures the graph again by itself. */
+int gb_fit_prepare(gb_ctx* ctx, int n, const gb_fit_item* items);
+/* One step: params[i] (host, gb_scene_param_count floats) become item i's
+ * scene parameters, as gb_scene_set_params sets them; dL_dparams[i] (host)
+ * receives the gradient of item i's loss and loss[i] (host, or NULL) the
+ * loss. */
+int gb_fit_step(gb_ctx* ctx, const float* const* params, float* const* dL_dparams, double* loss);
+
 /* Autotuner of the wavefront knobs (gb_tuning: graph capture, slot-pool
  * capacity, refill threshold, triangle policy, resident traversal blocks per
  * SM, traversal stack depth and block shape) for a batch (or one scene, n = 1): coordinate descent from the

@@ -75,7 +75,7 @@ def test_struct_layouts_match_the_header(tmp_path):
              "gb_render_desc": gbpt.RenderDesc, "gb_batch_item": gbpt.BatchItem, "gb_hit": gbpt.Hit,
              "gb_stats": gbpt.Stats, "gb_tuning": gbpt.Tuning, "gb_ctx_desc": gbpt.CtxDesc,
              "gb_adjoint_item": gbpt.AdjointItem, "gb_build_options": gbpt.BuildOptions,
-             "gb_texture": gbpt.Texture, "gb_bvh_stats": gbpt.BvhStats}
+             "gb_texture": gbpt.Texture, "gb_bvh_stats": gbpt.BvhStats, "gb_fit_item": gbpt.FitItem}
     c_fields = {"gb_batch_item": ["scene", "camera", "desc", "out_rgb"],
                 "gb_tuning": ["refill", "slots", "sample_mb", "tri_mode", "graph", "blocks_per_sm", "stack_depth",
                               "block_threads"],

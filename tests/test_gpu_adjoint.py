@@ -179,3 +179,60 @@ def test_autograd_inverse_rendering_descends(gpu_ctx):
     assert losses[-1] < 0.5 * losses[0], losses
     s.set_params(x_true)
     s.close()
+
+
+def test_fit_step_is_one_graph_and_matches_the_separate_calls(gpu_ctx):
+    """gb_fit_step (parameter upload, batched forward frame, L2 loss and
+    image gradient on the device, batched adjoint, gradient reduction: one
+    CUDA graph launch) gives the batched frame bit for bit, the L2 losses,
+    and the gradients of gb_backward_batch fed with 2 (image - target);
+    over several steps with changing parameters, and again after another
+    render on the context forced the graph to be captured anew."""
+    import torch
+    scs = [_scene(seed=7), _scene(seed=11, w=40, h=40, spp=3, bounces=3),
+           scenes.cornell(width=32, height=24, spp=2, max_bounces=4)]
+    scs[2].render["rng_mode"] = gbpt.GB_RNG_MRG32K3A_POOL
+    hs = [gpu_ctx.scene(sc) for sc in scs]
+    jobs = [(h, sc.camera, sc.render) for h, sc in zip(hs, scs)]
+    x0 = [h.get_params() for h in hs]
+    rng = np.random.default_rng(3)
+    targets = []
+    for h, sc, x in zip(hs, scs, x0):
+        xt = x.copy()
+        nm = 5 * len(sc.materials)
+        xt[:nm] = np.clip(xt[:nm] + rng.normal(0.0, 0.1, nm), 0.0, 1.0).astype(np.float32)
+        h.set_params(xt)
+        targets.append(torch.from_numpy(h.render(sc.camera, sc.render)).cuda())
+        h.set_params(x)
+    images = [torch.empty_like(t) for t in targets]
+    gpu_ctx.fit_prepare(jobs, [t.data_ptr() for t in targets], [i.data_ptr() for i in images])
+    xs = [x.copy() for x in x0]
+    for step in range(3):
+        if step == 2:
+            # another render on the context (a larger frame) moves its buffers
+            big = scenes.icospheres(n_spheres=8, level=2, box=8.0, width=200, height=150, spp=1, max_bounces=2)
+            hb = gpu_ctx.scene(big)
+            hb.render(big.camera, big.render)
+            hb.close()
+        grads, loss = gpu_ctx.fit_step(xs)
+        for h, x in zip(hs, xs):
+            assert np.array_equal(h.get_params(), x)
+        ref = gpu_ctx.render_batch(jobs, graph=True)
+        dimgs = []
+        for i, (r, t) in enumerate(zip(ref, targets)):
+            got = images[i].cpu().numpy()
+            assert np.array_equal(got, r), f"step {step} scene {i}: frame differs"
+            tn = t.cpu().numpy()
+            d = r.astype(np.float64) - tn
+            assert np.isclose(loss[i], float((d * d).sum()), rtol=1e-6, atol=0.0)
+            dimgs.append((2.0 * (r - tn)).astype(np.float32))
+        gref = gpu_ctx.backward_batch(jobs, dimgs, graph=True)
+        for g, gr in zip(grads, gref):
+            assert np.allclose(g, gr, rtol=1e-4, atol=1e-6 * np.abs(gr).max())
+        xs = [np.clip(x - 1e-3 * g / max(1e-12, np.abs(g).max()), 0.0, 1.0).astype(np.float32)
+              for x, g in zip(xs, grads)]
+        # lights keep their emission (only the materials move)
+        for x, x_init, sc in zip(xs, x0, scs):
+            x[5 * len(sc.materials):] = x_init[5 * len(sc.materials):]
+    for h in hs:
+        h.close()
