@@ -113,6 +113,7 @@ struct gb_ctx {
     int tri_mode = 0;                   // traversal triangle policy (see gb_tuning)
     int blocks_per_sm = 0;              // resident traversal blocks per SM (0 = occupancy limit)
     int stack_depth = 32;               // traversal stack entries (24 or 32)
+    int sampling_terms = 0;             // adjoint: add the derivatives of the sampling decisions
     int block_threads = 128;            // threads per traversal block (64 or 128)
     int slots = 1 << 20;                // path slots in flight (upper bound)
     int sample_mb = 1024;               // sample buffer budget (chunk size)
@@ -1055,6 +1056,7 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
     P.tri_mode = ctx->tri_mode;
     P.blocks_per_sm = ctx->blocks_per_sm;
     P.trav_variant = (ctx->stack_depth == 24 ? 1 : 0) + (ctx->block_threads == 64 ? 2 : 0);
+    P.sampling_terms = ctx->sampling_terms;
     P.mode = ctx->mode;
     P.textured = 0;
     for (const BatchScene& b : ctx->items)
@@ -1524,6 +1526,7 @@ std::vector<uint64_t> fit_key(const gb_ctx* ctx) {
     k.push_back(((uint64_t)(uint32_t)ctx->slots << 32) | (uint32_t)ctx->sample_mb);
     k.push_back(((uint64_t)(uint32_t)ctx->refill << 32) | (uint32_t)ctx->tri_mode);
     k.push_back(((uint64_t)(uint32_t)ctx->blocks_per_sm << 32) | (uint32_t)(ctx->stack_depth * 1000 + ctx->block_threads));
+    k.push_back((uint64_t)ctx->sampling_terms);
     for (const gb_fit_item& u : ctx->fit.user)
         k.push_back((uint64_t)(uintptr_t)u.scene->S.mats ^ ((uint64_t)(uintptr_t)u.scene->S.lights << 1));
     return k;
@@ -1961,6 +1964,13 @@ int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* t) {
     t->blocks_per_sm = ctx->blocks_per_sm + 1;
     t->stack_depth = ctx->stack_depth;
     t->block_threads = ctx->block_threads;
+    return GB_OK;
+}
+
+int gb_ctx_set_gradient_terms(gb_ctx* ctx, int sampling) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (sampling != 0 && sampling != 1) return fail(ctx, GB_ERR_INVALID, "sampling must be 0 or 1");
+    ctx->sampling_terms = sampling;
     return GB_OK;
 }
 

@@ -1182,7 +1182,7 @@ __global__ void __launch_bounds__(kBlock, GB_SHADE_MIN_BLOCKS) k_shade(Frame F, 
                               F.pix.ld(slot) - R.pixel_base, path, bounce, nullptr, nullptr, &tr);
                 int light = nee_light(F, R, slot, ld3(rn));
                 uint32_t info = (uint32_t)light | ((uint32_t)tr.lobe << 16) | (tr.clamp_mask << 20) |
-                                (tr.nee ? (1u << 23) : 0u);
+                                (tr.nee ? (1u << 23) : 0u) | ((tr.flags & 7u) << 24);
                 float4* rec = F.adj + (size_t)bounce * kAdjPlanes * F.nslots + slot;
                 rec[0] = make_float4(tp4.x, tp4.y, tp4.z, tr.pdf);
                 rec[(size_t)F.nslots] = make_float4(tr.wo.x, tr.wo.y, tr.wo.z, tr.q);
@@ -1244,6 +1244,14 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
         float* gm_base = grad + R.grad_base;
         float* gl_base = gm_base + (size_t)kMatGradFloats * (size_t)R.n_mats;
         v3 an = mk(0.0f, 0.0f, 0.0f);  // dLoss / dT_{k+1}
+        // sampling terms: gsuf = g . (light-sample terms of the vertices
+        // after k); each vertex's scores are kept for the path's final miss
+        // term, known once every light-sample term has been seen
+        const bool st = P.sampling_terms != 0;
+        float gsuf = 0.0f;
+        uint32_t smi[kMaxAdjBounces];
+        float ssm[kMaxAdjBounces], ssr[kMaxAdjBounces];
+        int nsc = 0;
         for (int k = K - 1; k >= 0; --k) {
             const float4* rec = F.adj + (size_t)k * kAdjPlanes * ns + slot;
             const float4 r0 = rec[0], r1 = rec[ns], r2 = rec[2 * ns], r3 = rec[3 * ns], r4 = rec[4 * ns];
@@ -1253,17 +1261,22 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
             const int light = (int)(info & 0xffffu), lobe = (int)((info >> 16) & 15u);
             const uint32_t cmask = (info >> 20) & 7u;
             const bool nee = (info >> 23) & 1u;
+            const uint32_t sflags = (info >> 24) & 7u;
             const MaterialRec m = load_material(R.S.mats, mi);
             MatGrad mg;
             matgrad_zero(&mg);
             v3 ak = mk(0.0f, 0.0f, 0.0f);
+            float gw = 0.0f;  // dLoss / d log w of this vertex's Walter weight (through T_{k+1})
             if (an.x != 0.0f || an.y != 0.0f || an.z != 0.0f) {
                 const v3 brdf = material_eval(m, lobe, wo, wi, N);
                 const float inv = 1.0f / (pdf * q);
                 const v3 c = mk((cmask & 1u) ? 0.0f : 1.0f, (cmask & 2u) ? 0.0f : 1.0f, (cmask & 4u) ? 0.0f : 1.0f);
-                material_eval_vjp(m, lobe, wo, wi, N, (c * T * an) * inv, &mg);
+                const v3 db = (c * T * an) * inv;  // dLoss / d brdf
+                material_eval_vjp(m, lobe, wo, wi, N, db, &mg);
                 ak = (c * brdf * an) * inv;
+                gw = -dot(db, brdf);
             }
+            float gnee = 0.0f;  // g . this vertex's light-sample term
             if (nee) {
                 const v3 col = R.S.lights[light].col;
                 const v3 psc = col * sc;
@@ -1275,13 +1288,48 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(Frame F, RenderParams P) {
                 if (acol.y != 0.0f) atomicAdd(gl + 1, acol.y);
                 if (acol.z != 0.0f) atomicAdd(gl + 2, acol.z);
                 ak = ak + g * bl * psc;
+                gnee = dot(g, T * (bl * psc));
             }
+            if (st) {
+                // the branch decision moves this vertex's light-sample term
+                // and everything after it; the sampled direction moves what
+                // comes after this vertex; the Walter weight divides T_{k+1}
+                float sm, sr, wr, zlo = 0.0f, zhi = 1.0f;
+                if (R.rng_mode == 0 && R.S.n_lights > 0)
+                    light_pick_interval(R.S.lights, R.S.n_lights, R.S.overall_power, light, &zlo, &zhi);
+                sampling_scores(m, lobe, sflags, wo, wi, N, pdf, zlo, zhi, &sm, &sr, &wr);
+                mg.metallic += sm * (gnee + gsuf);
+                mg.roughness += sr * gsuf + gw * wr;
+                if (sm != 0.0f || sr != 0.0f) {
+                    smi[nsc] = mi;
+                    ssm[nsc] = sm;
+                    ssr[nsc] = sr;
+                    ++nsc;
+                }
+            }
+            gsuf += gnee;
             float* gmat = gm_base + (size_t)kMatGradFloats * mi;
             const float* mv = &mg.cdlin[0];
 #pragma unroll
             for (int f = 0; f < kMatGradFloats; ++f)
                 if (mv[f] != 0.0f) atomicAdd(gmat + f, mv[f]);
             an = ak;
+        }
+        if (st && nsc > 0) {
+            // the path's final miss (the white background a throughput of
+            // (1, 1, 1) adds, hybrid-pt.cpp:567-572): its sample minus the
+            // light-sample terms; below rounding of the sum it is none
+            const uint32_t pbv = F.pb.ld(slot);
+            const float4 sv = F.samples[P.round_start[(pbv >> 10) - (uint32_t)P.p0] + F.pix.ld(slot)];
+            const float gtot = dot(g, ld3(sv));
+            const float gmiss = gtot - gsuf;
+            if (fabsf(gmiss) > 1e-4f * fabsf(gtot)) {
+                for (int i = 0; i < nsc; ++i) {
+                    float* gmat = gm_base + (size_t)kMatGradFloats * smi[i];
+                    if (ssm[i] != 0.0f) atomicAdd(gmat + offsetof(MatGrad, metallic) / sizeof(float), ssm[i] * gmiss);
+                    if (ssr[i] != 0.0f) atomicAdd(gmat + offsetof(MatGrad, roughness) / sizeof(float), ssr[i] * gmiss);
+                }
+            }
         }
     }
 }

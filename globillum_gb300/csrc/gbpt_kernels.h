@@ -219,6 +219,7 @@ struct RenderParams {
     int tri_mode;      // 0: all pending triangles then a node; 1/2: triangle postponing, one / all triangles;
                        // 3: warp-cooperative triangle tests, then a node
     int blocks_per_sm; // resident blocks per SM of the traversal kernels (0 = occupancy limit)
+    int sampling_terms; // adjoint: add the derivatives of the sampling decisions (sampling_scores)
     int trav_variant;  // traversal kernels of the default triangle policy: stack entries / threads per
                        // block 0: 32 / 128, 1: 24 / 128, 2: 32 / 64, 3: 24 / 64
     int mode;          // MODE_*

@@ -523,6 +523,16 @@ GB_HD float rect_light_power(float w, float h, v3 col) {
 // Light pick (arealight-sampler-cpu.cpp:32-39).  The reference reads
 // lights[n] when the accumulated power falls short of choice by rounding;
 // here the index stops at n-1.
+// The interval (lo, hi] of the uniform draw rnd_z that pick_light maps to
+// light l (choice = rnd_z * overall_power, the light pick of
+// arealight-sampler-cpu.cpp:32-39; the last light takes the rest).
+GB_HD void light_pick_interval(const LightRec* L, int n, float overall_power, int l, float* lo, float* hi) {
+    float acc = 0.0f;
+    for (int i = 0; i < l; ++i) acc += L[i].power;
+    *lo = acc / overall_power;
+    *hi = l + 1 < n ? (acc + L[l].power) / overall_power : 1.0f;
+}
+
 GB_HD int pick_light(const LightRec* L, int n, float overall_power, float rnd_z) {
     float choice = rnd_z * overall_power;
     float acc = 0.0f;
@@ -795,7 +805,8 @@ GB_HD float G1(v3 v, v3 m, v3 n, float a2, float tanv) {
 
 // principledMaterial.h:121-176 with T=(1,0,0), B=(0,1,0), n=(0,0,1) in
 // tangent space (:369-371).  Returns the Walter weight (>= 0.01 or NaN).
-GB_HD float sample_gtr2_aniso(float u, float v, float ax, float ay, float roughg2, v3 V, v3* Lout) {
+GB_HD float sample_gtr2_aniso(float u, float v, float ax, float ay, float roughg2, v3 V, v3* Lout,
+                              bool* flipped = nullptr) {
     float sn, cs; sincos_2pi(u, &sn, &cs);
     float fac = sqrtf(v / (1.0f - v));
     v3 t = mk(ax * cs, 0.0f, 0.0f);
@@ -803,7 +814,9 @@ GB_HD float sample_gtr2_aniso(float u, float v, float ax, float ay, float roughg
     v3 h = normalize_rcp(fac * t + mk(0.0f, 0.0f, 1.0f));
     v3 n = mk(0.0f, 0.0f, 1.0f);
     v3 L = reflect(V, h);
-    if (dot(L, n) < 0.0f) L = -1.0f * L;
+    const bool flip = dot(L, n) < 0.0f;
+    if (flip) L = -1.0f * L;
+    if (flipped) *flipped = flip;
     float dotLm = dot(L, h);
     float dotVm = dot(V, h);
     float tanL = sqrtf(1.0f - dotLm * dotLm) / dotLm;
@@ -836,10 +849,18 @@ GB_HD v3 sample_glass(float u, v3 V, float ior, int* lobe) {
 
 GB_HD bool is_glass(const MaterialRec& m) { return m.kind == MAT_PRINCIPLED && m.opacity < 1.0f; }
 
+// Flags of a sampled vertex (for the derivatives of the sampling
+// decisions): the metallic branch was taken (rnd.z < metallic), the GTR2
+// reflection was flipped to the upper side, the shading normal was flipped
+// to face the incoming ray.
+enum { SAMPLE_METAL_BRANCH = 1u, SAMPLE_L_FLIPPED = 2u, SAMPLE_N_FLIPPED = 4u };
+
 // materialBRDF::sample (material-wrapper.h:224-227) -> LambertianMaterial::sample
 // (simpleMaterial.h:183-186) or PrincipledMaterial::sample
 // (principledMaterial.h:354-390).  wo, wi in tangent space.
-GB_HD void material_sample(const MaterialRec& m, v3 wo, v3 rnd, v3* wi, float* pdf, int* lobe) {
+GB_HD void material_sample(const MaterialRec& m, v3 wo, v3 rnd, v3* wi, float* pdf, int* lobe,
+                           uint32_t* flags = nullptr) {
+    if (flags) *flags = 0u;
     if (m.kind == MAT_LAMBERT) {
         v3 w = cosine_sample_hemisphere(rnd.x, rnd.y);
         *wi = w;
@@ -854,7 +875,9 @@ GB_HD void material_sample(const MaterialRec& m, v3 wo, v3 rnd, v3* wi, float* p
     }
     if (rnd.z < m.metallic) {
         v3 L;
-        float p = sample_gtr2_aniso(rnd.x, rnd.y, m.ax, m.ay, m.roughg2, wo, &L);
+        bool flip = false;
+        float p = sample_gtr2_aniso(rnd.x, rnd.y, m.ax, m.ay, m.roughg2, wo, &L, &flip);
+        if (flags) *flags = SAMPLE_METAL_BRANCH | (flip ? SAMPLE_L_FLIPPED : 0u);
         *lobe = LOBE_DISNEY_REFLECTION;
         *wi = L;
         *pdf = p;
@@ -928,6 +951,84 @@ GB_HD v3 material_eval(const MaterialRec& m, int lobe, v3 wo, v3 wi, v3 N) {
     if (lobe == LOBE_SPECULAR_REFLECTION) return mk(1.0f, 1.0f, 1.0f);
     if (lobe == LOBE_SPECULAR_TRANSMISSION) return mk(1.0f, 1.0f, 1.0f) * (1.0f / fabsf(dot(wi, N)));
     return principled_diffuse(m, wo, N, wi);
+}
+
+// Derivatives of a vertex's sampling decisions (PrincipledMaterial::sample,
+// principledMaterial.h:354-390: the metallic lobe when rnd.z < metallic,
+// then the GTR2-aniso half vector of :46-61 and the Walter weight of
+// :121-176 as the sample's "pdf"):
+//   sm  d log P(branch | the other uses of rnd.z) / d metallic.  rnd.z is
+//       uniform on (zlo, zhi] given the vertex's other decisions that read
+//       it: with MRG32k3a light draws the light pick reads the same value
+//       (the light and path pools are seeded alike), so it is the picked
+//       light's power interval; otherwise (0, 1].  P(metallic branch) =
+//       clamp((metallic - zlo) / (zhi - zlo), 0, 1), so the score is
+//       1 / (metallic - zlo) for the metallic branch and
+//       -1 / (zhi - metallic) for the diffuse one while metallic lies in
+//       the interval (derivatives from inside the interval at its ends),
+//       0 otherwise; 0 for Lambert and glass
+//   sr  d log p(h) / d roughness of the sampled half vector, with
+//       p(h) = D_GTR2(h) cos(theta_h) (the density of the sampling formula)
+//       and h held fixed; the density of the second half vector that
+//       reflects to the same flipped direction is neglected
+//   wr  d log w / d roughness of the Walter weight the throughput is
+//       divided by (0 where it was clamped at 0.01)
+// sr and wr are nonzero for a successful metallic sample only.  The half
+// vector is recovered from the recorded directions: L = +-(V - 2 (V.h) h),
+// so h is parallel to V - L, or to V + L when L was flipped.
+GB_HD void sampling_scores(const MaterialRec& m, int lobe, uint32_t flags, v3 wo, v3 wi, v3 N, float pdf,
+                           float zlo, float zhi, float* sm, float* sr, float* wr) {
+    *sm = 0.0f;
+    *sr = 0.0f;
+    *wr = 0.0f;
+    if (m.kind != MAT_PRINCIPLED || m.opacity < 1.0f) return;
+    const float mt = m.metallic;
+    if (flags & SAMPLE_METAL_BRANCH) *sm = (mt > zlo && mt <= zhi) ? 1.0f / (mt - zlo) : 0.0f;
+    else *sm = (mt >= zlo && mt < zhi) ? -1.0f / (zhi - mt) : 0.0f;
+    if (lobe != LOBE_DISNEY_REFLECTION) return;
+    const float r = m.roughness;
+    if (!(r > 0.0f)) return;
+    // the sampling frame: tangents of the unflipped normal, z = N
+    const v3 Nu = (flags & SAMPLE_N_FLIPPED) ? -1.0f * N : N;
+    v3 T, B;
+    make_tangent_frame(Nu, &T, &B);
+    T = normalize_div(T);
+    B = normalize_div(B);
+    v3 h = (flags & SAMPLE_L_FLIPPED) ? wo + wi : wo - wi;
+    const float hl = length(h);
+    if (!(hl > 0.0f)) return;
+    h = h / hl;
+    float hz = dot(h, N);
+    if (hz < 0.0f) {
+        h = -1.0f * h;
+        hz = -hz;
+    }
+    const float hx = dot(h, T), hy = dot(h, B);
+    const float ax = m.ax, ay = m.ay;
+    // ax = max(.001, r^2 / aspect), ay = max(.001, r^2 aspect)
+    const float dax = ax > 0.001f ? 2.0f * ax / r : 0.0f;
+    const float day = ay > 0.001f ? 2.0f * ay / r : 0.0f;
+    // log D = -log(pi ax ay) - 2 log Q, Q = (hx / ax)^2 + (hy / ay)^2 + hz^2
+    const float qx = hx / ax, qy = hy / ay;
+    const float Q = qx * qx + qy * qy + hz * hz;
+    const float dlx = -1.0f / ax + 4.0f * qx * qx / (ax * Q);
+    const float dly = -1.0f / ay + 4.0f * qy * qy / (ay * Q);
+    *sr = dlx * dax + dly * day;
+    if (!(pdf > 0.01f)) return;
+    // w = |L.h| G1(L) G1(V) / (|L.n| |n.h|), G1 = Xi 2 / (1 + S),
+    // S = sqrt(1 + a2 tan^2): d log G1 / d a2 = -(tan^2 / (2 S)) / (1 + S)
+    const float a2 = m.roughg2;
+    float dlw = 0.0f;
+    for (int side = 0; side < 2; ++side) {
+        const float d = side ? dot(wo, h) : dot(wi, h);
+        const float t2 = (1.0f - d * d) / (d * d);
+        const float S = sqrtf(1.0f + a2 * t2);
+        dlw += -(t2 / (2.0f * S)) / (1.0f + S);
+    }
+    // a2 = roughg^2, roughg = b^2, b = ax ay / 2 + 1 / 2
+    const float b = ax * ay * 0.5f + 0.5f;
+    const float roughg = b * b;
+    *wr = dlw * (2.0f * roughg * b * (dax * ay + ax * day));
 }
 
 // ---------------------------------------------------------------- adjoint --
@@ -1053,6 +1154,7 @@ struct BsdfSample {
     float pdf;
     int lobe;
     bool glass;
+    uint32_t flags;  // SAMPLE_*
 };
 
 GB_HD BsdfSample sample_bsdf(const MaterialRec& m, v3 Nraw, v3 ray_dir, v3 rnd) {
@@ -1065,10 +1167,12 @@ GB_HD BsdfSample sample_bsdf(const MaterialRec& m, v3 Nraw, v3 ray_dir, v3 rnd) 
     B = normalize_div(B);
     s.inv_org_dir = -1.0f * s.org_dir;
     s.glass = is_glass(m);
-    if (dot(s.org_dir, N) > 0.0f) N = N * -1.0f;
+    const bool nflip = dot(s.org_dir, N) > 0.0f;
+    if (nflip) N = N * -1.0f;
     v3 wo_ts = to_tangent(s.inv_org_dir, T, B, N);
     v3 wi;
-    material_sample(m, wo_ts, rnd, &wi, &s.pdf, &s.lobe);
+    material_sample(m, wo_ts, rnd, &wi, &s.pdf, &s.lobe, &s.flags);
+    if (nflip) s.flags |= SAMPLE_N_FLIPPED;
     wi = from_tangent(wi, T, B, N);
     s.wi = normalize_div(wi);
     s.N = N;
@@ -1085,6 +1189,7 @@ struct ShadeTrace {
     int lobe;
     uint32_t clamp_mask;  // bit c: channel c of the new throughput was clamped
     bool nee;
+    uint32_t flags;       // SAMPLE_* of the vertex's BRDF sample
 };
 
 GB_HD v3 clamp_one(v3 t, uint32_t* mask) {
@@ -1163,6 +1268,7 @@ GB_HD ShadeOut shade_hit(const MaterialRec& m, v3 P, v3 Nraw, v3 ray_dir, v3 tp,
     if (trace) {
         trace->wo = inv_org_dir; trace->wi = wi; trace->N = N; trace->ld = ld;
         trace->pdf = pdf; trace->q = q; trace->lobe = lobe; trace->clamp_mask = cmask; trace->nee = nee;
+        trace->flags = bs.flags;
     }
     return o;
 }

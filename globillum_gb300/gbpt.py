@@ -141,7 +141,7 @@ EXPORTS = [
     "gb_backward", "gb_backward_batch", "gb_asset_create", "gb_asset_destroy", "gb_asset_last_error",
     "gb_asset_add_obj", "gb_asset_add_lights", "gb_asset_add_light", "gb_asset_get_desc", "gb_asset_material_name",
     "gb_read_pbrdf", "gb_render_direct", "gb_scene_create_ex", "gb_scene_refit", "gb_render_hybrid_direct",
-    "gb_bvh_build_stats", "gb_fit_prepare", "gb_fit_step",
+    "gb_bvh_build_stats", "gb_fit_prepare", "gb_fit_step", "gb_ctx_set_gradient_terms",
 ]
 
 _lib = None
@@ -200,6 +200,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.gb_backward.argtypes = [vp, vp, C.POINTER(Camera), C.POINTER(RenderDesc), vp, ip, vp]
     lib.gb_backward_batch.argtypes = [vp, ip, C.POINTER(AdjointItem), ip, ip]
     lib.gb_fit_prepare.argtypes = [vp, ip, C.POINTER(FitItem)]
+    lib.gb_ctx_set_gradient_terms.argtypes = [vp, ip]
     lib.gb_fit_step.argtypes = [vp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_double)]
     lib.gb_asset_create.argtypes = [C.POINTER(vp)]
     lib.gb_asset_destroy.argtypes = [vp]
@@ -413,6 +414,11 @@ class Context:
         self.check(self.lib.gb_autotune(self.h, len(jobs), self._items(jobs, None), proxy_spp, repeats,
                                         C.byref(t), C.byref(ms)))
         return {k: getattr(t, k) for k, _ in Tuning._fields_}, ms.value
+
+    def set_gradient_terms(self, sampling: bool):
+        """gb_ctx_set_gradient_terms: add the derivatives of the sampling
+        decisions to the adjoint (True) or freeze them (False, default)."""
+        self.check(self.lib.gb_ctx_set_gradient_terms(self.h, 1 if sampling else 0))
 
     def set_stage_timing(self, on: bool):
         self.check(self.lib.gb_ctx_set_stage_timing(self.h, 1 if on else 0))

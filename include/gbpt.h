@@ -466,6 +466,33 @@ typedef struct {
 int gb_ctx_set_tuning(gb_ctx* ctx, const gb_tuning* tuning);
 int gb_ctx_get_tuning(const gb_ctx* ctx, gb_tuning* tuning);
 
+/* Which derivative the adjoint computes (no counterpart in the reference).
+ * sampling = 0 (default): the derivative of the frame with every random
+ * decision frozen at the current parameters -- exactly the derivative of
+ * gb_forward(eval_params), with the BRDF "pdf" (the Walter weight of the
+ * metallic lobe) held fixed.  sampling = 1: also the derivatives of the
+ * sampling decisions that depend on the parameters, so that the gradient
+ * estimates the derivative of the expected frame:
+ *  - the metallic lobe choice (rnd.z < metallic, principledMaterial.h:365)
+ *    by its score times everything the choice moves.  With MRG32k3a light
+ *    draws the light pick reads the same rnd.z, so the score is taken given
+ *    the picked light's interval (lo, hi] of rnd.z: 1/(metallic - lo) for
+ *    the metallic branch, -1/(hi - metallic) for the diffuse one, 0 when
+ *    metallic lies outside the interval; with Halton light draws lo = 0,
+ *    hi = 1;
+ *  - the roughness dependence of the GTR2 half-vector density (:46-61) by
+ *    its score times what follows the vertex;
+ *  - the roughness dependence of the Walter weight (:121-176) through the
+ *    throughput.
+ * The survival probability q of the Russian-roulette extension is held
+ * fixed in both forms; for the expected frame that is exact (the survival
+ * score d log q cancels the derivative of the 1/q weight).  Not covered:
+ * the jump of a miss's contribution where a throughput reaches the clamp to
+ * exactly (1, 1, 1) (hybrid-pt.cpp:567-572 add the white background then),
+ * a discontinuity in the parameters.  Applies to gb_backward,
+ * gb_backward_batch and gb_fit_step. */
+int gb_ctx_set_gradient_terms(gb_ctx* ctx, int sampling);
+
 /* ------------------------------------------------ batched fitting steps */
 /* One scene of a fitting step: the frame it renders and the image it is
  * fitted to. */

@@ -407,11 +407,14 @@ void eval_d(const MatD& m, int lobe, V3d V, V3d L, V3d N, Dd out[3]) {
 }
 
 // One shaded vertex of a replayed path.
+constexpr int kReplayBounces = 64;  // bounces orc_adjoint_f64 replays per path at most
+
 struct AdjVertex {
     int mi, light, lobe;
     bool nee;
     float pdf, q, scale;
     v3 wo, wi, N, ld;
+    uint32_t flags;  // SAMPLE_* of the vertex's BRDF sample
 };
 
 int shade_stage(const OScene& s, int w, int h, const gb_render_desc* desc, float* ray_orig, float* ray_dir,
@@ -733,13 +736,14 @@ int orc_render(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0
 // make_material and the BRDF formulas (directions, pdfs and roulette held
 // at their sampled values).  dimg: rows' pixels x 3 (not divided by spp).
 int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int row0, int row1, const float* pool,
-                    int pool_updates, const float* dimg, int n_sel, const int* sel, double* out) {
+                    int pool_updates, const float* dimg, int n_sel, const int* sel, double* out, int sampling_terms) {
     const OScene& s = *(const OScene*)sp;
     const int W = d->width, H = d->height, L = d->max_bounces;
     if (row0 < 0 || row1 > H || row0 >= row1) return 1;
     if (pool_updates < d->spp * L) return 2;
     if (cam->aperture != 0.0f && (row0 != 0 || row1 != H)) return 3;
     if (s.sky.light >= 0) return 4;  // the adjoint covers rect lights only
+    if (L > kReplayBounces) return 5;
     const int n = W * (row1 - row0), base = row0 * W;
     const int nm = (int)s.mats_in.size();
     CameraRec C = make_camera(*cam, W, H);
@@ -768,9 +772,13 @@ int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int
                 float tmax = FLT_MAX;
                 v3 tp = mk(1.0f, 1.0f, 1.0f);
                 vs.clear();
+                v3 miss_end = mk(0.0f, 0.0f, 0.0f);  // what the path's final miss adds
                 for (int b = 0; b < L; ++b) {
                     gb_hit h = trace_closest(s, o, dd, tmax, nullptr, nullptr);
-                    if (h.ref == 0xffffffffu) break;
+                    if (h.ref == 0xffffffffu) {
+                        if (b > 0) miss_end = miss_contribution(tp, dd, par, &s.sky);
+                        break;
+                    }
                     const float* up = pool + ((size_t)p * L + b) * n * 3;
                     v3 rnd = mk(up[3 * i], up[3 * i + 1], up[3 * i + 2]);
                     v3 lr = rnd;
@@ -793,7 +801,8 @@ int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int
                     ShadeTrace tr;
                     ShadeOut so2 = shade_hit(s.mats[mi], P, Nr, dd, tp, rnd, !occl, sd, psc, par, (uint32_t)id,
                                              (uint32_t)p, b, nullptr, nullptr, &tr);
-                    vs.push_back(AdjVertex{mi, light, tr.lobe, tr.nee, tr.pdf, tr.q, scale, tr.wo, tr.wi, tr.N, tr.ld});
+                    vs.push_back(AdjVertex{mi, light, tr.lobe, tr.nee, tr.pdf, tr.q, scale, tr.wo, tr.wi, tr.N, tr.ld,
+                                           tr.flags});
                     if (!so2.alive || b + 1 >= L) break;
                     tp = so2.tp;
                     o = so2.org;
@@ -811,29 +820,54 @@ int orc_adjoint_f64(void* sp, const gb_camera* cam, const gb_render_desc* d, int
                         if ((pm >= 0 && v.mi == pm) || (pl >= 0 && v.nee && v.light == pl)) touched = true;
                     if (!touched) continue;
                     Dd T[3] = {cst(1.0), cst(1.0), cst(1.0)}, Cc[3] = {cst(0.0), cst(0.0), cst(0.0)};
+                    double gnee[kReplayBounces] = {}, sm[kReplayBounces] = {}, sr[kReplayBounces] = {};
                     for (int k = 0; k < K; ++k) {
                         const AdjVertex& v = vs[k];
                         MatD m = make_material_d(s.mats_in[v.mi], prm, v.mi == pm ? pk : -1);
+                        float fsm = 0.0f, fsr = 0.0f, fwr = 0.0f;
+                        if (sampling_terms && v.mi == pm) {
+                            float zlo = 0.0f, zhi = 1.0f;
+                            if (d->rng_mode == GB_RNG_MRG32K3A_POOL && !s.lights.empty())
+                                light_pick_interval(s.lights.data(), (int)s.lights.size(), s.overall, v.light, &zlo,
+                                                    &zhi);
+                            sampling_scores(s.mats[v.mi], v.lobe, v.flags, v.wo, v.wi, v.N, v.pdf, zlo, zhi, &fsm,
+                                            &fsr, &fwr);
+                        }
+                        sm[k] = fsm;
+                        sr[k] = fsr;
                         if (v.nee) {
                             Dd bl[3];
                             eval_d(m, v.lobe, vd(v.wo), vd(v.ld), vd(v.N), bl);
                             const gb_light& li = s.lights_in[v.light];
                             for (int c = 0; c < 3; ++c) {
                                 Dd col{li.col[c], (v.light == pl && c == pc) ? 1.0 : 0.0};
-                                Cc[c] = Cc[c] + T[c] * bl[c] * col * cst(v.scale);
+                                Dd term = T[c] * bl[c] * col * cst(v.scale);
+                                Cc[c] = Cc[c] + term;
+                                gnee[k] += (double)(c == 0 ? g.x : (c == 1 ? g.y : g.z)) * term.v;
                             }
                         }
                         if (k + 1 < K) {
                             Dd br[3];
                             eval_d(m, v.lobe, vd(v.wo), vd(v.wi), vd(v.N), br);
+                            // the Walter weight's roughness dependence (sampling terms)
+                            const Dd pdf{v.pdf, pk == 3 ? (double)v.pdf * (double)fwr : 0.0};
                             for (int c = 0; c < 3; ++c) {
-                                Dd t = T[c] * br[c] / cst(v.pdf);
+                                Dd t = T[c] * br[c] / pdf;
                                 if (t.v > 1.0) t = cst(1.0);
                                 T[c] = t / cst(v.q);
                             }
                         }
                     }
-                    acc[j] += ((double)g.x * Cc[0].d + (double)g.y * Cc[1].d + (double)g.z * Cc[2].d) / d->spp;
+                    double dval = (double)g.x * Cc[0].d + (double)g.y * Cc[1].d + (double)g.z * Cc[2].d;
+                    if (sampling_terms && (pk == 3 || pk == 4)) {
+                        // scores times the path terms each decision moves
+                        double after = (double)g.x * miss_end.x + (double)g.y * miss_end.y + (double)g.z * miss_end.z;
+                        for (int k = K - 1; k >= 0; --k) {
+                            if (vs[k].mi == pm) dval += pk == 4 ? sm[k] * (gnee[k] + after) : sr[k] * after;
+                            after += gnee[k];
+                        }
+                    }
+                    acc[j] += dval / d->spp;
                 }
             }
         }

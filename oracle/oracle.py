@@ -38,7 +38,7 @@ def load() -> C.CDLL:
         lib.orc_compute_path_contribution_and_bounce.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                                                  vp, vp, ip, ip, ip]
         lib.orc_render.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp]
-        lib.orc_adjoint_f64.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp, vp]
+        lib.orc_adjoint_f64.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp, ip, vp, vp, ip]
         lib.orc_render_direct.argtypes = [vp, vp, vp, ip, vp, ip, vp]
         lib.orc_render_hybrid_direct.argtypes = [vp, vp, vp, ip, ip, vp, ip, vp]
         lib.orc_halton_pool.argtypes = [ip, vp]
@@ -126,9 +126,11 @@ class OracleScene:
         return (out, st) if with_stats else out
 
     def adjoint_f64(self, cam: dict, rdesc: dict, pool: np.ndarray, dimg: np.ndarray, sel, row0: int = 0,
-                    row1: int | None = None) -> np.ndarray:
+                    row1: int | None = None, sampling_terms: bool = False) -> np.ndarray:
         """FP64 reference gradient of sum(dimg * image[rows]) with respect to
-        the parameters `sel` (gb_scene_param_count layout)."""
+        the parameters `sel` (gb_scene_param_count layout); sampling_terms
+        adds the derivatives of the sampling decisions, as
+        gb_ctx_set_gradient_terms(ctx, 1) does."""
         rd = _gbpt.make_render_desc(rdesc)
         cm = _gbpt.make_camera(cam)
         row1 = rd.height if row1 is None else row1
@@ -139,7 +141,7 @@ class OracleScene:
         sel = np.ascontiguousarray(sel, np.int32)
         out = np.zeros(sel.shape[0], np.float64)
         rc = self.lib.orc_adjoint_f64(self.h, C.byref(cm), C.byref(rd), row0, row1, _p(pool), pool.shape[0], _p(g),
-                                      sel.shape[0], _p(sel), _p(out))
+                                      sel.shape[0], _p(sel), _p(out), 1 if sampling_terms else 0)
         if rc != 0:
             raise ValueError(f"orc_adjoint_f64 failed ({rc})")
         return out

@@ -74,6 +74,45 @@ def test_backward_matches_fp64_replay(gpu_ctx):
     s.close()
 
 
+def test_backward_with_sampling_terms_matches_fp64_replay(gpu_ctx):
+    """gb_ctx_set_gradient_terms(ctx, 1): the device sweep with the
+    derivatives of the sampling decisions (metallic lobe choice, GTR2
+    half-vector density and Walter weight in roughness) against the oracle's
+    FP64 replay with the same terms, on the same MRG32k3a pools, for both
+    light-draw modes; the frozen gradient must differ from it."""
+    from oracle import oracle
+    sc = _scene(seed=9)
+    for mode in (gbpt.GB_RNG_MRG32K3A_POOL, gbpt.GB_RNG_HALTON_LIGHT):
+        rd = dict(sc.render, rng_mode=mode)
+        s = gpu_ctx.scene(sc)
+        rng = np.random.default_rng(3)
+        dimg = rng.normal(size=(rd["height"], rd["width"], 3)).astype(np.float32)
+        frozen = s.backward(sc.camera, rd, dimg)
+        gpu_ctx.set_gradient_terms(True)
+        try:
+            grad = s.backward(sc.camera, rd, dimg)
+        finally:
+            gpu_ctx.set_gradient_terms(False)
+        assert np.isfinite(grad).all()
+        nm = len(sc.materials)
+        rough_metal = np.array([5 * m + k for m in range(nm) for k in (3, 4)])
+        sel = np.union1d(_visible_params(grad, nm, 24, rng), rough_metal)
+        pool = gpu_ctx.mrg_pool(rd["width"] * rd["height"], rd["spp"] * rd["max_bounces"], seed=rd["seed"])
+        orc = oracle.OracleScene(sc, use_bvh=True)
+        ref = orc.adjoint_f64(sc.camera, rd, pool, dimg, sel, sampling_terms=True)
+        orc.close()
+        scale = np.abs(ref).max()
+        err = np.abs(grad[sel].astype(np.float64) - ref)
+        assert (err <= 2e-3 * np.abs(ref) + 2e-5 * scale).all(), (mode, sel[np.argmax(err)], err.max(), scale)
+        # the sampling terms moved the roughness and metallic gradients of
+        # the principled metals (Lambert and glass materials keep theirs)
+        moved = np.abs(grad[rough_metal] - frozen[rough_metal]) > 1e-2 * np.abs(grad[rough_metal]).max()
+        assert moved.sum() >= 4, moved
+        others = np.setdiff1d(np.arange(grad.size), rough_metal)
+        assert np.allclose(grad[others], frozen[others], rtol=1e-4, atol=1e-6 * np.abs(frozen).max())
+        s.close()
+
+
 def test_backward_matches_finite_differences(gpu_ctx):
     """L2 loss to a target rendered with other materials; central
     differences of the frozen-sampling forward.  A path whose throughput
