@@ -504,9 +504,8 @@ def inverse_leg(ctx, args, torch, dist):
         h.set_params(x0)
     outs = [torch.empty_like(t) for t in targets]
     ptrs = [o.data_ptr() for o in outs]
-    # one tensor per scene (scenes have 1-4 lights); only the materials are free
-    xs_t = [torch.tensor(x0, requires_grad=True) for x0 in x_init]
-    opt = torch.optim.Adam(xs_t, lr=1e-2)
+    # one parameter vector per scene (scenes have 1-4 lights); only the
+    # materials are free
     paths = sum(sc.render["width"] * sc.render["height"] * sc.render["spp"] for sc in mixed)
 
     def param_err(xs, visible=None):
@@ -521,38 +520,56 @@ def inverse_leg(ctx, args, torch, dist):
             e[name] = float(np.sqrt(np.mean(np.concatenate(sq)))) if sq else None
         return e
 
-    err0 = param_err([x.detach().numpy() for x in xs_t])
-    visible = None
-    losses = []
-    t_iter = []
     # one fitting step = one CUDA graph launch: parameter upload, batched
     # forward frame, L2 loss and image gradient on the device, batched
     # adjoint, gradient reduction (gb_fit_step)
     ctx.fit_prepare(jobs, [t.data_ptr() for t in targets], ptrs)
-    for it in range(args.inverse_iters):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        g, lv = ctx.fit_step([x.detach().numpy() for x in xs_t])
-        t_iter.append(time.perf_counter() - t0)
-        losses.append(float(lv.sum()))
-        if visible is None:
-            # materials that influence their image: colour-gradient norm at the
-            # start above 1 % of the scene's largest
-            visible = []
-            for gi in g:
-                gn = np.linalg.norm(gi[:nmp].reshape(64, 5)[:, :3], axis=1)
-                visible.append(gn > 1e-2 * max(gn.max(), 1e-30))
-            err0_vis = param_err([x.detach().numpy() for x in xs_t], visible)
-        for x, gi in zip(xs_t, g):
-            gt = torch.from_numpy(gi)
-            gt[nmp:] = 0.0
-            x.grad = gt
-        opt.step()
-        with torch.no_grad():
-            for x in xs_t:
-                x[:nmp] = x[:nmp].clamp(0.0, 1.0)
-    err1 = param_err([x.detach().numpy() for x in xs_t])
-    err1_vis = param_err([x.detach().numpy() for x in xs_t], visible) if visible is not None else None
+
+    def fit(sampling):
+        """Adam from the initial materials with the frozen-sampling gradient
+        or with the derivatives of the sampling decisions."""
+        ctx.set_gradient_terms(sampling)
+        xs_t = [torch.tensor(x0, requires_grad=True) for x0 in x_init]
+        opt = torch.optim.Adam(xs_t, lr=1e-2)
+        visible = None
+        losses, t_iter = [], []
+        for it in range(args.inverse_iters):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g, lv = ctx.fit_step([x.detach().numpy() for x in xs_t])
+            t_iter.append(time.perf_counter() - t0)
+            losses.append(float(lv.sum()))
+            if visible is None:
+                # materials that influence their image: colour-gradient norm
+                # at the start above 1 % of the scene's largest
+                visible = []
+                for gi in g:
+                    gn = np.linalg.norm(gi[:nmp].reshape(64, 5)[:, :3], axis=1)
+                    visible.append(gn > 1e-2 * max(gn.max(), 1e-30))
+            for x, gi in zip(xs_t, g):
+                gt = torch.from_numpy(gi)
+                gt[nmp:] = 0.0
+                x.grad = gt
+            opt.step()
+            with torch.no_grad():
+                for x in xs_t:
+                    x[:nmp] = x[:nmp].clamp(0.0, 1.0)
+        ctx.set_gradient_terms(False)
+        xs = [x.detach().numpy() for x in xs_t]
+        return {"gradient": "sampling decisions differentiated" if sampling else "frozen sampling",
+                "param_rmse_final": param_err(xs),
+                "visible_materials": int(sum(int(v.sum()) for v in visible)) if visible is not None else 0,
+                "param_rmse_initial_visible": param_err(x_init, visible) if visible is not None else None,
+                "param_rmse_final_visible": param_err(xs, visible) if visible is not None else None,
+                "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None,
+                }, t_iter
+
+    err0 = param_err(x_init)
+    fits = {}
+    t_iter = []
+    for name, sampling in (("frozen", False), ("sampling", True)):
+        fits[name], t = fit(sampling)
+        t_iter += t[1:] if len(t) > 1 else t
     # the same iteration as 16 sequential plain runs (gb_render + gb_backward per scene)
     seq = []
     for _ in range(max(3, args.steps)):
@@ -566,16 +583,12 @@ def inverse_leg(ctx, args, torch, dist):
         seq.append(time.perf_counter() - t0)
     for h, x0 in zip(handles, x_init):
         h.close()
-    it_s = float(np.median(t_iter[1:] if len(t_iter) > 1 else t_iter))
+    it_s = float(np.median(t_iter))
     seq_s = float(np.median(seq))
     return {"workload": {"scenes": n_sc, "triangles": [int(sc.num_triangles) for sc in mixed], "resolution": 256,
                          "spp": 8, "max_bounces": 4, "materials_per_scene": 64, "iterations": args.inverse_iters,
                          "optimizer": "Adam lr 1e-2 on base colour, roughness, metallic"},
-            "param_rmse_initial": err0, "param_rmse_final": err1,
-            "visible_materials": int(sum(int(v.sum()) for v in visible)) if visible is not None else 0,
-            "param_rmse_initial_visible": err0_vis if visible is not None else None,
-            "param_rmse_final_visible": err1_vis,
-            "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None,
+            "param_rmse_initial": err0, "fits": fits,
             "iteration_ms": it_s * 1e3, "sequential_iteration_ms": seq_s * 1e3,
             "batched_over_sequential": seq_s / it_s,
             "mpaths_per_s_fwd_plus_bwd": 2 * paths / it_s / 1e6,

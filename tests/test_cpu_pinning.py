@@ -8,8 +8,9 @@ driven through the sample_material / evaluate_material sequence of
 hybrid-pt.cpp:330-371, and rta::generate_arealight_sample of
 arealight-sampler-cpu.cpp.  The reference evaluates sin/cos through libm and
 some intermediate products in double; this build uses its own float
-sin/cos(2 pi u) and float arithmetic, so shading agrees to a tolerance while
-the area-light sample (only + - * / sqrt) agrees bit for bit.
+sin/cos(2 pi u) and float arithmetic, so shading agrees to a relative 1e-4 (every case outside it
+is shown to be ill-conditioned: one ulp of input covers the difference)
+while the area-light sample (only + - * / sqrt) agrees bit for bit.
 """
 from pathlib import Path
 
@@ -25,21 +26,48 @@ def _close(a, b, rtol, atol):
     return np.abs(a.astype(np.float64) - b) <= rtol * np.abs(b.astype(np.float64)) + atol
 
 
+def _shade_ok(mine, ref, rtol):
+    ok_dir = _close(mine[..., 0:3], ref[..., 0:3], 0.0, 2e-5).all(axis=-1)
+    ok_pdf = _close(mine[..., 3], ref[..., 3], rtol, 1e-7)
+    ok_f = _close(mine[..., 4:10], ref[..., 4:10], rtol, 1e-6).all(axis=-1)
+    return ok_dir & ok_pdf & ok_f
+
+
+def _ulp_nudges(args):
+    """The case's inputs with one component of the random numbers, the ray
+    direction or the raw normal moved by one ulp either way."""
+    for which in (5, 4, 3):  # rnd, ray_dir, n_raw
+        for k in range(3):
+            for toward in (np.float32(2.0), np.float32(-2.0)):
+                a = list(args)
+                v = np.array(a[which], np.float32, copy=True)
+                v[k] = np.nextafter(v[k], toward, dtype=np.float32)
+                a[which] = v
+                yield a
+
+
 def test_shade_matches_reference_golden():
+    """Relative 1e-4 on the pdf and BRDF values, 2e-5 on directions.  A case
+    outside that must be ill-conditioned: some one-ulp change of one input
+    component (the reference evaluates sin/cos through libm and some products
+    in double, this build in float) moves this build's result to within 1e-4
+    of the reference's.  Such cases are logged and must stay rare."""
     from oracle import oracle
     g = np.load(GOLDEN / "shade_cases.npz")
     ref = g["out"]
     n = ref.shape[0]
-    mine = np.stack([oracle.shade_eval(g["diffuse"][i], bool(g["principled"][i]), g["params"][i], g["n_raw"][i],
-                                       g["ray_dir"][i], g["rnd"][i], g["to_light"][i]) for i in range(n)])
+    case = lambda i: [g["diffuse"][i], bool(g["principled"][i]), g["params"][i], g["n_raw"][i], g["ray_dir"][i],
+                      g["rnd"][i], g["to_light"][i]]
+    mine = np.stack([oracle.shade_eval(*case(i)) for i in range(n)])
     assert np.array_equal(mine[:, 10], ref[:, 10]), "glass flag"
-    ok_dir = _close(mine[:, 0:3], ref[:, 0:3], 0.0, 2e-5).all(axis=1)
-    ok_pdf = _close(mine[:, 3], ref[:, 3], 2e-4, 1e-7)
-    ok_f = _close(mine[:, 4:10], ref[:, 4:10], 2e-4, 1e-6).all(axis=1)
-    ok = ok_dir & ok_pdf & ok_f
-    # a case may leave the tolerance only where the reference's lobe decision
-    # (glass Fresnel test, GTR2 fallback) sits on a rounding boundary
-    assert ok.mean() >= 0.998, f"{(~ok).sum()} of {n} shading cases differ"
+    ok = _shade_ok(mine, ref, 1e-4)
+    explained = []
+    for i in np.flatnonzero(~ok):
+        near = [a for a in _ulp_nudges(case(i)) if _shade_ok(oracle.shade_eval(*a), ref[i], 1e-4)]
+        assert near, f"case {i} (kind {g['kind'][i]}) differs and is not within one ulp of an input"
+        explained.append(int(i))
+    print(f"shading cases outside 1e-4 that one ulp of input reproduces: {explained}")
+    assert len(explained) <= n // 1000
     # every material family is covered
     for k in range(5):
         assert (g["kind"] == k).sum() > 100

@@ -151,6 +151,71 @@ def test_backward_matches_finite_differences(gpu_ctx):
     s.close()
 
 
+def _plain_differences(s, sc, rd, x0, w, sel, h):
+    """Central differences of sum(w * frame) of the plain frame (gb_render
+    after gb_scene_set_params: every random number the same, every sampling
+    decision re-made) at steps h and h / 2."""
+    loss = lambda: float((s.render(sc.camera, rd).astype(np.float64) * w).sum())
+    out = []
+    for hh in (h, 0.5 * h):
+        d = []
+        for i in sel:
+            xp, xm = x0.copy(), x0.copy()
+            xp[i] += hh
+            xm[i] -= hh
+            s.set_params(xp)
+            lp = loss()
+            s.set_params(xm)
+            d.append((lp - loss()) / (2 * hh))
+        out.append(np.array(d))
+    s.set_params(x0)
+    return out
+
+
+def test_backward_matches_plain_frame_differences(gpu_ctx):
+    """The gradient against central differences of the plain frame at common
+    random numbers, relative error <= 1e-3 for each parameter.
+    * Lambert room (Halton light draws, no roulette, one light): the frame
+      is a polynomial in every albedo and the light colour (brdf / pdf =
+      albedo < 1 never reaches the throughput clamp, no sampling decision
+      depends on them), so every parameter with a gradient is checked.
+    * Principled icospheres (black background, no roulette): colours and
+      light colours.  A throughput reaching the clamp, or a sampling decision
+      that a colour moves, puts a kink or a jump in the frame; parameters
+      whose differences at h and h / 2 disagree by more than 1e-4 are not
+      smooth at that scale and are skipped; most must qualify."""
+    sc = scenes.cornell(width=32, height=32, spp=4, max_bounces=5)
+    rd = sc.render
+    s = gpu_ctx.scene(sc)
+    x0 = s.get_params()
+    w = np.random.default_rng(5).uniform(0.0, 1.0, (rd["height"], rd["width"], 3))
+    grad = s.backward(sc.camera, rd, w.astype(np.float32)).astype(np.float64)
+    nm = len(sc.materials)
+    sel = np.array([5 * m + c for m in range(nm) for c in range(3)] + [5 * nm + c for c in range(3)])
+    sel = sel[np.abs(grad[sel]) > 1e-6 * np.abs(grad).max()]
+    assert sel.size >= 18
+    d1, d2 = _plain_differences(s, sc, rd, x0, w, sel, 1e-3)
+    rel = np.abs(grad[sel] - d2) / np.abs(d2)
+    assert rel.max() <= 1e-3, (sel[np.argmax(rel)], rel.max())
+    s.close()
+
+    sc = _scene(seed=11, rr=-1)
+    rd = dict(sc.render, background=(0.0, 0.0, 0.0))
+    s = gpu_ctx.scene(sc)
+    x0 = s.get_params()
+    w = np.random.default_rng(6).uniform(0.0, 1.0, (rd["height"], rd["width"], 3))
+    grad = s.backward(sc.camera, rd, w.astype(np.float32)).astype(np.float64)
+    nm, nl = len(sc.materials), len(sc.lights)
+    sel = np.array([5 * m + c for m in range(nm) for c in range(3)] + [5 * nm + c for c in range(3 * nl)])
+    sel = sel[np.abs(grad[sel]) > 1e-3 * np.abs(grad).max()]
+    d1, d2 = _plain_differences(s, sc, rd, x0, w, sel, 1e-3)
+    smooth = np.abs(d1 - d2) <= 1e-4 * np.abs(d2)
+    assert smooth.mean() >= 0.6, (smooth.sum(), sel.size)
+    rel = np.abs(grad[sel] - d2) / np.abs(d2)
+    assert rel[smooth].max() <= 1e-3, (sel[smooth][np.argmax(rel[smooth])], rel[smooth].max())
+    s.close()
+
+
 def test_backward_batch_equals_single(gpu_ctx):
     a, b = _scene(seed=3, w=40, h=24, spp=3), _scene(seed=5, w=24, h=24, spp=5, bounces=3)
     sa, sb = gpu_ctx.scene(a), gpu_ctx.scene(b)
