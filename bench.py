@@ -686,11 +686,20 @@ def run_gbpt(args, rank, world):
     ist = ctx.stats()
     node_b, tri_b = 80, 36
     ext_rays = ist["camera_rays"] + ist["extension_rays"]
-    closest_bytes = ist["closest_node_visits"] * node_b + ist["closest_tri_tests"] * tri_b + ext_rays * 48
+    trav_bytes = ist["closest_node_visits"] * node_b + ist["closest_tri_tests"] * tri_b + ext_rays * 48
+    # the light sample k_extend takes at every hit, and a miss's end of path:
+    # per hit the hit triangle's positions and normals (72 B), the light
+    # record (64 B), one draw of three uniforms (12 B), the shadow ray out
+    # (32 B) and its potential contribution (12 B); per miss the throughput
+    # and accumulation in (24 B) and the sample out (12 B)
+    hits = ist["light_samples"]
+    misses = ext_rays - hits
+    closest_bytes = trav_bytes + hits * (72 + 64 + 12 + 32 + 12) + misses * 36
     ext_ms = stage_ms[1]          # per frame
     ext_launches = stage_n[1]
     peak, peak_kind = measured_peaks()
     achieved = closest_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
+    achieved_trav = trav_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
     rays = ist["camera_rays"] + ist["extension_rays"] + ist["shadow_rays"]
     mrays = rays / (total_ms / args.steps / 1e3) / 1e6
 
@@ -721,8 +730,15 @@ def run_gbpt(args, rank, world):
                          "traffic_source": "ncu dram__bytes_read+write of k_extend per closest-hit ray "
                                            "(warm L2, whole 4-spp frame of this workload) x rays per launch",
                          "algorithmic_bytes_per_launch": closest_bytes / max(1.0, ext_launches),
-                         "bytes_model": "node visits*80 + tri tests*36 + 48 per ray (counted by the instrumented "
-                                        "traversal of the same frame)"},
+                         "bytes_model": "per ray: node visits*80 + tri tests*36 + 32 ray in + 16 hit out; per hit "
+                                        "(light sample): 72 hit triangle positions+normals + 64 light + 12 draw + "
+                                        "32 shadow ray out + 12 potential contribution; per miss: 24 in + 12 "
+                                        "sample out (counts from the instrumented render of the same frame)",
+                         "traversal_only": {"achieved": achieved_trav,
+                                            "frac": (achieved_trav / peak) if achieved_trav else None,
+                                            "bytes_per_launch": trav_bytes / max(1.0, ext_launches),
+                                            "bytes_model": "node visits*80 + tri tests*36 + 48 per ray"},
+                         "closest_hits_per_frame": int(hits), "misses_per_frame": int(misses)},
             "clocks": clocks,
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": W * H * 3 * 4},

@@ -114,6 +114,7 @@ struct gb_ctx {
     int blocks_per_sm = 0;              // resident traversal blocks per SM (0 = occupancy limit)
     int stack_depth = 32;               // traversal stack entries (24 or 32)
     int sampling_terms = 0;             // adjoint: add the derivatives of the sampling decisions
+    size_t l2_persist = 0;              // persisting L2 set-aside this context asked for (GB_NODE_L2_PERSIST)
     int block_threads = 128;            // threads per traversal block (64 or 128)
     int slots = 1 << 20;                // path slots in flight (upper bound)
     int sample_mb = 1024;               // sample buffer budget (chunk size)
@@ -150,6 +151,14 @@ struct gb_scene {
     void* shade_buf = nullptr;
     std::vector<int> mat_dtex;  // diffuse texture of each material (-1 = none)
 };
+
+// GB_NODE_L2_PERSIST: a frame of one scene keeps the scene's node array in a
+// persisting L2 set-aside (cudaLimitPersistingL2CacheSize, released when the
+// context is destroyed), given to the traversal launches as an access-policy
+// window
+#ifndef GB_NODE_L2_PERSIST
+#define GB_NODE_L2_PERSIST 1
+#endif
 
 namespace {
 
@@ -357,9 +366,9 @@ int gb_ctx_create(const gb_ctx_desc* desc, gb_ctx** out) {
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(unsigned long long) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(unsigned long long) * 16);
     if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMemset(ctx->d_stats, 0, sizeof(unsigned long long) * 8);
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_stats, 0, sizeof(unsigned long long) * 16);
     if (e == cudaSuccess) e = cudaHostAlloc((void**)&ctx->snap_host, sizeof(uint32_t) * kSnaps, cudaHostAllocDefault);
     for (int k = 0; k < kSnaps && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->snap_ev[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -395,6 +404,12 @@ void gb_ctx_destroy(gb_ctx* ctx) {
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_stats) cudaFree(ctx->d_stats);
+    if (ctx->l2_persist) {
+        // give back the persisting L2 set-aside this context asked for
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+        cudaGetLastError();
+    }
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -763,7 +778,7 @@ int chunk_end(const gb_ctx* ctx, int p0, int end, long long* paths) {
 // every pixel reset to them.  Captured into the fitting graph as well.
 int enqueue_frame_setup(gb_ctx* ctx, cudaStream_t st, const SceneRec* recs, bool record_start) {
     const Frame& F = ctx->F;
-    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * 8, st));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * 16, st));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), st));
     if (record_start) CK(cudaEventRecord(ctx->ev0, st));
     CK(cudaMemcpyAsync(ctx->d_scenes, recs, sizeof(SceneRec) * ctx->recs.size(), cudaMemcpyHostToDevice, st));
@@ -1063,6 +1078,24 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
         if (b.scene->S.texcoord) P.textured = 1;
     P.p0 = p0;
     P.rounds = p1 - p0;
+#if GB_NODE_L2_PERSIST
+    // a frame of one scene keeps its node array in a persisting L2 set-aside
+    if (ctx->items.size() == 1) {
+        const DevScene& S = ctx->items[0].scene->S;
+        int dev = 0, max_persist = 0, max_window = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+        const size_t bytes = std::min({(size_t)80 * (size_t)S.n_nodes, (size_t)max_persist, (size_t)max_window});
+        if (bytes > ctx->l2_persist && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes) == cudaSuccess)
+            ctx->l2_persist = bytes;
+        cudaGetLastError();
+        if (bytes > 0 && ctx->l2_persist >= bytes) {
+            P.l2_nodes = S.nodes;
+            P.l2_nodes_bytes = bytes;
+        }
+    }
+#endif
     long long acc = 0, n_last = 0;
     for (int r = 0; r < P.rounds; ++r) {
         P.round_start[r] = (uint32_t)acc;
@@ -1147,7 +1180,7 @@ int copy_scene(gb_ctx* ctx, const BatchScene& b, float* out, int out_is_device) 
 // Waits for the frame, gathers its statistics and reports kernel status.
 int finish_frame(gb_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
-    unsigned long long st[8];
+    unsigned long long st[16];
     CK(cudaMemcpy(st, ctx->d_stats, sizeof(st), cudaMemcpyDeviceToHost));
     ctx->stats.camera_rays = st[0];
     ctx->stats.extension_rays = st[1];
@@ -1156,6 +1189,7 @@ int finish_frame(gb_ctx* ctx) {
     ctx->stats.closest_tri_tests = st[4];
     ctx->stats.shadow_node_visits = st[5];
     ctx->stats.shadow_tri_tests = st[6];
+    ctx->stats.light_samples = st[8];
     // every slot-pool iteration (counted by k_step in st[7]) is 4 launches
     // (extend, shadow, shade, step), 6 with the adjoint sweep
     ctx->stats.kernel_launches = ctx->launches + (uint64_t)k_launches_per_iteration(ctx->mode) * st[7];

@@ -61,6 +61,9 @@ constexpr int kIterLimit = 1 << 22;
 #ifndef GB_STREAM_MIN_BLOCKS
 #define GB_STREAM_MIN_BLOCKS 1
 #endif
+#ifndef GB_NODE_FOLD
+#define GB_NODE_FOLD 0  // 1: plane bias folded into the per-node origin term
+#endif
 #ifndef GB_FUSED_RESTART
 #define GB_FUSED_RESTART 1  // paths ended by a miss restart in k_shadow's warps
 #endif
@@ -134,6 +137,20 @@ __device__ __forceinline__ float4 ld_tri(const float4* p) {
     return __ldg(p);
 #endif
 }
+// The hit triangle's shading record (positions and normals for the hit
+// point), read once per hit with little reuse across a frame: with
+// GB_SHADE_EVICT_FIRST the load is marked evict-first (ld.global.cs), so
+// that the 98 MB array streaming past does not push the tree out of L2.
+#ifndef GB_SHADE_EVICT_FIRST
+#define GB_SHADE_EVICT_FIRST 0
+#endif
+__device__ __forceinline__ float4 ld_shade(const float4* p) {
+#if GB_SHADE_EVICT_FIRST
+    return __ldcs(p);
+#else
+    return __ldg(p);
+#endif
+}
 __device__ __forceinline__ float4 ld_node(const float4* p) {
 #if GB_NODE_L2_128
     float4 v;
@@ -197,6 +214,13 @@ __device__ __forceinline__ uint32_t xor_permute8(uint32_t m, uint32_t x) {
 // entry distance is shrunk and the exit distance grown by 1e-5 relative on
 // top of the outward-rounded boxes.  Empty slots (meta 0, imask bit 0) may
 // test positive; they add neither a node nor a triangle.
+// Plane distances (GB_NODE_FOLD): q a + o is evaluated as one packed FMA
+// (2^15 + q) a + (o - 2^15 a).  One PRMT places byte q in bits 8-15 of the
+// float 2^15, which is then exactly 2^15 + q; the bias -2^15 a is folded
+// into the per-node origin term, whose rounding (at most |a| 2^-9 per
+// rounding, two roundings) is covered by moving near planes down and far
+// planes up by |a| / 64, a 64th of a quantisation step.  Without the fold,
+// byte q is made exact as (2^23 + q) - 2^23 (PRMT + packed FADD).
 __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes, uint32_t ni, const RayInv& r,
                                                float bound, uint2* ng, uint2* tg) {
     const float4* n = nodes + 5 * (size_t)ni;
@@ -209,8 +233,16 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
     const float aix = sx * r.idir.x, aiy = sy * r.idir.y, aiz = sz * r.idir.z;
     const uint64_t AX = pack2(aix, aix), AY = pack2(aiy, aiy), AZ = pack2(aiz, aiz);
     const float aox = (n0.x - r.o.x) * r.idir.x, aoy = (n0.y - r.o.y) * r.idir.y, aoz = (n0.z - r.o.z) * r.idir.z;
+#if GB_NODE_FOLD
+    const float bx = fmaf(-32768.0f, aix, aox), by = fmaf(-32768.0f, aiy, aoy), bz = fmaf(-32768.0f, aiz, aoz);
+    const float ex = fabsf(aix) * 0.015625f, ey = fabsf(aiy) * 0.015625f, ez = fabsf(aiz) * 0.015625f;
+    const uint64_t ONX = pack2(bx - ex, bx - ex), ONY = pack2(by - ey, by - ey), ONZ = pack2(bz - ez, bz - ez);
+    const uint64_t OFX = pack2(bx + ex, bx + ex), OFY = pack2(by + ey, by + ey), OFZ = pack2(bz + ez, bz + ez);
+#else
     const uint64_t OX = pack2(aox, aox), OY = pack2(aoy, aoy), OZ = pack2(aoz, aoz);
+    const uint64_t ONX = OX, ONY = OY, ONZ = OZ, OFX = OX, OFY = OY, OFZ = OZ;
     const uint64_t BIAS = pack2(-8388608.0f, -8388608.0f);
+#endif
     const uint64_t KN = pack2(0.99999f, 0.99999f), KF = pack2(1.00001f, 1.00001f);
     const bool fx = r.idir.x < 0.0f, fy = r.idir.y < 0.0f, fz = r.idir.z < 0.0f;
     uint32_t hm = 0;  // child hits by slot
@@ -226,16 +258,22 @@ __device__ __forceinline__ void intersect_node(const float4* __restrict__ nodes,
         for (uint32_t j = 0; j < 4; j += 2) {
             // plane index bytes j, j+1 as floats 2^23 + q (PRMT), minus 2^23
             // (exact), then the plane distance q * a + o (packed FMA)
+#if GB_NODE_FOLD
+#define GB_PLANES(w, A, O) fma2(pack2(__uint_as_float(__byte_perm(w, 0x47000000u, 0x7604u | (j << 4))),          \
+                                      __uint_as_float(__byte_perm(w, 0x47000000u, 0x7604u | ((j + 1u) << 4)))), \
+                                A, O)
+#else
 #define GB_PLANES(w, A, O) fma2(add2(pack2(__uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | j)),          \
                                             __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | (j + 1u)))), \
                                       BIAS), A, O)
+#endif
             float tnx0, tnx1, tny0, tny1, tnz0, tnz1, tfx0, tfx1, tfy0, tfy1, tfz0, tfz1;
-            unpack2(GB_PLANES(nx, AX, OX), tnx0, tnx1);
-            unpack2(GB_PLANES(ny, AY, OY), tny0, tny1);
-            unpack2(GB_PLANES(nz, AZ, OZ), tnz0, tnz1);
-            unpack2(GB_PLANES(fxw, AX, OX), tfx0, tfx1);
-            unpack2(GB_PLANES(fyw, AY, OY), tfy0, tfy1);
-            unpack2(GB_PLANES(fzw, AZ, OZ), tfz0, tfz1);
+            unpack2(GB_PLANES(nx, AX, ONX), tnx0, tnx1);
+            unpack2(GB_PLANES(ny, AY, ONY), tny0, tny1);
+            unpack2(GB_PLANES(nz, AZ, ONZ), tnz0, tnz1);
+            unpack2(GB_PLANES(fxw, AX, OFX), tfx0, tfx1);
+            unpack2(GB_PLANES(fyw, AY, OFY), tfy0, tfy1);
+            unpack2(GB_PLANES(fzw, AZ, OFZ), tfz0, tfz1);
 #undef GB_PLANES
             float lo0, lo1, hi0, hi1;
             unpack2(mul2(pack2(max3(tnx0, tny0, fmaxf(tnz0, 0.0f)), max3(tnx1, tny1, fmaxf(tnz1, 0.0f))), KN), lo0,
@@ -831,7 +869,9 @@ __device__ __forceinline__ bool coop_triangles(bool act, const float4* tris, con
 // exhausted), and traversal resumes where each lane stopped.  The first
 // wave is assigned by warp index (warp w takes entries [32w, 32w+32)); later
 // fetches take one atomic per warp on `head`.  Each lane carries the
-// geometry of its own scene.
+// geometry of its own scene.  fetch(q, &handle, ...) loads queue entry q's
+// ray and sets the handle that finish(fin, handle, trav, t_max) gets back
+// when the ray is done.
 template <bool ANY, bool INSTR, int MODE, int STACK, int BT, typename Fetch, typename Finish>
 __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int refill, uint32_t* status, Fetch fetch,
                                          Finish finish, uint32_t* nvis, uint32_t* ntri) {
@@ -840,7 +880,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
     const uint32_t dyn0 = nwarps * 32u;
     const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     bool act = false, fin = false, exhausted = false, first = true;
-    uint32_t qi = 0;
+    uint32_t qi = 0;  // the lane's handle for finish, as fetch sets it
     int iters = 0;
     RayInv r;
     float tmax = 0.0f;
@@ -854,7 +894,7 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
     __shared__ unsigned long long s_key[MODE == 3 ? BT : 1];
     unsigned long long* skey = s_key + (MODE == 3 ? (threadIdx.x & ~31u) : 0u);
     while (true) {
-        finish(fin, qi, s);
+        finish(fin, qi, s, tmax);
         fin = false;
         uint32_t idle = __ballot_sync(0xffffffffu, !act);
         if (!exhausted && idle) {
@@ -874,9 +914,8 @@ __device__ __forceinline__ void ray_loop(uint32_t count, uint32_t* head, int ref
             if (!act) {
                 uint32_t q = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (q < count) {
-                    qi = q;
                     v3 o, d;
-                    if (fetch(q, &o, &d, &tmax, &nodes, &tris, &shade)) {
+                    if (fetch(q, &qi, &o, &d, &tmax, &nodes, &tris, &shade)) {
                         r = make_ray(o, d);
                         trav_init(s, r);
                         iters = 0;
@@ -993,10 +1032,13 @@ __global__ void __launch_bounds__(BT, GB_TRAV_MIN_BLOCKS * 128 / BT) k_extend(Fr
     const uint32_t count = cs[0];
     const uint32_t* qin = F.q[it & 1];
     uint32_t* qsh = F.q[2];
-    uint32_t nvis = 0, ntri = 0;
-    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
-                     const float4** shade) {
-        uint32_t slot = qin[q];
+    uint32_t nvis = 0, ntri = 0, nhit = 0;
+    // the handle finish gets back is the queue entry: re-reading the slot
+    // there costs less than keeping it live through the traversal
+    auto fetch = [&](uint32_t q, uint32_t* handle, v3* o, v3* d, float* tmax, const float4** nodes,
+                     const float4** tris, const float4** shade) {
+        const uint32_t slot = qin[q];
+        *handle = q;
         float4 ro = F.ray_o.ld(slot), rd = F.ray_d.ld(slot);
         const SceneRec& R = scene_of(F, slot);
         *nodes = R.S.nodes;
@@ -1005,7 +1047,7 @@ __global__ void __launch_bounds__(BT, GB_TRAV_MIN_BLOCKS * 128 / BT) k_extend(Fr
         *o = ld3(ro); *d = ld3(rd); *tmax = ro.w;
         return true;
     };
-    auto finish = [&](bool fin, uint32_t q, const Trav& h) {
+    auto finish = [&](bool fin, uint32_t q, const Trav& h, float) {
         bool hit = false, ended = false;
         uint32_t slot = 0;
         if (fin) {
@@ -1022,9 +1064,10 @@ __global__ void __launch_bounds__(BT, GB_TRAV_MIN_BLOCKS * 128 / BT) k_extend(Fr
                 ended = true;
             } else {
                 const DevScene& S = R.S;
+                if (INSTR) ++nhit;
                 const float4* sh = S.shade + 6 * (size_t)h.best_id;
-                float4 a = __ldg(sh + 0), b = __ldg(sh + 1), c = __ldg(sh + 2);
-                float4 na = __ldg(sh + 3), nb = __ldg(sh + 4), nc = __ldg(sh + 5);
+                float4 a = ld_shade(sh + 0), b = ld_shade(sh + 1), c = ld_shade(sh + 2);
+                float4 na = ld_shade(sh + 3), nb = ld_shade(sh + 4), nc = ld_shade(sh + 5);
                 v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
                 v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
                 if (!GB_SPLIT_NEE) nee_at_hit(F, R, slot, Pp, Nr, P.mode != MODE_ADJOINT);
@@ -1036,7 +1079,11 @@ __global__ void __launch_bounds__(BT, GB_TRAV_MIN_BLOCKS * 128 / BT) k_extend(Fr
         end_paths(F, ended, slot, cn);
     };
     ray_loop<false, INSTR, MODE, STACK, BT>(count, cs + 1, P.refill, F.status, fetch, finish, &nvis, &ntri);
-    if (INSTR) { add_stats(&F.stats[3], nvis); add_stats(&F.stats[4], ntri); }
+    if (INSTR) {
+        add_stats(&F.stats[3], nvis);
+        add_stats(&F.stats[4], ntri);
+        add_stats(&F.stats[8], nhit);
+    }
 }
 
 // Light samples of every hit of the iteration (shadow queue), when they are
@@ -1060,9 +1107,11 @@ __global__ void __launch_bounds__(BT, GB_SHADOW_MIN_BLOCKS * 128 / BT) k_shadow(
     const uint32_t count = cs[2];
     const uint32_t* qsh = F.q[2];
     uint32_t nvis = 0, ntri = 0;
-    auto fetch = [&](uint32_t q, v3* o, v3* d, float* tmax, const float4** nodes, const float4** tris,
-                     const float4** shade) {
-        uint32_t slot = qsh[q];
+    // the handle finish gets back is the slot
+    auto fetch = [&](uint32_t q, uint32_t* handle, v3* o, v3* d, float* tmax, const float4** nodes,
+                     const float4** tris, const float4** shade) {
+        const uint32_t slot = qsh[q];
+        *handle = slot;
         float4 so = F.sh_o.ld(slot), sd = F.sh_d.ld(slot);
         const SceneRec& R = scene_of(F, slot);
         *nodes = R.S.nodes;
@@ -1073,10 +1122,9 @@ __global__ void __launch_bounds__(BT, GB_SHADOW_MIN_BLOCKS * 128 / BT) k_shadow(
         if (traced) add_stats_lane(&F.stats[2]);  // shadow rays traced
         return traced;
     };
-    auto finish = [&](bool fin, uint32_t q, const Trav& h) {
+    // smax: the shadow ray's max_t (negative: a dark sample, not traced)
+    auto finish = [&](bool fin, uint32_t slot, const Trav& h, float smax) {
         if (fin) {
-            uint32_t slot = qsh[q];
-            float smax = F.sh_o.ld(slot).w;
             bool occl = smax < 0.0f || h.best_id != 0xffffffffu;
             rec_st(reinterpret_cast<float*>(&F.sh_d[slot]) + 3, occl ? 1.0f : 0.0f);
         }
@@ -1719,10 +1767,37 @@ cudaError_t k_launch_start(const Frame& F, const RenderParams& P, int nstart, cu
     return cudaGetLastError();
 }
 
+// Launch of a traversal kernel; with an L2 window in P (the scene's node
+// array) the launch carries it as an access-policy attribute: node lines
+// persist in the L2 set-aside, so that the per-iteration state streaming
+// past does not evict them.
+template <typename K>
+void launch_traversal(K kernel, dim3 grid, int block, const Frame& F, const RenderParams& P, cudaStream_t st) {
+    if (P.l2_nodes_bytes == 0) {
+        kernel<<<grid, block, 0, st>>>(F, P);
+        return;
+    }
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    at[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(P.l2_nodes);
+    at[0].val.accessPolicyWindow.num_bytes = (size_t)P.l2_nodes_bytes;
+    at[0].val.accessPolicyWindow.hitRatio = 1.0f;
+    at[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    at[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, F, P);
+}
+
 template <bool INSTR, int MODE, int STACK, int BT>
 void launch_extend_v(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static Grid g = persistent_grid(k_extend<INSTR, MODE, STACK, BT>, BT);
-    k_extend<INSTR, MODE, STACK, BT><<<traversal_grid(g, P.blocks_per_sm, BT), BT, 0, st>>>(F, P);
+    launch_traversal(k_extend<INSTR, MODE, STACK, BT>, traversal_grid(g, P.blocks_per_sm, BT), BT, F, P, st);
 }
 
 // The default triangle policy has variants for two stack depths and two
@@ -1742,7 +1817,7 @@ void launch_extend_t(const Frame& F, const RenderParams& P, cudaStream_t st) {
 template <bool INSTR, int MODE, int STACK, int BT>
 void launch_shadow_v(const Frame& F, const RenderParams& P, cudaStream_t st) {
     static Grid g = persistent_grid(k_shadow<INSTR, MODE, STACK, BT>, BT);
-    k_shadow<INSTR, MODE, STACK, BT><<<traversal_grid(g, P.blocks_per_sm, BT), BT, 0, st>>>(F, P);
+    launch_traversal(k_shadow<INSTR, MODE, STACK, BT>, traversal_grid(g, P.blocks_per_sm, BT), BT, F, P, st);
 }
 
 template <bool INSTR, int MODE>

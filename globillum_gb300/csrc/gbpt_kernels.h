@@ -176,7 +176,8 @@ struct Frame {
     uint32_t* ctr;     // 3 sets of 8 (by iteration % 3): count, ext head, shadow count, shadow head, ended
     uint32_t* path_ctr;  // next path of the chunk to start
     int* iter;         // iteration index of the chunk's slot-pool loop
-    unsigned long long* stats;  // 0 camera, 1 ext, 2 shadow rays; 3/4 closest, 5/6 shadow node visits / tri tests
+    unsigned long long* stats;  // 0 camera, 1 ext, 2 shadow rays; 3/4 closest, 5/6 shadow node visits / tri tests;
+                                // 7 iterations; 8 closest hits (light samples); 16 words
     uint32_t* status;
     // frozen-sampling replay: throughput of the path under the sampling records
     float4* tp0;
@@ -225,6 +226,10 @@ struct RenderParams {
     int mode;          // MODE_*
     int textured;      // some scene of the frame has textures (k_shade's texture variant)
     int p0, rounds;    // path samples p0 .. p0+rounds-1
+    // L2 window of the traversal launches (GB_NODE_L2_PERSIST, frames of one
+    // scene): the scene's node array, accessed as persisting
+    const void* l2_nodes;
+    unsigned long long l2_nodes_bytes;
     uint32_t chunk_paths;  // paths of the chunk
     uint32_t round_start[kMaxRounds + 1];  // first path index of each round (prefix sums of N_p)
 };

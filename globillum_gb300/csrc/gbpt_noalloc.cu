@@ -53,7 +53,7 @@ constexpr size_t kV4 = align_up(sizeof(float4) * (size_t)kNoAllocMaxPixels);  //
 constexpr size_t kRng = align_up(sizeof(MrgState) * (size_t)kNoAllocMaxPixels);  // MRG32k3a words per slot / pixel
 constexpr size_t kU32 = align_up(4 * (size_t)kNoAllocMaxPixels);              // one 32-bit word per slot
 constexpr size_t kCtr = align_up(4 * 32);
-constexpr size_t kStats = align_up(8 * 8);
+constexpr size_t kStats = align_up(16 * 8);
 constexpr size_t kStatus = align_up(4);
 constexpr size_t kRec = align_up(sizeof(SceneRec));
 constexpr size_t kSlots = kSlotBytes * (size_t)kNoAllocMaxPixels;  // slot records
@@ -194,7 +194,7 @@ int render_noalloc(const gb_scene* scene, const gb_camera* cam, const gb_render_
     P.round_start[1] = (uint32_t)n;
     P.chunk_paths = (uint32_t)n;
     cudaError_t e = cudaMemcpyAsync(d_rec, &R, sizeof(R), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(F.stats, 0, 8 * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(F.stats, 0, 16 * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(F.status, 0, 4, st);
     if (e == cudaSuccess) e = k_launch_frame_init(F, true, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(F.cursor, F.pristine, sizeof(MrgState) * (size_t)n, cudaMemcpyDeviceToDevice, st);

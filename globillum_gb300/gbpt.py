@@ -125,7 +125,7 @@ class Stats(C.Structure):
                 ("closest_node_visits", C.c_uint64), ("closest_tri_tests", C.c_uint64),
                 ("shadow_node_visits", C.c_uint64), ("shadow_tri_tests", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("render_ms", C.c_double), ("stage_ms", C.c_double * 6),
-                ("stage_launches", C.c_uint64 * 6), ("paths_done", C.c_int)]
+                ("stage_launches", C.c_uint64 * 6), ("paths_done", C.c_int), ("light_samples", C.c_uint64)]
 
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("beta", "<f4"), ("gamma", "<f4"), ("ref", "<u4")])

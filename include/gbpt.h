@@ -435,6 +435,8 @@ typedef struct {
     double stage_ms[6];
     uint64_t stage_launches[6];
     int paths_done;
+    uint64_t light_samples;  /* closest hits, each with its light sample; only
+                              * counted by gb_render_instrumented          */
 } gb_stats;
 
 /* Knobs of the wavefront (chosen by the autotuner); 0 keeps a value:
