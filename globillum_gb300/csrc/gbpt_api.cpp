@@ -292,6 +292,7 @@ cudaError_t ensure_frame(gb_ctx* ctx, int n, int nslots, size_t samples, int nsc
         ctx->sample_cap = 0;
         if ((e = dalloc(ctx->sample_allocs, (void**)&F.samples, sizeof(float4) * samples)) != cudaSuccess) return e;
         if ((e = dalloc(ctx->sample_allocs, (void**)&F.jpool, sizeof(float4) * samples)) != cudaSuccess) return e;
+        if ((e = dalloc(ctx->sample_allocs, (void**)&F.spool, sizeof(MrgState) * samples)) != cudaSuccess) return e;
         ctx->sample_cap = samples;
     }
     return cudaSuccess;
@@ -753,10 +754,8 @@ long long round_pixels(const gb_ctx* ctx, int p) {
 long long sample_budget(const gb_ctx* ctx) { return std::max(1ll, ((long long)ctx->sample_mb << 20) / 16); }
 
 // End of the chunk that starts at round p0 (exclusive, <= end): rounds are
-// added while the chunk's paths fit the sample budget and 2^31, the chunk
-// has at most kMaxRounds rounds, and a round keeps at least half the pixels
-// of the first one (the slot pool of a chunk holds at most one path per
-// pixel of its smallest round).
+// added while the chunk's paths fit the sample budget and 2^31, and the
+// chunk has at most kMaxRounds rounds.
 int chunk_end(const gb_ctx* ctx, int p0, int end, long long* paths) {
     const long long budget = sample_budget(ctx);
     const long long n0 = round_pixels(ctx, p0);
@@ -764,7 +763,7 @@ int chunk_end(const gb_ctx* ctx, int p0, int end, long long* paths) {
     int p1 = p0 + 1;
     while (p1 < end && p1 - p0 < kMaxRounds) {
         long long np = round_pixels(ctx, p1);
-        if (tot + np > budget || tot + np >= (1ll << 31) || 2 * np < n0) break;
+        if (tot + np > budget || tot + np >= (1ll << 31)) break;
         tot += np;
         ++p1;
     }
@@ -821,7 +820,7 @@ int begin_frame(gb_ctx* ctx, std::vector<BatchScene>& items) {
                      [](const BatchScene& a, const BatchScene& b) { return a.desc.spp > b.desc.spp; });
     CK(cudaSetDevice(ctx->device));
     const long long samples = std::min(total_paths, std::max(ntot, sample_budget(ctx)));
-    const int nslots = (int)std::max(1ll, std::min<long long>(ntot, ctx->slots));
+    const int nslots = (int)std::max(1ll, std::min<long long>(total_paths, ctx->slots));
     CK(ensure_frame(ctx, (int)ntot, nslots, (size_t)samples, (int)items.size()));
     ctx->recs.assign(items.size(), SceneRec{});
     uint32_t base = 0;
@@ -933,7 +932,7 @@ std::vector<uint64_t> graph_key(const gb_ctx* ctx, const RenderParams& P, int ns
     k.push_back(((uint64_t)(uint32_t)F.nscenes << 32) | (uint32_t)nstart);
     k.push_back(((uint64_t)(uint32_t)max_iters << 32) | (ctx->instrument ? 1u : 0u));
     const void* ptrs[] = {F.scenes, F.slots, F.shadow, F.q[0], F.q[1], F.q[2], F.q[3], F.out,
-                          F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr,
+                          F.pristine, F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.spool, F.ctr, F.path_ctr,
                           F.iter, F.stats, F.status, F.tp0, F.adj, F.dimg, F.grad};
     for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
     k.push_back(((uint64_t)(uint32_t)F.grad_stride << 32) | (uint32_t)F.grad_replicas);
@@ -1096,17 +1095,17 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
         }
     }
 #endif
-    long long acc = 0, n_last = 0;
+    long long acc = 0;
     for (int r = 0; r < P.rounds; ++r) {
         P.round_start[r] = (uint32_t)acc;
-        n_last = round_pixels(ctx, p0 + r);
-        acc += n_last;
+        acc += round_pixels(ctx, p0 + r);
     }
     P.round_start[P.rounds] = (uint32_t)acc;
     P.chunk_paths = (uint32_t)acc;
-    // a launch starts at most nslots consecutive paths, at most one per pixel
+    // paths start in order on the free slots, several per pixel at once
+    // (each from its own jump of the pixel's stream)
     Frame& F = ctx->F;
-    F.nslots = (int)std::max(1ll, std::min({(long long)ctx->slot_cap, (long long)ctx->slots, n_last}));
+    F.nslots = (int)std::max(1ll, std::min({(long long)ctx->slot_cap, (long long)ctx->slots, acc}));
     const int nstart = (int)std::min<long long>(F.nslots, acc);
     // Every iteration moves each busy slot's path one bounce (at most L + 1
     // per path), and all slots stay busy until the chunk's last path has
@@ -1553,7 +1552,7 @@ std::vector<uint64_t> fit_key(const gb_ctx* ctx) {
     const Frame& F = ctx->F;
     std::vector<uint64_t> k;
     const void* ptrs[] = {ctx->d_scenes, F.slots, F.shadow, F.q[0], F.q[1], F.q[2], F.q[3], F.out, F.pristine,
-                          F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.ctr, F.path_ctr, F.iter, F.stats,
+                          F.cursor, F.jcursor, F.pscene, F.samples, F.jpool, F.spool, F.ctr, F.path_ctr, F.iter, F.stats,
                           F.status, F.adj, F.dimg, F.grad, ctx->d_gsum, ctx->d_rgb, ctx->fit.d_loss};
     for (const void* p : ptrs) k.push_back((uint64_t)(uintptr_t)p);
     k.push_back(((uint64_t)ctx->slot_cap << 32) ^ (uint64_t)ctx->sample_cap);

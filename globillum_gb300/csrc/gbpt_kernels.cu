@@ -584,24 +584,35 @@ __global__ void k_fill_pscene(Frame F) {
 //   camera jitter  = update p of the pixel's stream, read from the chunk's
 //                    jitter pool (k_jitter_pool walks each pixel's stream)
 //   lens sample    = update p of pixel (pixel+17)%n (raygen.cu:100-106)
-//   light/path     = updates pL, pL+1, ... one per bounce (hybrid-pt.h:229-233),
-//                    handed out by a per-pixel stream cursor that jumps by
-//                    L updates (3L generator steps, mrg_jump) whenever a path
-//                    of the pixel starts.
-// A launch starts paths from a contiguous range of at most nslots <= min_r
-// N_r paths, so it starts at most one path per pixel and never shares a
-// cursor; paths of a pixel start in sample order.
+//   light/path     = updates pL, pL+1, ... one per bounce (hybrid-pt.h:229-233):
+//                    k_jitter_pool walks the pixel's stream cursor over the
+//                    chunk's paths (a jump of L updates, 3L generator steps,
+//                    mrg_jump, per path) and leaves each path's start state
+//                    in the chunk's stream pool.
+// A path's stream therefore depends only on (pixel, p): a launch may start
+// several paths of one pixel, in any order, on any slots.
+// Per pixel at the start of a chunk, for every path p of the pixel in the
+// chunk (path l = round_start[p - p0] + pixel): its camera jitter (update p
+// of the pixel's jitter stream) and the state of its light/path stream
+// (L updates per path: one jump of 3 L generator steps from the previous
+// path's).  Paths then start from their own pool entries, in any order and
+// several per pixel at once.
 __global__ void k_jitter_pool(Frame F, RenderParams P) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= F.ntot) return;
-    const int spp = F.scenes[F.pscene[g]].spp;
+    const SceneRec& R = F.scenes[F.nscenes == 1 ? 0u : F.pscene[g]];
     MrgState s = ld_mrg(F.jcursor, (size_t)g);
-    const int pe = min(P.p0 + P.rounds, spp);
+    MrgState c = ld_mrg(F.cursor, (size_t)g);
+    const int pe = min(P.p0 + P.rounds, R.spp);
     for (int p = P.p0; p < pe; ++p) {
+        const uint32_t l = P.round_start[p - P.p0] + (uint32_t)g;
         v3 j = draw3(&s);
-        F.jpool[P.round_start[p - P.p0] + (uint32_t)g] = make_float4(j.x, j.y, j.z, 0.0f);
+        rec_st(&F.jpool[l], make_float4(j.x, j.y, j.z, 0.0f));
+        st_mrg(F.spool, l, c);
+        mrg_jump(c.s1, c.s2, R.jump1, R.jump2);  // = L draw3 calls
     }
     st_mrg(F.jcursor, (size_t)g, s);
+    st_mrg(F.cursor, (size_t)g, c);
 }
 
 // Ray differentials of a slot, 12 floats in 3 planes of nslots float4.
@@ -639,10 +650,7 @@ __device__ __forceinline__ void start_path(const Frame& F, const RenderParams& P
         lx = lj.z - 0.5f;
         ly = lj.y - 0.5f;
     }
-    MrgState bs = ld_mrg(F.cursor, gpix);
-    st_mrg(F.rng, slot, bs);
-    mrg_jump(bs.s1, bs.s2, R.jump1, R.jump2);  // = L draw3 calls
-    st_mrg(F.cursor, gpix, bs);
+    st_mrg(F.rng, slot, ld_mrg(F.spool, l));
     v3 o, d;
     camera_ray(R.cam, (int)(lp % (uint32_t)R.w), (int)(lp / (uint32_t)R.w), j.x, j.y, lx, ly, &o, &d);
     F.ray_o.st(slot, make_float4(o.x, o.y, o.z, FLT_MAX));

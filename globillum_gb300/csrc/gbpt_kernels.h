@@ -167,11 +167,12 @@ struct Frame {
     // per global pixel
     float4* out;       // output_color (moving average)
     MrgState* pristine;  // stream after curand_init(seed, pixel, 0)
-    MrgState* cursor;    // light/path stream at the pixel's next path
+    MrgState* cursor;    // light/path stream at the pixel's next chunk
     MrgState* jcursor;   // camera-jitter stream at the pixel's next path
     uint32_t* pscene;  // scene of each pixel
     float4* samples;   // sample of path l of the chunk (l = round_start[r] + pixel)
     float4* jpool;     // camera jitter of path l of the chunk
+    MrgState* spool;   // light/path stream state at the start of path l of the chunk
     // control
     uint32_t* ctr;     // 3 sets of 8 (by iteration % 3): count, ext head, shadow count, shadow head, ended
     uint32_t* path_ctr;  // next path of the chunk to start

@@ -60,10 +60,11 @@ constexpr size_t kSlots = kSlotBytes * (size_t)kNoAllocMaxPixels;  // slot recor
 constexpr size_t kShadow = GB_SHADOW_SPLIT ? 32 * (size_t)kNoAllocMaxPixels : 0;  // shadow rays
 // One slot per pixel and one path sample per pass: the slot records and
 // 4 queues; per pixel the image, the
-// initial RNG states, the two stream cursors, the scene word, one sample and
+// initial RNG states, the two stream cursors, the scene word, one sample,
+// one stream state and
 // one jitter value; counters, path counter, iteration, stats, status and the
 // scene record.
-constexpr size_t kScratchBytes = kSlots + kShadow + 4 * kU32 + kV4 + 3 * kRng + kU32 + 2 * kV4 + kCtr +
+constexpr size_t kScratchBytes = kSlots + kShadow + 4 * kU32 + kV4 + 4 * kRng + kU32 + 2 * kV4 + kCtr +
                                  kCtr + kCtr + kStats + kStatus + kRec;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -95,6 +96,7 @@ Frame carve(unsigned char* base, int n, SceneRec** rec) {
     F.out = (float4*)(base + off); off += kV4;
     F.pristine = (MrgState*)(base + off); off += kRng;
     F.cursor = (MrgState*)(base + off); off += kRng;
+    F.spool = (MrgState*)(base + off); off += kRng;
     F.jcursor = (MrgState*)(base + off); off += kRng;
     F.pscene = (uint32_t*)(base + off); off += kU32;
     F.samples = (float4*)(base + off); off += kV4;
