@@ -506,10 +506,17 @@ __device__ __forceinline__ void st_mrg(MrgState* base, size_t i, const MrgState&
 // the same for the stream of a slot record, stored as its whole 32-byte
 // sector (the state and 8 zero bytes)
 __device__ __forceinline__ MrgState ld_mrg(const SlotField<MrgState>& f, size_t slot) { return ld_mrg(&f[slot], 0); }
-__device__ __forceinline__ void st_mrg(const SlotField<MrgState>& f, size_t slot, const MrgState& m) {
+__device__ __forceinline__ void st_mrg(const SlotField<MrgState>& f, size_t slot, const MrgState& m,
+                                       bool hit_line = false) {
     uint4* q = reinterpret_cast<uint4*>(&f[slot]);
-    rec_st(q, make_uint4(m.s1[0], m.s1[1], m.s1[2], m.s2[0]));
-    rec_st(q + 1, make_uint4(m.s2[1], m.s2[2], 0u, 0u));
+    const uint4 a = make_uint4(m.s1[0], m.s1[1], m.s1[2], m.s2[0]), b = make_uint4(m.s2[1], m.s2[2], 0u, 0u);
+    if (GB_HIT_LINE_KEEP && hit_line) {
+        q[0] = a;
+        q[1] = b;
+    } else {
+        rec_st(q, a);
+        rec_st(q + 1, b);
+    }
 }
 __device__ __forceinline__ v3 draw3(MrgState* m) {
     curandStateMRG32k3a st = mrg_expand(*m);
@@ -1004,7 +1011,7 @@ __device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, ui
     const DevScene& S = R.S;
     MrgState st = ld_mrg(F.rng, slot);
     v3 rnd = draw3(&st);
-    st_mrg(F.rng, slot, st);
+    st_mrg(F.rng, slot, st, true);
     v3 lr = rnd;
     if (R.rng_mode == 1) {
         int pid = (int)(F.pix.ld(slot) - R.pixel_base) + 1;
@@ -1024,10 +1031,10 @@ __device__ __forceinline__ void nee_at_hit(const Frame& F, const SceneRec& R, ui
                               &so, &sd, &smax, &psc, &scale);
     }
     if (skip_dark && psc.x == 0.0f && psc.y == 0.0f && psc.z == 0.0f) smax = -1.0f;
-    F.sh_o.st(slot, make_float4(so.x, so.y, so.z, smax));
-    F.sh_d.st(slot, make_float4(sd.x, sd.y, sd.z, 0.0f));
-    F.psc.st(slot, make_float4(psc.x, psc.y, psc.z, scale));
-    F.rnd.st(slot, make_float4(rnd.x, rnd.y, rnd.z, 0.0f));
+    F.sh_o.st_hit(slot, make_float4(so.x, so.y, so.z, smax));
+    F.sh_d.st_hit(slot, make_float4(sd.x, sd.y, sd.z, 0.0f));
+    F.psc.st_hit(slot, make_float4(psc.x, psc.y, psc.z, scale));
+    F.rnd.st_hit(slot, make_float4(rnd.x, rnd.y, rnd.z, 0.0f));
 }
 
 // STACK: traversal stack entries; BT: threads per block (the register
@@ -1079,8 +1086,8 @@ __global__ void __launch_bounds__(BT, GB_TRAV_MIN_BLOCKS * 128 / BT) k_extend(Fr
                 v3 Pp = bary(h.bb, h.bg, ld3(a), ld3(b), ld3(c));
                 v3 Nr = bary(h.bb, h.bg, ld3(na), ld3(nb), ld3(nc));
                 if (!GB_SPLIT_NEE) nee_at_hit(F, R, slot, Pp, Nr, P.mode != MODE_ADJOINT);
-                F.hit_p.st(slot, make_float4(Pp.x, Pp.y, Pp.z, a.w));
-                F.hit_n.st(slot, make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id)));
+                F.hit_p.st_hit(slot, make_float4(Pp.x, Pp.y, Pp.z, a.w));
+                F.hit_n.st_hit(slot, make_float4(Nr.x, Nr.y, Nr.z, __uint_as_float(h.best_id)));
             }
         }
         push(fin && hit, slot, qsh, cs + 2);

@@ -100,6 +100,9 @@ static_assert(kSlotRdiff + 48 <= 128 && kSlotRng + 24 <= kSlotBytes, "slot recor
 #ifndef GB_REC_EVICT_FIRST
 #define GB_REC_EVICT_FIRST 1
 #endif
+#ifndef GB_HIT_LINE_KEEP
+#define GB_HIT_LINE_KEEP 0
+#endif
 #ifdef __CUDACC__
 template <class T>
 __device__ __forceinline__ T rec_ld(const T* p) {
@@ -134,6 +137,16 @@ struct SlotField {
     __device__ inline T ld(size_t slot) const { return rec_ld(reinterpret_cast<const T*>(base + slot * Stride)); }
     __device__ inline void st(size_t slot, const T& v) const {
         rec_st(reinterpret_cast<T*>(base + slot * Stride), v);
+    }
+    // the hit line the closest-hit kernel writes and the any-hit and
+    // shading kernels of the same iteration read back (GB_HIT_LINE_KEEP:
+    // with normal L2 priority instead of evict-first)
+    __device__ inline void st_hit(size_t slot, const T& v) const {
+#if GB_HIT_LINE_KEEP
+        *reinterpret_cast<T*>(base + slot * Stride) = v;
+#else
+        rec_st(reinterpret_cast<T*>(base + slot * Stride), v);
+#endif
     }
 #endif
 };

@@ -557,7 +557,7 @@ int gb_render_instrumented(gb_ctx* ctx, gb_scene* scene, const gb_camera* cam,
  * The scene is created beforehand (gb_scene_create allocates); this call
  * renders the same frame as gb_render into the caller's device buffer
  * `out_rgb` (w*h*3 floats) on `stream` (NULL = legacy default stream), with
- * its wavefront state in one fixed file-scope device array (about 25 MB,
+ * its wavefront state in one fixed file-scope device array (about 27 MB,
  * held by every GPU that loads the library until exit) instead of cudaMalloc.
  * Limits: w*h <= 65536 pixels and max_bounces <= 64, else GB_ERR_INVALID;
  * scenes with texture coordinates return GB_ERR_UNSUPPORTED (use gb_render).
