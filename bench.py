@@ -32,7 +32,7 @@ sys.path.insert(0, str(ROOT))
 # DRAM bytes (read + write) k_extend moves per closest-hit ray on the 1M-triangle
 # workload, from an ncu capture of a whole 4-spp frame with a warm L2
 # (profiles/k_extend_dram_traffic_icospheres1m_4spp.txt).
-K_EXTEND_DRAM_BYTES_PER_RAY = 703.1
+K_EXTEND_DRAM_BYTES_PER_RAY = 642.6
 METRIC = "Mpaths/s"
 
 
