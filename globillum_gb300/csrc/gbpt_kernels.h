@@ -181,7 +181,7 @@ struct Frame {
     float4* out;       // output_color (moving average)
     MrgState* pristine;  // stream after curand_init(seed, pixel, 0)
     MrgState* cursor;    // light/path stream at the pixel's next chunk
-    MrgState* jcursor;   // camera-jitter stream at the pixel's next path
+    MrgState* jcursor;   // camera-jitter stream at the pixel's next chunk
     uint32_t* pscene;  // scene of each pixel
     float4* samples;   // sample of path l of the chunk (l = round_start[r] + pixel)
     float4* jpool;     // camera jitter of path l of the chunk

@@ -217,18 +217,23 @@ def test_backward_matches_plain_frame_differences(gpu_ctx):
 
 
 def test_backward_batch_equals_single(gpu_ctx):
-    a, b = _scene(seed=3, w=40, h=24, spp=3), _scene(seed=5, w=24, h=24, spp=5, bounces=3)
-    sa, sb = gpu_ctx.scene(a), gpu_ctx.scene(b)
+    """Three scenes of different sizes, spp, bounces and materials (principled
+    and Lambert): the batched adjoint, host-driven and as one CUDA graph,
+    gives each scene's single gb_backward gradient."""
+    c = scenes.cornell(width=32, height=20, spp=2, max_bounces=4)
+    c.render["rng_mode"] = gbpt.GB_RNG_MRG32K3A_POOL
+    scs = [_scene(seed=3, w=40, h=24, spp=3), _scene(seed=5, w=24, h=24, spp=5, bounces=3), c]
+    hs = [gpu_ctx.scene(sc) for sc in scs]
     rng = np.random.default_rng(4)
-    ga = rng.normal(size=(24, 40, 3)).astype(np.float32)
-    gb = rng.normal(size=(24, 24, 3)).astype(np.float32)
-    single = [sa.backward(a.camera, a.render, ga), sb.backward(b.camera, b.render, gb)]
+    gs = [rng.normal(size=(sc.render["height"], sc.render["width"], 3)).astype(np.float32) for sc in scs]
+    single = [h.backward(sc.camera, sc.render, g) for h, sc, g in zip(hs, scs, gs)]
+    jobs = [(h, sc.camera, sc.render) for h, sc in zip(hs, scs)]
     for graph in (False, True):
-        batch = gpu_ctx.backward_batch([(sa, a.camera, a.render), (sb, b.camera, b.render)], [ga, gb], graph=graph)
+        batch = gpu_ctx.backward_batch(jobs, gs, graph=graph)
         for x, y in zip(single, batch):
             assert np.allclose(x, y, rtol=1e-4, atol=1e-6 * np.abs(x).max())
-    sa.close()
-    sb.close()
+    for h in hs:
+        h.close()
 
 
 def test_backward_rejects_long_paths(gpu_ctx):
