@@ -1086,7 +1086,13 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
         cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
         cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev);
         const size_t bytes = std::min({(size_t)80 * (size_t)S.n_nodes, (size_t)max_persist, (size_t)max_window});
-        if (bytes > ctx->l2_persist && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes) == cudaSuccess)
+        // the set-aside is a device limit: raised only outside a stream capture
+        // (a fitting step is captured whole), the window is used once it is there
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone, cap_aux = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(ctx->stream, &cap);
+        if (ctx->aux) cudaStreamIsCapturing(ctx->aux, &cap_aux);
+        if (bytes > ctx->l2_persist && cap == cudaStreamCaptureStatusNone && cap_aux == cudaStreamCaptureStatusNone &&
+            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes) == cudaSuccess)
             ctx->l2_persist = bytes;
         cudaGetLastError();
         if (bytes > 0 && ctx->l2_persist >= bytes) {

@@ -345,3 +345,35 @@ def test_fit_step_is_one_graph_and_matches_the_separate_calls(gpu_ctx):
             x[5 * len(sc.materials):] = x_init[5 * len(sc.materials):]
     for h in hs:
         h.close()
+
+
+def test_fit_step_of_one_scene_on_a_fresh_context():
+    """A fitting step of a single scene on a new context: the frame of one
+    scene gives the traversal launches its persisting L2 window, whose
+    set-aside the context has not asked for yet when the step is captured.
+    The step must still equal gb_render + gb_backward of 2 (image - target)."""
+    import torch
+    ctx = gbpt.Context(0)
+    try:
+        sc = _scene(seed=17, w=40, h=32, spp=2, bounces=3)
+        h = ctx.scene(sc)
+        x0 = h.get_params()
+        xt = x0.copy()
+        nm = 5 * len(sc.materials)
+        xt[:nm] = np.clip(xt[:nm] * 0.8 + 0.1, 0.0, 1.0).astype(np.float32)
+        h.set_params(xt)
+        target = torch.from_numpy(h.render(sc.camera, sc.render)).cuda()
+        h.set_params(x0)
+        image = torch.empty_like(target)
+        ctx.fit_prepare([(h, sc.camera, sc.render)], [target.data_ptr()], [image.data_ptr()])
+        for _ in range(2):
+            grads, loss = ctx.fit_step([x0])
+            ref = h.render(sc.camera, sc.render)
+            assert np.array_equal(image.cpu().numpy(), ref)
+            tn = target.cpu().numpy()
+            assert np.isclose(loss[0], float(((ref.astype(np.float64) - tn) ** 2).sum()), rtol=1e-6, atol=0.0)
+            gref = h.backward(sc.camera, sc.render, (2.0 * (ref - tn)).astype(np.float32))
+            assert np.allclose(grads[0], gref, rtol=1e-4, atol=1e-6 * np.abs(gref).max())
+        h.close()
+    finally:
+        ctx.close()
