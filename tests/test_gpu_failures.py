@@ -100,3 +100,42 @@ def test_injected_allocation_failures():
     finally:
         gbpt.load_library().gb_set_fault_injection(-1)
         ctx.close()
+
+
+def test_bad_fitting_and_tuning_requests_are_rejected():
+    """gb_ctx_set_gradient_terms, gb_ctx_set_tuning (stack depth, block
+    shape), gb_fit_prepare and gb_fit_step refuse bad arguments with
+    GB_ERR_INVALID and a message, and the context keeps working."""
+    import torch
+    ctx = gbpt.Context(0)
+    lib = ctx.lib
+    try:
+        _expect(ctx, lib.gb_ctx_set_gradient_terms(ctx.h, 2), gbpt.GB_ERR_INVALID, "sampling")
+        for field, val in (("stack_depth", 16), ("block_threads", 96)):
+            t = gbpt.Tuning()
+            setattr(t, field, val)
+            _expect(ctx, lib.gb_ctx_set_tuning(ctx.h, C.byref(t)), gbpt.GB_ERR_INVALID, field)
+        # a step before any gb_fit_prepare
+        p = (C.c_void_p * 1)()
+        g = (C.c_void_p * 1)()
+        _expect(ctx, lib.gb_fit_step(ctx.h, p, g, None), gbpt.GB_ERR_INVALID, "no fitting step prepared")
+        sc = scenes.cornell(width=16, height=16, spp=1, max_bounces=2)
+        sc.render["rng_mode"] = gbpt.GB_RNG_MRG32K3A_POOL
+        h = ctx.scene(sc)
+        target = torch.zeros((16, 16, 3), device="cuda")
+        _expect(ctx, lib.gb_fit_prepare(ctx.h, 0, None), gbpt.GB_ERR_INVALID, "1..1024")
+        with pytest.raises(gbpt.GBError):
+            ctx.fit_prepare([(h, sc.camera, sc.render)] * 2, [target.data_ptr()] * 2)
+        assert "twice" in lib.gb_last_error(ctx.h).decode()
+        ctx.fit_prepare([(h, sc.camera, sc.render)], [target.data_ptr()])
+        x = h.get_params()
+        bad = x.copy()
+        bad[0] = np.nan
+        with pytest.raises(gbpt.GBError):
+            ctx.fit_step([bad])
+        assert "non-finite" in lib.gb_last_error(ctx.h).decode()
+        grads, loss = ctx.fit_step([x])
+        assert np.isfinite(grads[0]).all() and np.isfinite(loss).all()
+        h.close()
+    finally:
+        ctx.close()
