@@ -263,6 +263,10 @@ def c0_leg(ctx, args, torch, flush, with_cpu: bool):
     scene = ctx.scene(sc)
     out = torch.empty((H, W, 3), device="cuda", dtype=torch.float32)
     stream = torch.cuda.current_stream()
+    # the library's autotuner on this frame (whole frames, 3 repeats); the
+    # context's tuning is restored afterwards
+    saved = ctx.get_tuning()
+    tuning, _ = ctx.autotune([(scene, sc.camera, r)], proxy_spp=0, repeats=3)
     for _ in range(max(1, args.warmup)):
         scene.render_device(sc.camera, r, out.data_ptr())
     ts = []
@@ -275,21 +279,25 @@ def c0_leg(ctx, args, torch, flush, with_cpu: bool):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     img = out.cpu().numpy()
+    ctx.set_tuning(**saved)
     ms = float(np.median(ts))
     res = {"workload": {"scene": sc.name, "triangles": sc.num_triangles, "width": W, "height": H, "spp": spp,
                         "max_bounces": r["max_bounces"], "light_samples": "Halton"},
-           "value": W * H * spp / ms / 1e3, "unit": METRIC, "ms_per_frame": ms,
+           "value": W * H * spp / ms / 1e3, "unit": METRIC, "ms_per_frame": ms, "tuning": tuning,
            "rmse": fp64_rmse(img, "c0", spp)}
     if with_cpu:
         from oracle import oracle
         orc = oracle.OracleScene(sc, use_bvh=True)
         pool = ctx.mrg_pool(W * H, spp * r["max_bounces"], seed=r["seed"])
         for serial, name in ((False, "cpu_openmp_fixed"), (True, "cpu_reference_as_is")):
-            t0 = time.perf_counter()
-            cimg = orc.render(sc.camera, r, pool, serial_nee=serial)
-            dt = time.perf_counter() - t0
-            res[name] = {"value": W * H * spp / dt / 1e6, "unit": METRIC, "seconds": dt, "cores": oracle.threads(),
-                         "image_equals_gpu": bool(np.array_equal(cimg, img))}
+            dt, frames = 0.0, 0
+            while dt < 2.0 and frames < 32:  # whole frames, at least 2 s of CPU time
+                t0 = time.perf_counter()
+                cimg = orc.render(sc.camera, r, pool, serial_nee=serial)
+                dt += time.perf_counter() - t0
+                frames += 1
+            res[name] = {"value": W * H * spp * frames / dt / 1e6, "unit": METRIC, "seconds": dt, "frames": frames,
+                         "cores": oracle.threads(), "image_equals_gpu": bool(np.array_equal(cimg, img))}
         res["rmse"]["cpu_frame"] = fp64_rmse(cimg, "c0", spp)["value"]
         orc.close()
     scene.close()
@@ -316,6 +324,7 @@ def batch_leg(ctx, args, torch, flush, dist):
     outs = [torch.empty((sc.render["height"], sc.render["width"], 3), device="cuda", dtype=torch.float32)
             for sc in mixed]
     ptrs = [o.data_ptr() for o in outs]
+    saved = ctx.get_tuning()
     t0 = time.perf_counter()
     tuning, tune_ms = ctx.autotune(jobs, proxy_spp=4, repeats=3)
     tune_s = time.perf_counter() - t0
@@ -379,6 +388,7 @@ def batch_leg(ctx, args, torch, flush, dist):
     vb, vp = replicas.mpaths_per_s(tot_b, ms_b), replicas.mpaths_per_s(tot_p, ms_p)
     for h in handles:
         h.close()
+    ctx.set_tuning(**saved)
     tris = [sc.num_triangles for sc in mixed]
     return {"value": vb, "unit": METRIC, "plain_value": vp, "batched_over_plain": vb / vp,
             "ms_per_step": ms_b / args.steps, "plain_ms_per_step": ms_p / args.steps,
@@ -476,6 +486,7 @@ def adjoint_leg(ctx, scene, sc, args, torch, flush, orc):
     out = {"workload": {"scene": sc.name, "width": W, "height": H, "spp": rd["spp"], "max_bounces": rd["max_bounces"],
                         "params": int(x0.size), "loss": "L2 to a target from materials seeded 97"},
            "forward_ms": fwd_ms, "backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms, "loss": loss0,
+           "tuning": ctx.get_tuning(),
            "rmse_forward_frame": rmse_fwd,
            "adjoint_record_bytes": int(80 * rd["max_bounces"] * min(W * H, 1 << 20)),
            "finite_differences": {"h": h, "params": int(sel.size), "median_rel_err": float(np.median(rel_fd)),
@@ -499,7 +510,8 @@ def inverse_leg(ctx, args, torch, dist):
     scene's 64 materials (base colour, roughness, metallic) are recovered
     from a target rendered with hidden seeded parameters: Adam (lr 1e-2) on
     the summed L2 image losses, starting from the scenes' own seeded
-    materials.  One iteration = one gb_fit_step: a single CUDA graph launch
+    materials, with the knobs gb_autotune picks for this batch.  One
+    iteration = one gb_fit_step: a single CUDA graph launch
     that uploads the parameters, renders the batched forward frame, forms
     the losses and image gradients on the device and runs the batched
     adjoint; the host applies the parameter Jacobian and Adam.  The same
@@ -544,6 +556,9 @@ def inverse_leg(ctx, args, torch, dist):
             e[name] = float(np.sqrt(np.mean(np.concatenate(sq)))) if sq else None
         return e
 
+    # knobs for this batch from the library's autotuner (restored at the end)
+    saved = ctx.get_tuning()
+    tuning, _ = ctx.autotune(jobs, proxy_spp=0, repeats=3)
     # one fitting step = one CUDA graph launch: parameter upload, batched
     # forward frame, L2 loss and image gradient on the device, batched
     # adjoint, gradient reduction (gb_fit_step)
@@ -607,12 +622,13 @@ def inverse_leg(ctx, args, torch, dist):
         seq.append(time.perf_counter() - t0)
     for h, x0 in zip(handles, x_init):
         h.close()
+    ctx.set_tuning(**saved)
     it_s = float(np.median(t_iter))
     seq_s = float(np.median(seq))
     return {"workload": {"scenes": n_sc, "triangles": [int(sc.num_triangles) for sc in mixed], "resolution": 256,
                          "spp": 8, "max_bounces": 4, "materials_per_scene": 64, "iterations": args.inverse_iters,
                          "optimizer": "Adam lr 1e-2 on base colour, roughness, metallic"},
-            "param_rmse_initial": err0, "fits": fits,
+            "param_rmse_initial": err0, "fits": fits, "tuning": tuning,
             "iteration_ms": it_s * 1e3, "sequential_iteration_ms": seq_s * 1e3,
             "batched_over_sequential": seq_s / it_s,
             "mpaths_per_s_fwd_plus_bwd": 2 * paths / it_s / 1e6,
