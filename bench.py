@@ -488,7 +488,7 @@ def adjoint_leg(ctx, scene, sc, args, torch, flush, orc):
            "forward_ms": fwd_ms, "backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms, "loss": loss0,
            "tuning": ctx.get_tuning(),
            "rmse_forward_frame": rmse_fwd,
-           "adjoint_record_bytes": int(80 * rd["max_bounces"] * min(W * H, 1 << 20)),
+           "adjoint_record_bytes": int(80 * rd["max_bounces"] * min(W * H * rd["spp"], 1 << 22)),
            "finite_differences": {"h": h, "params": int(sel.size), "median_rel_err": float(np.median(rel_fd)),
                                   "max_rel_err": float(rel_fd.max()),
                                   "within_1e-3": int((rel_fd <= 1e-3).sum()), "outliers": outliers,

@@ -116,7 +116,7 @@ struct gb_ctx {
     int sampling_terms = 0;             // adjoint: add the derivatives of the sampling decisions
     size_t l2_persist = 0;              // persisting L2 set-aside this context asked for (GB_NODE_L2_PERSIST)
     int block_threads = 128;            // threads per traversal block (64 or 128)
-    int slots = 1 << 20;                // path slots in flight (upper bound)
+    int slots = 1 << 24;                // path slots in flight (upper bound)
     int sample_mb = 1024;               // sample buffer budget (chunk size)
     // queue-count snapshots: pinned ring + events (host stays a few iterations ahead)
     uint32_t* snap_host = nullptr;
@@ -1112,6 +1112,8 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
     // (each from its own jump of the pixel's stream)
     Frame& F = ctx->F;
     F.nslots = (int)std::max(1ll, std::min({(long long)ctx->slot_cap, (long long)ctx->slots, acc}));
+    // the adjoint's vertex records take 80 B x bounces per slot
+    if (ctx->mode == MODE_ADJOINT) F.nslots = std::min(F.nslots, kAdjMaxSlots);
     const int nstart = (int)std::min<long long>(F.nslots, acc);
     // Every iteration moves each busy slot's path one bounce (at most L + 1
     // per path), and all slots stay busy until the chunk's last path has
@@ -1483,7 +1485,8 @@ int gb_backward_batch(gb_ctx* ctx, int n, const gb_adjoint_item* items, int dimg
     const int replicas = k_adjoint_grid();
     const int stride = (int)std::max<uint32_t>(1, gtot);
     cudaError_t e = ensure_buf(ctx, (void**)&F.adj, &ctx->adj_cap,
-                               sizeof(float4) * kAdjPlanes * (size_t)ctx->max_L * ctx->slot_cap);
+                               sizeof(float4) * kAdjPlanes * (size_t)ctx->max_L *
+                                   std::min(ctx->slot_cap, (size_t)kAdjMaxSlots));
     if (e == cudaSuccess) e = ensure_buf(ctx, (void**)&F.dimg, &ctx->dimg_cap, sizeof(float4) * (size_t)F.ntot);
     if (e == cudaSuccess)
         e = ensure_buf(ctx, (void**)&F.grad, &ctx->grad_cap, sizeof(float) * (size_t)replicas * (size_t)stride);
@@ -1613,7 +1616,8 @@ int fit_build(gb_ctx* ctx) {
     f.stride = (int)std::max<uint32_t>(1, gtot);
     const size_t ns = f.items.size();
     cudaError_t e = ensure_buf(ctx, (void**)&F.adj, &ctx->adj_cap,
-                               sizeof(float4) * kAdjPlanes * (size_t)ctx->max_L * ctx->slot_cap);
+                               sizeof(float4) * kAdjPlanes * (size_t)ctx->max_L *
+                                   std::min(ctx->slot_cap, (size_t)kAdjMaxSlots));
     if (e == cudaSuccess) e = ensure_buf(ctx, (void**)&F.dimg, &ctx->dimg_cap, sizeof(float4) * (size_t)F.ntot);
     if (e == cudaSuccess)
         e = ensure_buf(ctx, (void**)&F.grad, &ctx->grad_cap, sizeof(float) * (size_t)f.replicas * (size_t)f.stride);
@@ -1855,7 +1859,7 @@ int gb_autotune(gb_ctx* ctx, int n, const gb_batch_item* items, int proxy_spp, i
     };
     const Knob knobs[] = {
         {&gb_tuning::graph, {1, 2}},
-        {&gb_tuning::slots, {1 << 18, 1 << 19, 1 << 20, 1 << 21}},
+        {&gb_tuning::slots, {1 << 20, 1 << 22, 1 << 23, 1 << 24, 1 << 25}},
         {&gb_tuning::refill, {8, 16, 24, 32}},
         {&gb_tuning::tri_mode, {1, 2, 3, 4}},
         {&gb_tuning::blocks_per_sm, {1, 3, 4, 5, 6}},

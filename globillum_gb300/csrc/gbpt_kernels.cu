@@ -1871,10 +1871,14 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
     return cudaGetLastError();
 }
 
-// Grid of the streaming per-path kernels: persistent (the default), or one
-// thread per slot (GB_WIDE_STREAM_GRIDS).
+// Grid of the streaming per-path kernels (k_shade, k_regen): persistent for
+// pools of up to 2^20 slots, one thread per slot above that (or always,
+// with GB_WIDE_STREAM_GRIDS).  On the 1M-triangle frame with 2^21 slots the
+// wide grid shades in 7.0 ms against 8.0 (931 against 914 Mpaths/s); on the
+// 256x256 16-spp Cornell frame (2^20 slots) the persistent grid in 0.39 ms
+// against 0.47.
 inline int stream_grid(int persistent, int nslots) {
-    return GB_WIDE_STREAM_GRIDS ? std::max(1, blocks_for(nslots)) : persistent;
+    return (GB_WIDE_STREAM_GRIDS || nslots > (1 << 20)) ? std::max(1, blocks_for(nslots)) : persistent;
 }
 
 template <int MODE, bool TEX>

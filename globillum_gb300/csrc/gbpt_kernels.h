@@ -60,6 +60,7 @@ struct SceneRec {
 enum { MODE_FORWARD = 0, MODE_FROZEN = 1, MODE_ADJOINT = 2 };
 constexpr int kAdjPlanes = 5;        // float4 planes of one adjoint vertex record
 constexpr int kMaxAdjBounces = 16;   // bounces the adjoint records per path
+constexpr int kAdjMaxSlots = 1 << 22;  // slots of an adjoint chunk (vertex records: 80 B x bounces each)
 
 constexpr int kMaxRounds = 64;  // path samples per chunk
 
