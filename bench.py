@@ -30,9 +30,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 # DRAM bytes (read + write) k_extend moves per closest-hit ray on the 1M-triangle
-# workload, from an ncu capture of a whole 4-spp frame with a warm L2
-# (profiles/k_extend_dram_traffic_icospheres1m_4spp.txt).
-K_EXTEND_DRAM_BYTES_PER_RAY = 642.6
+# workload with the default slot pool, from an ncu capture of a whole 16-spp
+# frame with a warm L2 (profiles/k_extend_dram_traffic_icospheres1m_16spp.txt).
+K_EXTEND_DRAM_BYTES_PER_RAY = 1243.4
 METRIC = "Mpaths/s"
 
 
@@ -768,7 +768,7 @@ def run_gbpt(args, rank, world):
                          "traffic": (K_EXTEND_DRAM_BYTES_PER_RAY * ext_rays / max(1.0, ext_launches)
                                      if args.workload == "icospheres-1m" else None),
                          "traffic_source": "ncu dram__bytes_read+write of k_extend per closest-hit ray "
-                                           "(warm L2, whole 4-spp frame of this workload) x rays per launch",
+                                           "(warm L2, whole 16-spp frame of this workload) x rays per launch",
                          "algorithmic_bytes_per_launch": closest_bytes / max(1.0, ext_launches),
                          "bytes_model": "per ray: node visits*80 + tri tests*36 + 32 ray in + 16 hit out; per hit "
                                         "(light sample): 72 hit triangle positions+normals + 64 light + 12 draw + "

@@ -149,6 +149,7 @@ struct gb_scene {
     GpuBvh gbvh;
     std::vector<int> material_index;
     void* shade_buf = nullptr;
+    size_t tree_bytes = 0;  // host-built tree: nodes then triangles in one allocation at S.nodes
     std::vector<int> mat_dtex;  // diffuse texture of each material (-1 = none)
 };
 
@@ -158,6 +159,9 @@ struct gb_scene {
 // window
 #ifndef GB_NODE_L2_PERSIST
 #define GB_NODE_L2_PERSIST 1
+#endif
+#ifndef GB_TREE_WINDOW
+#define GB_TREE_WINDOW 0
 #endif
 
 namespace {
@@ -591,8 +595,10 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
         bt = 0;
         sc->material_index.assign(d->material_index, d->material_index + n);
     }
-    if ((builder == GB_BVH_HOST_SAH &&
-         ((e = dalloc(sc->allocs, &pn, bn)) != cudaSuccess || (e = dalloc(sc->allocs, &pt, bt)) != cudaSuccess)) ||
+    // a host-built tree is one allocation (nodes, then triangles at a
+    // 256-byte boundary), so that one L2 access-policy window can cover it
+    const size_t bn_al = (bn + 255) & ~(size_t)255;
+    if ((builder == GB_BVH_HOST_SAH && (e = dalloc(sc->allocs, &pn, bn_al + bt)) != cudaSuccess) ||
         (e = dalloc(sc->allocs, &ps, bs)) != cudaSuccess || (e = dalloc(sc->allocs, &pm, bm)) != cudaSuccess ||
         (e = dalloc(sc->allocs, &pl, bl)) != cudaSuccess) {
         free_all(sc->allocs);
@@ -600,6 +606,10 @@ int gb_scene_create_ex(gb_ctx* ctx, const gb_scene_desc* d, const gb_build_optio
         return cuda_fail(ctx, e, "scene allocation");
     }
     sc->shade_buf = ps;
+    if (builder == GB_BVH_HOST_SAH) {
+        pt = (unsigned char*)pn + bn_al;
+        sc->tree_bytes = bn_al + bt;
+    }
     e = cudaSuccess;
     if (builder == GB_BVH_HOST_SAH) {
         e = cudaMemcpy(pn, bvh.nodes.data(), bn, cudaMemcpyHostToDevice);
@@ -1085,7 +1095,11 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
         cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev);
-        const size_t bytes = std::min({(size_t)80 * (size_t)S.n_nodes, (size_t)max_persist, (size_t)max_window});
+        // the window: the node array, or the whole host-built tree (GB_TREE_WINDOW)
+        const size_t tree = ctx->items[0].scene->tree_bytes;
+        const size_t want = (GB_TREE_WINDOW && tree) ? tree : (size_t)80 * (size_t)S.n_nodes;
+        const size_t window = std::min(want, (size_t)max_window);
+        const size_t bytes = std::min(window, (size_t)max_persist);
         // the set-aside is a device limit: raised only outside a stream capture
         // (a fitting step is captured whole), the window is used once it is there
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone, cap_aux = cudaStreamCaptureStatusNone;
@@ -1097,7 +1111,8 @@ void make_chunk(gb_ctx* ctx, int p0, int p1, RenderParams* out, int* nstart_out,
         cudaGetLastError();
         if (bytes > 0 && ctx->l2_persist >= bytes) {
             P.l2_nodes = S.nodes;
-            P.l2_nodes_bytes = bytes;
+            P.l2_nodes_bytes = window;
+            P.l2_hit_ratio = (float)((double)bytes / (double)window);
         }
     }
 #endif

@@ -1796,7 +1796,7 @@ void launch_traversal(K kernel, dim3 grid, int block, const Frame& F, const Rend
     at[0].id = cudaLaunchAttributeAccessPolicyWindow;
     at[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(P.l2_nodes);
     at[0].val.accessPolicyWindow.num_bytes = (size_t)P.l2_nodes_bytes;
-    at[0].val.accessPolicyWindow.hitRatio = 1.0f;
+    at[0].val.accessPolicyWindow.hitRatio = P.l2_hit_ratio;
     at[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
     at[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     cudaLaunchConfig_t cfg{};

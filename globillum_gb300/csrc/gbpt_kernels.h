@@ -245,6 +245,7 @@ struct RenderParams {
     // scene): the scene's node array, accessed as persisting
     const void* l2_nodes;
     unsigned long long l2_nodes_bytes;
+    float l2_hit_ratio;  // fraction of the window's accesses that persist
     uint32_t chunk_paths;  // paths of the chunk
     uint32_t round_start[kMaxRounds + 1];  // first path index of each round (prefix sums of N_p)
 };
