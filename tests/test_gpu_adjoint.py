@@ -377,3 +377,23 @@ def test_fit_step_of_one_scene_on_a_fresh_context():
         h.close()
     finally:
         ctx.close()
+
+
+def test_backward_with_a_small_slot_pool(gpu_ctx):
+    """Fewer slots than paths (the adjoint's chunks are capped to bound its
+    vertex records): the paths replay in several waves of the pool and the
+    gradient equals the one of a pool holding every path (sums in another
+    order: relative 1e-4)."""
+    sc = _scene(seed=21)
+    rd = sc.render
+    s = gpu_ctx.scene(sc)
+    g = np.random.default_rng(8).normal(size=(rd["height"], rd["width"], 3)).astype(np.float32)
+    full = s.backward(sc.camera, rd, g)
+    old = gpu_ctx.get_tuning()
+    try:
+        gpu_ctx.set_tuning(slots=1000)
+        small = s.backward(sc.camera, rd, g)
+    finally:
+        gpu_ctx.set_tuning(slots=old["slots"])
+    assert np.allclose(small, full, rtol=1e-4, atol=1e-6 * np.abs(full).max())
+    s.close()
