@@ -109,7 +109,7 @@ struct gb_ctx {
     gb_stats stats{};
     uint64_t launches = 0;              // launches outside the slot-pool iterations
     bool stage_timing = false;
-    int refill = 16;                    // idle lanes that trigger a warp refill
+    int refill = 20;                    // idle lanes that trigger a warp refill
     int tri_mode = 0;                   // traversal triangle policy (see gb_tuning)
     int blocks_per_sm = 0;              // resident traversal blocks per SM (0 = occupancy limit)
     int stack_depth = 32;               // traversal stack entries (24 or 32)

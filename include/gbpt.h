@@ -441,7 +441,7 @@ typedef struct {
 
 /* Knobs of the wavefront (chosen by the autotuner); 0 keeps a value:
  *   refill    idle lanes (1..32) at which a closest-hit traversal warp
- *             fetches new rays (any-hit warps refill at 12)
+ *             fetches new rays, default 20 (any-hit warps refill at 12)
  *   slots     paths in flight (queue capacity), default 2^24 (a frame
  *             allocates min(its paths, slots); 256 B of path state per slot;
  *             the adjoint replay uses at most 2^22)
