@@ -307,7 +307,7 @@ def c0_leg(ctx, args, torch, flush, with_cpu: bool):
 def batch_leg(ctx, args, torch, flush, dist):
     """Mixed-scene batch (64 icosphere soups, log-uniform 1K-500K triangles,
     64^2-512^2 pixels, 4/16/64 spp, 1-4 lights, 6 bounces): knobs picked by
-    gb_autotune on a 4-spp proxy frame, then the batched frame
+    gb_autotune on the whole batch frame, then the batched frame
     (gb_render_batch) against the plain form (one gb_render per scene, in
     sequence), both device-timed with L2 flushed between steps, and against
     the sum of each scene's best frame time rendered alone.  Images of the
@@ -326,7 +326,7 @@ def batch_leg(ctx, args, torch, flush, dist):
     ptrs = [o.data_ptr() for o in outs]
     saved = ctx.get_tuning()
     t0 = time.perf_counter()
-    tuning, tune_ms = ctx.autotune(jobs, proxy_spp=4, repeats=3)
+    tuning, tune_ms = ctx.autotune(jobs, proxy_spp=0, repeats=3)
     tune_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
 
@@ -399,7 +399,7 @@ def batch_leg(ctx, args, torch, flush, dist):
             "workload": {"scenes": len(mixed), "triangles_total": int(sum(tris)), "triangles_min": int(min(tris)),
                          "triangles_max": int(max(tris)), "resolutions": [64, 128, 256, 512], "spp": [4, 16, 64],
                          "max_bounces": 6, "generate_s": gen_s, "bvh_build_and_upload_s": build_s},
-            "autotune": {"tuning": tuning, "proxy_frame_ms": tune_ms, "seconds": tune_s, "proxy_spp": 4}}
+            "autotune": {"tuning": tuning, "frame_ms": tune_ms, "seconds": tune_s, "proxy_spp": None}}
 
 
 def adjoint_leg(ctx, scene, sc, args, torch, flush, orc):
