@@ -740,6 +740,10 @@ def run_gbpt(args, rank, world):
     peak, peak_kind = measured_peaks()
     achieved = closest_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
     achieved_trav = trav_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
+    # FP32 work of the traversal: ~24 flops per child slab test (8 children
+    # per node visit), ~30 per triangle test
+    trav_flops = ist["closest_node_visits"] * 8 * 24 + ist["closest_tri_tests"] * 30
+    fp32_tflops = trav_flops / (ext_ms / 1e3) / 1e12 if ext_ms > 0 else None
     rays = ist["camera_rays"] + ist["extension_rays"] + ist["shadow_rays"]
     mrays = rays / (total_ms / args.steps / 1e3) / 1e6
 
@@ -778,7 +782,10 @@ def run_gbpt(args, rank, world):
                                             "frac": (achieved_trav / peak) if achieved_trav else None,
                                             "bytes_per_launch": trav_bytes / max(1.0, ext_launches),
                                             "bytes_model": "node visits*80 + tri tests*36 + 48 per ray"},
-                         "closest_hits_per_frame": int(hits), "misses_per_frame": int(misses)},
+                         "closest_hits_per_frame": int(hits), "misses_per_frame": int(misses),
+                         "fp32": {"achieved_tflops": fp32_tflops,
+                                  "model": "node visits*8*24 + tri tests*30 flops (slab tests of 8 children, "
+                                           "Moller-Trumbore), no measured FP32 peak to divide by"}},
             "clocks": clocks,
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": W * H * 3 * 4},
