@@ -6,8 +6,8 @@
 // cudaMalloc on first use.  Some callers cannot allow that: a render loop
 // that runs while other work owns the device's memory through its own pool
 // (cudaMalloc and cudaFree synchronise the whole device and fragment such a
-// pool), or code on a path where the host must not block in the driver's
-// allocator.  For them this entry point keeps that state in one
+// pool), or code on a path where the host must not block in the CUDA
+// driver's allocator.  For them this entry point keeps that state in one
 // file-scope __device__ array of fixed size instead.  Every GPU that loads
 // the library holds the array until the process exits.
 //

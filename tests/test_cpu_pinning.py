@@ -7,7 +7,7 @@ its materialBRDF (principledMaterial.h, simpleMaterial.h, material-wrapper.h)
 driven through the sample_material / evaluate_material sequence of
 hybrid-pt.cpp:330-371, and rta::generate_arealight_sample of
 arealight-sampler-cpu.cpp.  The reference evaluates sin/cos through libm and
-some intermediate products in double; this build uses its own float
+some intermediate products in double; the library uses its own float
 sin/cos(2 pi u) and float arithmetic, so shading agrees to a relative 1e-4 (every case outside it
 is shown to be ill-conditioned: one ulp of input covers the difference)
 while the area-light sample (only + - * / sqrt) agrees bit for bit.
@@ -50,8 +50,8 @@ def test_shade_matches_reference_golden():
     """Relative 1e-4 on the pdf and BRDF values, 2e-5 on directions.  A case
     outside that must be ill-conditioned: some one-ulp change of one input
     component (the reference evaluates sin/cos through libm and some products
-    in double, this build in float) moves this build's result to within 1e-4
-    of the reference's.  Such cases are logged and must stay rare."""
+    in double, the library in float) moves the library's result to within
+    1e-4 of the reference's.  Such cases are logged and must stay rare."""
     from oracle import oracle
     g = np.load(GOLDEN / "shade_cases.npz")
     ref = g["out"]
