@@ -73,7 +73,7 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> Path:
     # experimental compile options (GBPT_<name> in the environment -> -DGB_<name>)
     knobs = ("TRAV_MIN_BLOCKS", "SMEM_STACK", "PREFETCH", "SPLIT_NEE", "SHADE_MIN_BLOCKS", "STREAM_MIN_BLOCKS",
              "WIDE_STREAM_GRIDS", "SHADOW_SPLIT", "FUSED_RESTART", "TRI_NOALLOC", "NODE_L2_128", "SHADOW_REFILL", "SHADOW_MIN_BLOCKS",
-             "REC_EVICT_FIRST", "NODE_FOLD", "SHADE_EVICT_FIRST", "NODE_L2_PERSIST", "HIT_LINE_KEEP", "TREE_WINDOW")
+             "REC_EVICT_FIRST", "NODE_FOLD", "SHADE_EVICT_FIRST", "NODE_L2_PERSIST", "HIT_LINE_KEEP", "TREE_WINDOW", "WIDE_GRID_DIV")
     flags = " ".join(f"GB_{k}={os.environ.get('GBPT_' + k, '')}" for k in knobs)
     stamp = LIB.with_suffix(".flags")
     if not stamp.exists() or stamp.read_text() != flags:

@@ -1872,13 +1872,20 @@ cudaError_t k_launch_shadow(const Frame& F, const RenderParams& P, bool instrume
 }
 
 // Grid of the streaming per-path kernels (k_shade, k_regen): persistent for
-// pools of up to 2^20 slots, one thread per slot above that (or always,
-// with GB_WIDE_STREAM_GRIDS).  On the 1M-triangle frame with 2^21 slots the
-// wide grid shades in 7.0 ms against 8.0 (931 against 914 Mpaths/s); on the
-// 256x256 16-spp Cornell frame (2^20 slots) the persistent grid in 0.39 ms
-// against 0.47.
+// pools of up to 2^20 slots, one thread per four slots above that (or
+// always, with GB_WIDE_STREAM_GRIDS), each thread taking every
+// (grid size)-th queue entry.  On the 1M-triangle frame with 2^21 slots a
+// thread per slot shades in 7.0 ms against 8.0 for the persistent grid; with
+// 2^24 slots a quarter of that grid (an iteration shades ~3 M hits) in
+// 4.8 ms against 6.2 for a thread per slot (1071 against 1058 Mpaths/s); on
+// the 256x256 16-spp Cornell frame (2^20 slots) the persistent grid in
+// 0.39 ms against 0.47.
+#ifndef GB_WIDE_GRID_DIV
+#define GB_WIDE_GRID_DIV 4  // the wide grid has nslots / GB_WIDE_GRID_DIV threads
+#endif
 inline int stream_grid(int persistent, int nslots) {
-    return (GB_WIDE_STREAM_GRIDS || nslots > (1 << 20)) ? std::max(1, blocks_for(nslots)) : persistent;
+    return (GB_WIDE_STREAM_GRIDS || nslots > (1 << 20)) ? std::max(1, blocks_for(nslots / GB_WIDE_GRID_DIV))
+                                                          : persistent;
 }
 
 template <int MODE, bool TEX>
