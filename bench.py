@@ -32,7 +32,7 @@ sys.path.insert(0, str(ROOT))
 # DRAM bytes (read + write) k_extend moves per closest-hit ray on the 1M-triangle
 # workload with the default slot pool, from an ncu capture of a whole 16-spp
 # frame with a warm L2 (profiles/k_extend_dram_traffic_icospheres1m_16spp.txt).
-K_EXTEND_DRAM_BYTES_PER_RAY = 1245.4
+K_EXTEND_DRAM_BYTES_PER_RAY = 1246.3
 METRIC = "Mpaths/s"
 
 
