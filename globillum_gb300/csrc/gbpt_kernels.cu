@@ -116,7 +116,7 @@ __device__ __forceinline__ RayInv make_ray(v3 o, v3 d) {
 // allocation (GB_TRI_NOALLOC), nodes with a 128-byte L2 fetch (GB_NODE_L2_128);
 // plain __ldg otherwise.
 #ifndef GB_SHADOW_MIN_BLOCKS
-#define GB_SHADOW_MIN_BLOCKS GB_TRAV_MIN_BLOCKS  // resident any-hit blocks per SM (register budget)
+#define GB_SHADOW_MIN_BLOCKS 8  // resident any-hit blocks per SM (register budget)
 #endif
 #ifndef GB_SHADOW_REFILL
 #define GB_SHADOW_REFILL 12  // refill threshold of the any-hit kernel (0: the frame's refill)
